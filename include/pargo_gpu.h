@@ -1,0 +1,189 @@
+/*
+ * pargo_gpu.h -- C ABI of the GB300 focal raster operators (libpargo_gpu.so).
+ *
+ * The PaRGO reference runs its focal operators through
+ * RasterOperator<double>::Run() -> Work() (gpro/rasterOperator.h:148-362), a
+ * per-cell virtual Operator() sweep over a CellSpace with halos.  Each entry
+ * point below replaces one such Run() for one operator:
+ *
+ *   pargo_slope / pargo_slope_d8  SlopeOperator::Run   apps/morphology/slope/slopeOperator.cpp:51-139
+ *   pargo_d8 / pargo_slope_d8     D8Operator::Run      apps/hydrology/flowdird8/d8Operator.cpp:28-101
+ *   pargo_fill                    PitRemoveOperator::Run apps/hydrology/pitremove/pitRemoveOperator.cpp:26-72
+ *   pargo_sca                     SCAOperator::Run     apps/hydrology/scad8/scaOperator.cpp:37-131
+ *   pargo_nbr_parse               operator>>(istream&, Neighborhood&) gpro/neighborhood.h:626-662
+ *                                 + Neighborhood::_initCoords checks :110-194
+ *
+ * and three additions with no reference counterpart: batched slope+D8 over
+ * many rasters in one launch, and the forward/backward (adjoint) pair of Horn
+ * slope.
+ *
+ * Conventions
+ *  - Plain C: pointers, sizes, enums.  `stream` is a cudaStream_t passed as
+ *    void* (NULL = the legacy default stream).
+ *  - A raster is row-major with a row pitch in bytes, like CellSpace::_matrix
+ *    (gpro/cellSpace.h:230) but with an explicit pitch.  Every raster carries
+ *    its own nodata value: inputs use it to detect nodata (|v - nodata| < Eps
+ *    with the reference's Eps), outputs write it into nodata cells.
+ *  - Buffers may live on the device or on the host.  Host buffers are copied
+ *    through the context's device staging and the call returns after the
+ *    results are back (synchronous); all-device calls are stream-ordered and
+ *    return without waiting.
+ *  - The caller owns every buffer.  The library owns only the scratch of a
+ *    context (staging, work queues, counters); it grows on demand and is reused.
+ *  - Errors are status codes; pargo_last_error() gives the message.  There is
+ *    no CPU fallback: without a usable GPU every compute call fails with
+ *    PARGO_ERR_NO_DEVICE or PARGO_ERR_CUDA.
+ *  - One host thread per context at a time.
+ */
+#ifndef PARGO_GPU_H
+#define PARGO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PARGO_ABI_VERSION 1
+
+typedef enum pargo_status {
+    PARGO_OK = 0,
+    PARGO_ERR_INVALID_ARG = 1,     /* bad pointer, size, dtype, pitch or option */
+    PARGO_ERR_NBR_UNSUPPORTED = 2, /* the operator needs a 3x3 Moore neighbourhood */
+    PARGO_ERR_NOT_CONVERGED = 3,   /* fill hit its round cap before the fixpoint */
+    PARGO_ERR_CYCLE = 4,           /* SCA: some in-degree is never consumed */
+    PARGO_ERR_CUDA = 5,            /* a CUDA runtime or launch error */
+    PARGO_ERR_NO_DEVICE = 6,       /* no CUDA device */
+    PARGO_ERR_OUT_OF_MEMORY = 7,
+    PARGO_ERR_DEVICE_TIMEOUT = 8   /* a bounded device-side wait gave up */
+} pargo_status;
+
+typedef enum pargo_dtype {
+    PARGO_F32 = 0,
+    PARGO_F64 = 1,
+    PARGO_I8 = 2,
+    PARGO_I16 = 3,
+    PARGO_I32 = 4
+} pargo_dtype;
+
+typedef enum pargo_location { PARGO_HOST = 0, PARGO_DEVICE = 1 } pargo_location;
+
+typedef struct pargo_raster {
+    void* data;       /* cell (0, 0) */
+    int32_t dtype;    /* pargo_dtype */
+    int32_t location; /* pargo_location */
+    int64_t rows;
+    int64_t cols;
+    int64_t pitch;    /* bytes from one row to the next; 0 = cols * element size */
+    double nodata;    /* MetaData::noData (gpro/metaData.h:55) */
+    double cellsize;  /* MetaData::cellSize; the reference stores it as float
+                         (gpro/metaData.h:56) and the operators use that float
+                         value, so it is rounded to float before use */
+} pargo_raster;
+
+/* A parsed .nbr neighbourhood: the cell count and the MBR of the offsets.
+ * The focal operators use only int(sqrt(count))/2 (slopeOperator.cpp:55) and
+ * the work rectangle the MBR implies (gpro/neighborhood.h:423-467). */
+typedef struct pargo_nbr {
+    int32_t count;
+    int32_t min_row, min_col, max_row, max_col;
+} pargo_nbr;
+
+/* SlopeAlgor, apps/morphology/slope/slopeOperator.h:18-26 */
+typedef enum pargo_slope_method {
+    PARGO_SLOPE_FD = 0, PARGO_SLOPE_FFD = 1, PARGO_SLOPE_MD = 2, PARGO_SLOPE_SD = 3,
+    PARGO_SLOPE_SFD = 4, PARGO_SLOPE_TFD = 5, PARGO_SLOPE_TFDW = 6
+} pargo_slope_method;
+
+typedef enum pargo_slope_units {
+    PARGO_SLOPE_RATIO = 0,  /* rise/run, as the reference writes it (slopeOperator.cpp:86) */
+    PARGO_SLOPE_DEGREES = 1 /* atan(rise/run) in degrees */
+} pargo_slope_units;
+
+typedef enum pargo_sca_contract {
+    PARGO_SCA_CONVERGED = 0, /* the reference rule iterated until every in-degree is consumed */
+    PARGO_SCA_SHIPPED = 1    /* what the shipped operator's single accumulation sweep leaves (scaOperator.cpp:126) */
+} pargo_sca_contract;
+
+typedef struct pargo_fill_opts {
+    double gap;         /* reference: 0.0005 (pitRemoveOperator.cpp:36) */
+    double init_level;  /* reference: 10000.0 (pitRemoveOperator.cpp:41) */
+    int64_t max_rounds; /* cap on relaxation rounds; <= 0 = no cap */
+} pargo_fill_opts;
+
+typedef struct pargo_fill_stats {
+    int64_t rounds;       /* worklist rounds run */
+    int64_t tile_visits;  /* tiles relaxed, summed over rounds */
+    int64_t raised_cells; /* cells whose filled level is above the DEM */
+} pargo_fill_stats;
+
+typedef struct pargo_ctx pargo_ctx;
+
+/* Context on CUDA device `device`. */
+pargo_status pargo_create(int device, pargo_ctx** out);
+pargo_status pargo_destroy(pargo_ctx* ctx);
+const char* pargo_last_error(const pargo_ctx* ctx);
+int pargo_abi_version(void);
+
+/* Parse .nbr text: a count N, then N lines "dRow dCol weight"; N >= 100 means
+ * an automatic sqrt(N) x sqrt(N) square (neighborhood.h:626-662).  Rejects an
+ * empty set, a set without (0, 0) and duplicates (neighborhood.h:110-140). */
+pargo_status pargo_nbr_parse(const char* text, pargo_nbr* out);
+
+/* Slope of `dem` into `slope` (F32 or F64).  dem: F32 or F64. */
+pargo_status pargo_slope(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, const pargo_nbr* nbr,
+                         int method, int units, void* stream);
+
+/* D8 codes of `dem` into `d8`.  dir_type 8: receiver index 0..8 of the 3x3
+ * window, -1 flat/pit (d8Operator.cpp:78-88); any other dir_type: the
+ * ArcGIS-style bit sum (:89-97).  d8: I8 (dir_type 8 only), I16, I32, F32 or F64. */
+pargo_status pargo_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* d8, const pargo_nbr* nbr,
+                      int dir_type, void* stream);
+
+/* Fused slope + D8: one read of the DEM, either output may be NULL. */
+pargo_status pargo_slope_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
+                            const pargo_nbr* nbr, int method, int units, int dir_type, void* stream);
+
+/* Planchon-Darboux pit removal: the fixpoint the reference's Gauss-Seidel
+ * sweeps reach (any visiting order reaches the same one).  dem: F32;
+ * wdem: F64 (the reference's values) or F32 (those values rounded to float).
+ * opts may be NULL (reference constants); stats may be NULL. */
+pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
+                        const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream);
+
+/* D8 specific catchment area (upslope cell count, as the reference computes
+ * it).  d8: F64 codes as the reference writes them, or I8/I16/I32 codes with
+ * the raster's nodata as sentinel; sca: F64 or F32. */
+pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr,
+                       int contract, void* stream);
+
+/* Batched fused slope + D8 over `count` independent rasters in one persistent
+ * launch; slopes / d8s may be NULL (no such output) and all rasters must be on
+ * the device. */
+pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* slopes,
+                                  pargo_raster* d8s, const pargo_nbr* nbr, int method, int units, int dir_type,
+                                  void* stream);
+
+/* Differentiable Horn (FD) slope.  Forward: slope of z into `slope`.
+ * Backward: given dL/dslope per cell (`gslope`, F32), accumulate dL/dz into
+ * `gz` (F32, overwritten).  Subgradient convention: at zero slope the
+ * derivative is taken as 0; windows touching nodata contribute nothing. */
+pargo_status pargo_slope_fwd(pargo_ctx* ctx, const pargo_raster* z, pargo_raster* slope, const pargo_nbr* nbr,
+                             void* stream);
+pargo_status pargo_slope_bwd(pargo_ctx* ctx, const pargo_raster* z, const pargo_raster* gslope, pargo_raster* gz,
+                             const pargo_nbr* nbr, void* stream);
+
+/* Fused forward + backward of L = sum over cells of (slope(z) - slope(z_ref))^2:
+ * writes dL/dz into `gz` (F32) and L into *loss (may be NULL). */
+pargo_status pargo_slope_loss_grad(pargo_ctx* ctx, const pargo_raster* z, const pargo_raster* z_ref,
+                                   pargo_raster* gz, double* loss, const pargo_nbr* nbr, void* stream);
+
+/* Number of D8 cells of the last slope+D8/D8 call that took the exact FP64
+ * path (the FP32 decision was not certified), for diagnostics. */
+int64_t pargo_last_d8_fallbacks(const pargo_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARGO_GPU_H */

@@ -1,0 +1,214 @@
+"""ctypes binding of the C ABI in ``include/pargo_gpu.h`` (``lib/libpargo_gpu.so``).
+
+This is plumbing for Python callers, tests and the benchmark: every call goes
+straight to the C entry point.  Rasters can be numpy arrays (host buffers,
+staged by the library) or torch tensors (device buffers used in place).  The
+library must be built; importing this module without it raises
+``NativeLibraryMissing`` -- there is no Python or CPU fallback.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _paths
+
+PARGO_OK = 0
+STATUS_NAMES = {
+    0: "PARGO_OK", 1: "PARGO_ERR_INVALID_ARG", 2: "PARGO_ERR_NBR_UNSUPPORTED", 3: "PARGO_ERR_NOT_CONVERGED",
+    4: "PARGO_ERR_CYCLE", 5: "PARGO_ERR_CUDA", 6: "PARGO_ERR_NO_DEVICE", 7: "PARGO_ERR_OUT_OF_MEMORY",
+    8: "PARGO_ERR_DEVICE_TIMEOUT",
+}
+F32, F64, I8, I16, I32 = 0, 1, 2, 3, 4
+HOST, DEVICE = 0, 1
+SLOPE_FD, SLOPE_FFD, SLOPE_MD, SLOPE_SD, SLOPE_SFD, SLOPE_TFD, SLOPE_TFDW = range(7)
+RATIO, DEGREES = 0, 1
+SCA_CONVERGED, SCA_SHIPPED = 0, 1
+
+_NP_DTYPES = {np.dtype(np.float32): F32, np.dtype(np.float64): F64, np.dtype(np.int8): I8,
+              np.dtype(np.int16): I16, np.dtype(np.int32): I32}
+
+
+class PargoError(RuntimeError):
+    def __init__(self, status, message):
+        self.status = status
+        self.status_name = STATUS_NAMES.get(status, str(status))
+        super().__init__("%s: %s" % (self.status_name, message))
+
+
+class Raster(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("dtype", ctypes.c_int32), ("location", ctypes.c_int32),
+                ("rows", ctypes.c_int64), ("cols", ctypes.c_int64), ("pitch", ctypes.c_int64),
+                ("nodata", ctypes.c_double), ("cellsize", ctypes.c_double)]
+
+
+class Nbr(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_int32), ("min_row", ctypes.c_int32), ("min_col", ctypes.c_int32),
+                ("max_row", ctypes.c_int32), ("max_col", ctypes.c_int32)]
+
+
+class FillOpts(ctypes.Structure):
+    _fields_ = [("gap", ctypes.c_double), ("init_level", ctypes.c_double), ("max_rounds", ctypes.c_int64)]
+
+
+class FillStats(ctypes.Structure):
+    _fields_ = [("rounds", ctypes.c_int64), ("tile_visits", ctypes.c_int64), ("raised_cells", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        L = ctypes.CDLL(_paths.require(_paths.GPU_SO))
+        P = ctypes.POINTER
+        vp, i, st = ctypes.c_void_p, ctypes.c_int, ctypes.c_int
+        R = P(Raster)
+        N = P(Nbr)
+        L.pargo_create.argtypes = [i, P(vp)]
+        L.pargo_destroy.argtypes = [vp]
+        L.pargo_last_error.argtypes = [vp]
+        L.pargo_last_error.restype = ctypes.c_char_p
+        L.pargo_abi_version.restype = i
+        L.pargo_nbr_parse.argtypes = [ctypes.c_char_p, N]
+        L.pargo_slope.argtypes = [vp, R, R, N, i, i, vp]
+        L.pargo_d8.argtypes = [vp, R, R, N, i, vp]
+        L.pargo_slope_d8.argtypes = [vp, R, R, R, N, i, i, i, vp]
+        L.pargo_fill.argtypes = [vp, R, R, N, P(FillOpts), P(FillStats), vp]
+        L.pargo_sca.argtypes = [vp, R, R, N, i, vp]
+        L.pargo_batch_slope_d8.argtypes = [vp, i, R, R, R, N, i, i, i, vp]
+        L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
+        L.pargo_slope_bwd.argtypes = [vp, R, R, R, N, vp]
+        L.pargo_slope_loss_grad.argtypes = [vp, R, R, R, P(ctypes.c_double), N, vp]
+        L.pargo_last_d8_fallbacks.argtypes = [vp]
+        L.pargo_last_d8_fallbacks.restype = ctypes.c_int64
+        for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
+                     "pargo_fill", "pargo_sca", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
+                     "pargo_slope_loss_grad"):
+            getattr(L, name).restype = st
+        _lib = L
+    return _lib
+
+
+def nbr_parse(text):
+    n = Nbr()
+    rc = lib().pargo_nbr_parse(text.encode() if isinstance(text, str) else text, ctypes.byref(n))
+    if rc:
+        raise PargoError(rc, "invalid neighbourhood text")
+    return n
+
+
+MOORE = "9\n0 0 1.0\n-1 -1 1.0\n-1 0 1.0\n-1 1 1.0\n0 -1 1.0\n0 1 1.0\n1 -1 1.0\n1 0 1.0\n1 1 1.0\n"
+
+
+def raster(a, nodata=-9999.0, cellsize=1.0):
+    """Describe a 2-D numpy array (host) or torch tensor (its own device) as a
+    pargo_raster.  The array must stay alive while the raster is in use."""
+    try:
+        import torch
+        is_t = isinstance(a, torch.Tensor)
+    except ImportError:  # pragma: no cover
+        is_t = False
+    if is_t:
+        if a.dim() != 2 or a.stride(1) != 1:
+            raise ValueError("raster tensors must be 2-D with unit column stride")
+        dt = {"torch.float32": F32, "torch.float64": F64, "torch.int8": I8, "torch.int16": I16,
+              "torch.int32": I32}[str(a.dtype)]
+        loc = DEVICE if a.is_cuda else HOST
+        return Raster(a.data_ptr(), dt, loc, a.shape[0], a.shape[1], a.stride(0) * a.element_size(),
+                      float(nodata), float(cellsize))
+    if a.ndim != 2 or a.strides[1] != a.itemsize:
+        raise ValueError("raster arrays must be 2-D with unit column stride")
+    return Raster(a.ctypes.data, _NP_DTYPES[a.dtype], HOST, a.shape[0], a.shape[1], a.strides[0],
+                  float(nodata), float(cellsize))
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream  # torch.cuda.Stream
+
+
+class Context:
+    """A pargo_ctx on one CUDA device (scratch, staging, counters)."""
+
+    def __init__(self, device=0):
+        self._p = ctypes.c_void_p()
+        rc = lib().pargo_create(device, ctypes.byref(self._p))
+        if rc:
+            raise PargoError(rc, "pargo_create(%d) failed" % device)
+        self.device = device
+        self.moore = nbr_parse(MOORE)
+
+    def close(self):
+        if self._p:
+            lib().pargo_destroy(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc:
+            raise PargoError(rc, lib().pargo_last_error(self._p).decode(errors="replace"))
+
+    def _nbr(self, nbr):
+        return ctypes.byref(nbr if nbr is not None else self.moore)
+
+    @property
+    def last_d8_fallbacks(self):
+        return lib().pargo_last_d8_fallbacks(self._p)
+
+    def slope_d8(self, dem, slope=None, d8=None, method=SLOPE_FD, units=RATIO, dir_type=8, nbr=None, stream=None):
+        """Fused slope + D8; dem/slope/d8 are Raster descriptors (see raster())."""
+        self._check(lib().pargo_slope_d8(self._p, ctypes.byref(dem), ctypes.byref(slope) if slope else None,
+                                         ctypes.byref(d8) if d8 else None, self._nbr(nbr), method, units, dir_type,
+                                         _stream_ptr(stream)))
+
+    def slope(self, dem, slope, method=SLOPE_FD, units=RATIO, nbr=None, stream=None):
+        self._check(lib().pargo_slope(self._p, ctypes.byref(dem), ctypes.byref(slope), self._nbr(nbr), method, units,
+                                      _stream_ptr(stream)))
+
+    def d8(self, dem, d8, dir_type=8, nbr=None, stream=None):
+        self._check(lib().pargo_d8(self._p, ctypes.byref(dem), ctypes.byref(d8), self._nbr(nbr), dir_type,
+                                   _stream_ptr(stream)))
+
+    def fill(self, dem, wdem, gap=0.0005, init_level=10000.0, max_rounds=0, nbr=None, stream=None):
+        opts = FillOpts(gap, init_level, max_rounds)
+        stats = FillStats()
+        self._check(lib().pargo_fill(self._p, ctypes.byref(dem), ctypes.byref(wdem), self._nbr(nbr),
+                                     ctypes.byref(opts), ctypes.byref(stats), _stream_ptr(stream)))
+        return stats
+
+    def sca(self, d8, sca, contract=SCA_CONVERGED, nbr=None, stream=None):
+        self._check(lib().pargo_sca(self._p, ctypes.byref(d8), ctypes.byref(sca), self._nbr(nbr), contract,
+                                    _stream_ptr(stream)))
+
+    def batch_slope_d8(self, dems, slopes=None, d8s=None, method=SLOPE_FD, units=RATIO, dir_type=8, nbr=None,
+                       stream=None):
+        n = len(dems)
+        D = (Raster * n)(*dems)
+        S = (Raster * n)(*slopes) if slopes else None
+        C = (Raster * n)(*d8s) if d8s else None
+        self._check(lib().pargo_batch_slope_d8(self._p, n, D, S, C, self._nbr(nbr), method, units, dir_type,
+                                               _stream_ptr(stream)))
+
+    def slope_fwd(self, z, slope, nbr=None, stream=None):
+        self._check(lib().pargo_slope_fwd(self._p, ctypes.byref(z), ctypes.byref(slope), self._nbr(nbr),
+                                          _stream_ptr(stream)))
+
+    def slope_bwd(self, z, gslope, gz, nbr=None, stream=None):
+        self._check(lib().pargo_slope_bwd(self._p, ctypes.byref(z), ctypes.byref(gslope), ctypes.byref(gz),
+                                          self._nbr(nbr), _stream_ptr(stream)))
+
+    def slope_loss_grad(self, z, zref, gz, want_loss=True, nbr=None, stream=None):
+        loss = ctypes.c_double(0.0)
+        self._check(lib().pargo_slope_loss_grad(self._p, ctypes.byref(z), ctypes.byref(zref), ctypes.byref(gz),
+                                                ctypes.byref(loss) if want_loss else None, self._nbr(nbr),
+                                                _stream_ptr(stream)))
+        return loss.value if want_loss else None

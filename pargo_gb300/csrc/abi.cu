@@ -1,0 +1,892 @@
+// abi.cu -- the extern "C" entry points declared in include/pargo_gpu.h.
+//
+// Host side of every operator: argument checks (mirroring the reference's own
+// checks where it has them), host<->device staging for host buffers, exact
+// nodata bands, TMA descriptors, kernel dispatch, CUDA-graph-captured fill
+// rounds.  No CPU compute path exists: every result is produced by a kernel.
+
+#include <cudaTypedefs.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdarg>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace pargo;
+
+struct pargo_ctx {
+    int device = 0;
+    int num_sms = 0;
+    std::string err;
+    cudaStream_t own = nullptr;  // stream for captured fill rounds
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    // grow-only device scratch slots
+    struct Slot {
+        void* p = nullptr;
+        size_t n = 0;
+    };
+    Slot slots[24];
+    // pinned host scratch (counter read-back, table staging)
+    void* pinned = nullptr;
+    size_t pinned_n = 0;
+    unsigned long long* d_counters = nullptr;  // [0] fallbacks [1] visits [2] changed [3] raised
+    int* d_error = nullptr;
+    int64_t last_fallbacks = 0;
+    // fill graph cache
+    cudaGraphExec_t fill_graph = nullptr;
+    std::string fill_graph_key;
+    // batch table cache
+    std::string batch_key;
+};
+
+enum SlotId {
+    kSlotIn0 = 0, kSlotIn1, kSlotOut0, kSlotOut1, kSlotFillW, kSlotFillLists, kSlotFillQueued,
+    kSlotScaIndeg, kSlotScaConv, kSlotScaShip, kSlotScaFlags, kSlotScaCounters, kSlotBatchMaps,
+    kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut
+};
+
+namespace {
+
+pargo_status fail(pargo_ctx* ctx, pargo_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    return st;
+}
+
+pargo_status cuda_fail(pargo_ctx* ctx, cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(ctx, PARGO_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+        return fail(ctx, PARGO_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+    return fail(ctx, PARGO_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CU(ctx, call)                                          \
+    do {                                                       \
+        cudaError_t e__ = (call);                              \
+        if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call); \
+    } while (0)
+
+void* slot(pargo_ctx* ctx, int id, size_t bytes, cudaError_t* err) {
+    auto& s = ctx->slots[id];
+    *err = cudaSuccess;
+    if (bytes == 0) bytes = 16;
+    if (s.n >= bytes) return s.p;
+    if (s.p) {
+        cudaDeviceSynchronize();
+        cudaFree(s.p);
+        s.p = nullptr;
+        s.n = 0;
+    }
+    size_t want = bytes + bytes / 8;
+    *err = cudaMalloc(&s.p, want);
+    if (*err != cudaSuccess) {
+        s.p = nullptr;
+        return nullptr;
+    }
+    s.n = want;
+    return s.p;
+}
+
+void* pinned(pargo_ctx* ctx, size_t bytes, cudaError_t* err) {
+    *err = cudaSuccess;
+    if (ctx->pinned_n >= bytes) return ctx->pinned;
+    if (ctx->pinned) {
+        cudaDeviceSynchronize();
+        cudaFreeHost(ctx->pinned);
+    }
+    ctx->pinned = nullptr;
+    ctx->pinned_n = 0;
+    *err = cudaMallocHost(&ctx->pinned, bytes);
+    if (*err != cudaSuccess) return nullptr;
+    ctx->pinned_n = bytes;
+    return ctx->pinned;
+}
+
+int64_t row_bytes(const pargo_raster* r) { return r->cols * (int64_t)elem_size(r->dtype); }
+int64_t pitch_of(const pargo_raster* r) { return r->pitch ? r->pitch : row_bytes(r); }
+
+pargo_status check_raster(pargo_ctx* ctx, const pargo_raster* r, const char* name) {
+    if (!r) return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: null raster", name);
+    if (elem_size(r->dtype) == 0) return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: unknown dtype %d", name, r->dtype);
+    if (r->location != PARGO_HOST && r->location != PARGO_DEVICE)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: unknown location %d", name, r->location);
+    if (r->rows < 0 || r->cols < 0) return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: negative size", name);
+    if (r->rows > 0 && r->cols > 0 && !r->data) return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: null data", name);
+    if (r->pitch != 0 && r->pitch < row_bytes(r))
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: pitch %lld below row size %lld", name, (long long)r->pitch,
+                    (long long)row_bytes(r));
+    if (r->pitch % elem_size(r->dtype) != 0)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: pitch not a multiple of the element size", name);
+    if ((uintptr_t)r->data % elem_size(r->dtype) != 0)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: data not aligned to its element size", name);
+    return PARGO_OK;
+}
+
+// The neighbourhood the focal operators accept: iNeighborCells = int(sqrt(n))/2
+// must be 1 (the operators read exactly d[0..8], slopeOperator.cpp:55-73) and
+// the MBR must be the 3x3 square (the work rectangle, neighborhood.h:447-448).
+pargo_status check_nbr(pargo_ctx* ctx, const pargo_nbr* nbr) {
+    if (!nbr) return PARGO_OK;  // NULL = Moore
+    const int half = ((int)sqrt((double)nbr->count)) / 2;
+    if (half != 1 || nbr->min_row != -1 || nbr->min_col != -1 || nbr->max_row != 1 || nbr->max_col != 1)
+        return fail(ctx, PARGO_ERR_NBR_UNSUPPORTED,
+                    "neighbourhood of %d cells with MBR [%d,%d]x[%d,%d]: the focal operators need the 3x3 Moore "
+                    "window (int(sqrt(n))/2 == 1)",
+                    nbr->count, nbr->min_row, nbr->max_row, nbr->min_col, nbr->max_col);
+    return PARGO_OK;
+}
+
+// Neighborhood::calcWorkBR rejects rasters smaller than the window
+// (neighborhood.h:440-446).
+pargo_status check_dims(pargo_ctx* ctx, const pargo_raster* r) {
+    if (r->rows < 3 || r->cols < 3)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "raster %lldx%lld is smaller than the 3x3 neighbourhood",
+                    (long long)r->rows, (long long)r->cols);
+    if (r->rows > INT32_MAX || r->cols > INT32_MAX)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "raster dimensions above 2^31-1");
+    return PARGO_OK;
+}
+
+pargo_status check_same(pargo_ctx* ctx, const pargo_raster* a, const pargo_raster* b, const char* name) {
+    if (a->rows != b->rows || a->cols != b->cols)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: %lldx%lld does not match the input %lldx%lld", name,
+                    (long long)b->rows, (long long)b->cols, (long long)a->rows, (long long)a->cols);
+    return PARGO_OK;
+}
+
+// ---- exact nodata bands: { x : |(double)x - nodata| < eps } as [lo, hi] ----
+uint32_t fkey(float x) {
+    uint32_t b;
+    memcpy(&b, &x, 4);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+float fval(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float x;
+    memcpy(&x, &b, 4);
+    return x;
+}
+uint64_t dkey_h(double x) {
+    uint64_t b;
+    memcpy(&b, &x, 8);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+double dval_h(uint64_t k) {
+    uint64_t b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
+}
+
+template <typename K, typename T, typename ToV>
+void band_search(K kmin, K kmax, double nodata, double eps, ToV val, T* lo, T* hi) {
+    // f(k) = fl64((double)val(k) - nodata) is non-decreasing in k.
+    auto f = [&](K k) { return (double)val(k) - nodata; };
+    // smallest k with f(k) > -eps
+    K a = kmin, b = kmax;
+    if (!(f(b) > -eps)) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
+    while (a < b) {
+        K m = a + (b - a) / 2;
+        if (f(m) > -eps) b = m; else a = m + 1;
+    }
+    K l = a;
+    // largest k with f(k) < eps
+    a = kmin; b = kmax;
+    if (!(f(a) < eps)) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
+    while (a < b) {
+        K m = a + (b - a + 1) / 2;
+        if (f(m) < eps) a = m; else b = m - 1;
+    }
+    K h = a;
+    if (l > h) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
+    *lo = val(l);
+    *hi = val(h);
+}
+
+Band<float> float_band(double nodata, double eps) {
+    Band<float> b;
+    // keys of -inf .. +inf (NaNs excluded)
+    band_search<uint32_t, float>(fkey(-INFINITY), fkey(INFINITY), nodata, eps, fval, &b.lo, &b.hi);
+    return b;
+}
+Band<double> double_band(double nodata, double eps) {
+    Band<double> b;
+    band_search<uint64_t, double>(dkey_h(-INFINITY), dkey_h(INFINITY), nodata, eps, dval_h, &b.lo, &b.hi);
+    return b;
+}
+
+SlopeConsts slope_consts(double cellsize, int method, int units) {
+    const double cs = (double)(float)cellsize;  // MetaData::cellSize is a float (gpro/metaData.h:56)
+    SlopeConsts k;
+    k.k_fd = (float)(1.0 / (8.0 * cs));
+    k.k_ffd = (float)(1.0 / (4.0 * cs));
+    k.k_sd = (float)(1.0 / cs);
+    k.k_sfd = (float)(1.0 / (2.0 * cs));
+    k.k_tfd = (float)(1.0 / (6.0 * cs));
+    k.k_tfdw = (float)(1.0 / ((4.0 + sqrt(8.0)) * cs));
+    k.sqrt2 = (float)sqrt(2.0);
+    k.k_md = (float)(1.0 / (cs * sqrt(2.0)));
+    k.method = method;
+    k.degrees = units == PARGO_SLOPE_DEGREES;
+    return k;
+}
+
+// ---- staging of host buffers ----
+struct Staged {
+    InView in;   // device view of an input
+    OutView out; // device view of an output
+    bool host = false;
+    const pargo_raster* user = nullptr;
+    int64_t dpitch = 0;
+};
+
+int64_t round16(int64_t x) { return (x + 15) / 16 * 16; }
+
+pargo_status stage_in(pargo_ctx* ctx, const pargo_raster* r, int slot_id, cudaStream_t st, Staged* s) {
+    s->user = r;
+    s->host = r->location == PARGO_HOST;
+    if (!s->host) {
+        s->in = InView{(const char*)r->data, pitch_of(r), r->dtype};
+        return PARGO_OK;
+    }
+    const int64_t dp = round16(row_bytes(r));
+    cudaError_t e;
+    char* d = (char*)slot(ctx, slot_id, (size_t)(dp * r->rows), &e);
+    if (!d) return cuda_fail(ctx, e, "staging input");
+    CU(ctx, cudaMemcpy2DAsync(d, dp, r->data, pitch_of(r), row_bytes(r), r->rows, cudaMemcpyHostToDevice, st));
+    s->in = InView{d, dp, r->dtype};
+    s->dpitch = dp;
+    return PARGO_OK;
+}
+
+pargo_status stage_out(pargo_ctx* ctx, pargo_raster* r, int slot_id, Staged* s) {
+    s->user = r;
+    s->host = r->location == PARGO_HOST;
+    if (!s->host) {
+        s->out = OutView{(char*)r->data, pitch_of(r), r->dtype, r->nodata};
+        return PARGO_OK;
+    }
+    const int64_t dp = round16(row_bytes(r));
+    cudaError_t e;
+    char* d = (char*)slot(ctx, slot_id, (size_t)(dp * r->rows), &e);
+    if (!d) return cuda_fail(ctx, e, "staging output");
+    s->out = OutView{d, dp, r->dtype, r->nodata};
+    s->dpitch = dp;
+    return PARGO_OK;
+}
+
+pargo_status unstage_out(pargo_ctx* ctx, const Staged& s, cudaStream_t st) {
+    if (!s.host) return PARGO_OK;
+    const pargo_raster* r = s.user;
+    CU(ctx, cudaMemcpy2DAsync(r->data, pitch_of(r), s.out.base, s.dpitch, row_bytes(r), r->rows,
+                              cudaMemcpyDeviceToHost, st));
+    return PARGO_OK;
+}
+
+pargo_status make_tma_map(pargo_ctx* ctx, CUtensorMap* map, const void* base, int64_t rows, int64_t cols,
+                          int64_t pitch) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+            return fail(ctx, PARGO_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+        encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch};
+    cuuint32_t box[2] = {(cuuint32_t)focal_tma_box_cols(), (cuuint32_t)focal_tma_box_rows()};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ctx, PARGO_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return PARGO_OK;
+}
+
+bool tma_ok(const InView& v) {
+    return v.dtype == PARGO_F32 && ((uintptr_t)v.base % 16 == 0) && (v.pitch % 16 == 0);
+}
+
+// Outputs the TMA kernel can store directly (float4 slope, packed int8 codes).
+bool fast_out_ok(const FocalParams& p) {
+    if (p.do_slope && !(p.slope.dtype == PARGO_F32 && (uintptr_t)p.slope.base % 16 == 0 && p.slope.pitch % 16 == 0))
+        return false;
+    if (p.do_d8 && !(p.d8.dtype == PARGO_I8 && (uintptr_t)p.d8.base % 4 == 0 && p.d8.pitch % 4 == 0)) return false;
+    return true;
+}
+
+pargo_status check_d8_out(pargo_ctx* ctx, const pargo_raster* d8, int dir_type) {
+    if (d8->dtype == PARGO_I8) {
+        if (dir_type != 8)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "I8 D8 output holds dir_type 8 codes only (bit sums reach 255)");
+        if (d8->nodata < -128 || d8->nodata > 127 || d8->nodata != floor(d8->nodata))
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "I8 D8 output: nodata %g is not an int8 value", d8->nodata);
+        if (d8->nodata >= -1 && d8->nodata <= 8)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "I8 D8 output: nodata %g collides with a D8 code", d8->nodata);
+    }
+    if (d8->dtype == PARGO_I16 && (d8->nodata < -32768 || d8->nodata > 32767 || d8->nodata != floor(d8->nodata)))
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "I16 D8 output: nodata %g is not an int16 value", d8->nodata);
+    return PARGO_OK;
+}
+
+pargo_status finish_call(pargo_ctx* ctx, cudaStream_t st, bool sync) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+    if (sync) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "stream synchronize");
+        int flag = 0;
+        e = cudaMemcpy(&flag, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "error flag read");
+        if (flag) {
+            cudaMemset(ctx->d_error, 0, sizeof(int));
+            return fail(ctx, PARGO_ERR_DEVICE_TIMEOUT, "a device-side wait exceeded its bound");
+        }
+    }
+    return PARGO_OK;
+}
+
+pargo_status focal_impl(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
+                        const pargo_nbr* nbr, int method, int units, int dir_type, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if ((st = check_raster(ctx, dem, "dem")) != PARGO_OK) return st;
+    if (dem->dtype != PARGO_F32 && dem->dtype != PARGO_F64)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "dem must be F32 or F64");
+    if ((st = check_dims(ctx, dem)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if (!slope && !d8) return fail(ctx, PARGO_ERR_INVALID_ARG, "no output requested");
+    if (slope) {
+        if ((st = check_raster(ctx, slope, "slope")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, slope, "slope")) != PARGO_OK) return st;
+        if (slope->dtype != PARGO_F32 && slope->dtype != PARGO_F64)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "slope must be F32 or F64");
+        if (method < 0 || method > 6) return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown slope method %d", method);
+        if (units != PARGO_SLOPE_RATIO && units != PARGO_SLOPE_DEGREES)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown slope units %d", units);
+    }
+    if (d8) {
+        if ((st = check_raster(ctx, d8, "d8")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, d8, "d8")) != PARGO_OK) return st;
+        if ((st = check_d8_out(ctx, d8, dir_type)) != PARGO_OK) return st;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sdem, sslope, sd8;
+    if ((st = stage_in(ctx, dem, kSlotIn0, s, &sdem)) != PARGO_OK) return st;
+    if (slope && (st = stage_out(ctx, slope, kSlotOut0, &sslope)) != PARGO_OK) return st;
+    if (d8 && (st = stage_out(ctx, d8, kSlotOut1, &sd8)) != PARGO_OK) return st;
+
+    FocalParams p{};
+    p.rows = dem->rows;
+    p.cols = dem->cols;
+    p.nd6f = float_band(dem->nodata, kEpsHydro);
+    p.nd7f = float_band(dem->nodata, kEpsSlope);
+    p.nd6d = double_band(dem->nodata, kEpsHydro);
+    p.nd7d = double_band(dem->nodata, kEpsSlope);
+    p.sk = slope_consts(dem->cellsize, method, units);
+    p.do_slope = slope != nullptr;
+    p.do_d8 = d8 != nullptr;
+    p.dir_type = dir_type;
+    if (slope) p.slope = sslope.out;
+    if (d8) p.d8 = sd8.out;
+    p.fallbacks = &ctx->d_counters[0];
+    p.error_flag = ctx->d_error;
+    CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
+
+    if (tma_ok(sdem.in)) {
+        CUtensorMap map;
+        if ((st = make_tma_map(ctx, &map, sdem.in.base, p.rows, p.cols, sdem.in.pitch)) != PARGO_OK) return st;
+        CU(ctx, launch_focal_tma(&map, p, fast_out_ok(p) ? 1 : 0, ctx->num_sms, s));
+    } else {
+        CU(ctx, launch_focal_generic(sdem.in, p, s));
+    }
+    const bool host_io = sdem.host || (slope && sslope.host) || (d8 && sd8.host);
+    if (slope && (st = unstage_out(ctx, sslope, s)) != PARGO_OK) return st;
+    if (d8 && (st = unstage_out(ctx, sd8, s)) != PARGO_OK) return st;
+    if (host_io) {
+        unsigned long long fb = 0;
+        CU(ctx, cudaMemcpyAsync(&fb, &ctx->d_counters[0], sizeof(fb), cudaMemcpyDeviceToHost, s));
+        if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+        ctx->last_fallbacks = (int64_t)fb;
+        return PARGO_OK;
+    }
+    ctx->last_fallbacks = -1;  // not read back for asynchronous device calls
+    return finish_call(ctx, s, false);
+}
+
+}  // namespace
+
+extern "C" {
+
+int pargo_abi_version(void) { return PARGO_ABI_VERSION; }
+
+const char* pargo_last_error(const pargo_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int64_t pargo_last_d8_fallbacks(const pargo_ctx* ctx) { return ctx ? ctx->last_fallbacks : -1; }
+
+pargo_status pargo_create(int device, pargo_ctx** out) {
+    if (!out) return PARGO_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return PARGO_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return PARGO_ERR_INVALID_ARG;
+    pargo_ctx* ctx = new pargo_ctx();
+    ctx->device = device;
+    if ((e = cudaSetDevice(device)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev_a, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&ctx->ev_b, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->d_counters, 8 * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&ctx->d_error, sizeof(int))) != cudaSuccess ||
+        (e = cudaMemset(ctx->d_counters, 0, 8 * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMemset(ctx->d_error, 0, sizeof(int))) != cudaSuccess) {
+        pargo_destroy(ctx);
+        return e == cudaErrorMemoryAllocation ? PARGO_ERR_OUT_OF_MEMORY : PARGO_ERR_CUDA;
+    }
+    *out = ctx;
+    return PARGO_OK;
+}
+
+pargo_status pargo_destroy(pargo_ctx* ctx) {
+    if (!ctx) return PARGO_OK;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    if (ctx->fill_graph) cudaGraphExecDestroy(ctx->fill_graph);
+    for (auto& s : ctx->slots)
+        if (s.p) cudaFree(s.p);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
+    if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
+    if (ctx->own) cudaStreamDestroy(ctx->own);
+    delete ctx;
+    return PARGO_OK;
+}
+
+pargo_status pargo_nbr_parse(const char* text, pargo_nbr* out) {
+    if (!text || !out) return PARGO_ERR_INVALID_ARG;
+    std::istringstream is(text);
+    int n = 0;
+    if (!(is >> n) || n <= 0) return PARGO_ERR_INVALID_ARG;  // empty set (neighborhood.h:113-117)
+    std::vector<std::pair<int, int>> v;
+    if (n >= 100) {  // automatic sqrt(n) x sqrt(n) square (neighborhood.h:634-646)
+        const int half = ((int)sqrt((double)n)) / 2;
+        for (int i = -half; i <= half; i++)
+            for (int j = -half; j <= half; j++) v.emplace_back(i, j);
+    } else {
+        for (int k = 0; k < n; k++) {
+            int r, c;
+            double w;
+            if (!(is >> r >> c >> w)) return PARGO_ERR_INVALID_ARG;
+            v.emplace_back(r, c);
+        }
+    }
+    bool origin = false;
+    for (size_t i = 0; i < v.size(); i++) {
+        if (v[i].first == 0 && v[i].second == 0) origin = true;
+        for (size_t j = 0; j < i; j++)
+            if (v[j] == v[i]) return PARGO_ERR_INVALID_ARG;  // duplicate (neighborhood.h:131-137)
+    }
+    if (!origin) return PARGO_ERR_INVALID_ARG;  // must hold (0,0) (neighborhood.h:118-123)
+    pargo_nbr r{(int32_t)v.size(), v[0].first, v[0].second, v[0].first, v[0].second};
+    for (auto& p : v) {
+        r.min_row = std::min(r.min_row, p.first);
+        r.min_col = std::min(r.min_col, p.second);
+        r.max_row = std::max(r.max_row, p.first);
+        r.max_col = std::max(r.max_col, p.second);
+    }
+    *out = r;
+    return PARGO_OK;
+}
+
+pargo_status pargo_slope(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, const pargo_nbr* nbr,
+                         int method, int units, void* stream) {
+    if (!slope) return fail(ctx, PARGO_ERR_INVALID_ARG, "slope output is required");
+    return focal_impl(ctx, dem, slope, nullptr, nbr, method, units, 8, stream);
+}
+
+pargo_status pargo_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* d8, const pargo_nbr* nbr, int dir_type,
+                      void* stream) {
+    if (!d8) return fail(ctx, PARGO_ERR_INVALID_ARG, "d8 output is required");
+    return focal_impl(ctx, dem, nullptr, d8, nbr, 0, 0, dir_type, stream);
+}
+
+pargo_status pargo_slope_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
+                            const pargo_nbr* nbr, int method, int units, int dir_type, void* stream) {
+    return focal_impl(ctx, dem, slope, d8, nbr, method, units, dir_type, stream);
+}
+
+// ------------------------------------------------------------------ fill --
+pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
+                        const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if ((st = check_raster(ctx, dem, "dem")) != PARGO_OK) return st;
+    if (dem->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: dem must be F32");
+    if ((st = check_dims(ctx, dem)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, wdem, "wdem")) != PARGO_OK) return st;
+    if ((st = check_same(ctx, dem, wdem, "wdem")) != PARGO_OK) return st;
+    if (wdem->dtype != PARGO_F64 && wdem->dtype != PARGO_F32)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: wdem must be F64 or F32");
+    pargo_fill_opts o{0.0005, 10000.0, 0};
+    if (opts) o = *opts;
+    if (!(o.gap > 0.0) || !isfinite(o.gap) || !isfinite(o.init_level))
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: gap must be positive and finite");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sdem, sw;
+    if ((st = stage_in(ctx, dem, kSlotIn0, s, &sdem)) != PARGO_OK) return st;
+    if ((st = stage_out(ctx, wdem, kSlotOut0, &sw)) != PARGO_OK) return st;
+
+    const int64_t rows = dem->rows, cols = dem->cols, n = rows * cols;
+    const int T = fill_tile_rows();
+    FillParams p{};
+    p.rows = rows;
+    p.cols = cols;
+    p.dem = (const float*)sdem.in.base;
+    p.dem_pitch = sdem.in.pitch;
+    p.nd6f = float_band(dem->nodata, kEpsHydro);
+    p.gap = o.gap;
+    p.init_level = o.init_level;
+    p.tiles_y = (rows + T - 1) / T;
+    p.tiles_x = (cols + T - 1) / T;
+    const int64_t ntiles = p.tiles_y * p.tiles_x;
+    if (ntiles >= INT32_MAX) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: raster too large");
+    cudaError_t e;
+    p.w = (double*)slot(ctx, kSlotFillW, (size_t)n * sizeof(double), &e);
+    if (!p.w) return cuda_fail(ctx, e, "fill levels");
+    int32_t* lists = (int32_t*)slot(ctx, kSlotFillLists, (size_t)(2 * ntiles + 8) * sizeof(int32_t), &e);
+    if (!lists) return cuda_fail(ctx, e, "fill worklists");
+    int32_t* queued = (int32_t*)slot(ctx, kSlotFillQueued, (size_t)ntiles * sizeof(int32_t), &e);
+    if (!queued) return cuda_fail(ctx, e, "fill queue flags");
+    FillScratch sc{};
+    sc.list_a = lists;
+    sc.list_b = lists + ntiles;
+    sc.counts = lists + 2 * ntiles;
+    sc.queued = queued;
+    sc.visits = &ctx->d_counters[1];
+    sc.changed = &ctx->d_counters[2];
+    CU(ctx, cudaMemsetAsync(ctx->d_counters, 0, 8 * sizeof(unsigned long long), s));
+    {
+        cudaError_t ee = fill_init(p, sc, s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill init");
+    }
+    // Rounds run on the context's own stream, as CUDA-graph launches of
+    // kRoundsPerGraph rounds (an even number, so list A is current again).
+    const int kRoundsPerGraph = 16;
+    CU(ctx, cudaEventRecord(ctx->ev_a, s));
+    CU(ctx, cudaStreamWaitEvent(ctx->own, ctx->ev_a, 0));
+    char keybuf[256];
+    snprintf(keybuf, sizeof(keybuf), "%p %p %p %p %lld %lld %a %a %a %a %d", (void*)p.w, (void*)p.dem, (void*)lists,
+             (void*)queued, (long long)rows, (long long)cols, p.gap, p.init_level, (double)p.nd6f.lo,
+             (double)p.nd6f.hi, (int)p.dem_pitch);
+    if (!ctx->fill_graph || ctx->fill_graph_key != keybuf) {
+        if (ctx->fill_graph) {
+            cudaGraphExecDestroy(ctx->fill_graph);
+            ctx->fill_graph = nullptr;
+        }
+        cudaGraph_t g;
+        CU(ctx, cudaStreamBeginCapture(ctx->own, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaSuccess;
+        for (int r = 0; r < kRoundsPerGraph && ce == cudaSuccess; r++) ce = fill_round(p, sc, r & 1, ctx->num_sms, ctx->own);
+        cudaError_t ee = cudaStreamEndCapture(ctx->own, &g);
+        if (ce != cudaSuccess) return cuda_fail(ctx, ce, "fill round capture");
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill graph capture");
+        ee = cudaGraphInstantiate(&ctx->fill_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill graph instantiate");
+        ctx->fill_graph_key = keybuf;
+    }
+    unsigned long long* hp = (unsigned long long*)pinned(ctx, 64, &e);
+    if (!hp) return cuda_fail(ctx, e, "pinned counters");
+    int64_t rounds = 0;
+    bool converged = false;
+    for (;;) {
+        CU(ctx, cudaGraphLaunch(ctx->fill_graph, ctx->own));
+        rounds += kRoundsPerGraph;
+        int32_t* hc = (int32_t*)hp;
+        CU(ctx, cudaMemcpyAsync(hc, sc.counts, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->own));
+        CU(ctx, cudaStreamSynchronize(ctx->own));
+        if (hc[0] == 0 && hc[1] == 0) {
+            converged = true;
+            break;
+        }
+        if (o.max_rounds > 0 && rounds >= o.max_rounds) break;
+    }
+    CU(ctx, cudaEventRecord(ctx->ev_b, ctx->own));
+    CU(ctx, cudaStreamWaitEvent(s, ctx->ev_b, 0));
+    {
+        cudaError_t ee = fill_finish(p, sw.out, &ctx->d_counters[3], s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill finish");
+    }
+    if ((st = unstage_out(ctx, sw, s)) != PARGO_OK) return st;
+    CU(ctx, cudaMemcpyAsync(hp, ctx->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+    if (stats) {
+        stats->rounds = rounds;
+        stats->tile_visits = (int64_t)hp[1];
+        stats->raised_cells = (int64_t)hp[3];
+    }
+    if (!converged)
+        return fail(ctx, PARGO_ERR_NOT_CONVERGED, "fill: worklist not empty after %lld rounds", (long long)rounds);
+    return PARGO_OK;
+}
+
+// ------------------------------------------------------------------- SCA --
+pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr, int contract,
+                       void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if ((st = check_raster(ctx, d8, "d8")) != PARGO_OK) return st;
+    if ((st = check_dims(ctx, d8)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, sca, "sca")) != PARGO_OK) return st;
+    if ((st = check_same(ctx, d8, sca, "sca")) != PARGO_OK) return st;
+    if (sca->dtype != PARGO_F64 && sca->dtype != PARGO_F32)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "sca must be F64 or F32");
+    if (contract != PARGO_SCA_CONVERGED && contract != PARGO_SCA_SHIPPED)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown SCA contract %d", contract);
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sd8, so;
+    if ((st = stage_in(ctx, d8, kSlotIn0, s, &sd8)) != PARGO_OK) return st;
+    if ((st = stage_out(ctx, sca, kSlotOut0, &so)) != PARGO_OK) return st;
+    const int64_t n = d8->rows * d8->cols;
+    cudaError_t e;
+    ScaScratch sc{};
+    sc.indeg = (int32_t*)slot(ctx, kSlotScaIndeg, (size_t)n * 4, &e);
+    if (!sc.indeg) return cuda_fail(ctx, e, "sca in-degrees");
+    sc.conv = (unsigned long long*)slot(ctx, kSlotScaConv, (size_t)n * 8, &e);
+    if (!sc.conv) return cuda_fail(ctx, e, "sca totals");
+    sc.ship = (unsigned long long*)slot(ctx, kSlotScaShip, (size_t)n * 8, &e);
+    if (!sc.ship) return cuda_fail(ctx, e, "sca pulled totals");
+    sc.flags = (uint8_t*)slot(ctx, kSlotScaFlags, (size_t)((n + 3) / 4 * 4), &e);
+    if (!sc.flags) return cuda_fail(ctx, e, "sca flags");
+    sc.counters = (unsigned long long*)slot(ctx, kSlotScaCounters, 8 * sizeof(unsigned long long), &e);
+    if (!sc.counters) return cuda_fail(ctx, e, "sca counters");
+    ScaParams p{};
+    p.rows = d8->rows;
+    p.cols = d8->cols;
+    p.d8 = sd8.in;
+    p.nodata = d8->nodata;
+    p.out = so.out;
+    p.shipped = contract == PARGO_SCA_SHIPPED;
+    {
+        cudaError_t ee = sca_run(p, sc, s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "sca");
+    }
+    if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
+    unsigned long long* hp = (unsigned long long*)pinned(ctx, 64, &e);
+    if (!hp) return cuda_fail(ctx, e, "pinned counters");
+    CU(ctx, cudaMemcpyAsync(hp, sc.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+    if (hp[0] != hp[1])
+        return fail(ctx, PARGO_ERR_CYCLE, "sca: %llu of %llu valid cells completed (cycle or inflow from the ring)",
+                    hp[0], hp[1]);
+    return PARGO_OK;
+}
+
+// ------------------------------------------------------------------ batch --
+pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* slopes,
+                                  pargo_raster* d8s, const pargo_nbr* nbr, int method, int units, int dir_type,
+                                  void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (count < 0 || (count > 0 && !dems)) return fail(ctx, PARGO_ERR_INVALID_ARG, "batch: bad count or dems");
+    if (!slopes && !d8s) return fail(ctx, PARGO_ERR_INVALID_ARG, "batch: no output requested");
+    if (count == 0) return PARGO_OK;
+    pargo_status st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if (slopes && (method < 0 || method > 6)) return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown slope method %d", method);
+    bool all_tma = true;
+    for (int i = 0; i < count; i++) {
+        const pargo_raster* d = &dems[i];
+        if ((st = check_raster(ctx, d, "batch dem")) != PARGO_OK) return st;
+        if ((st = check_dims(ctx, d)) != PARGO_OK) return st;
+        if (d->dtype != PARGO_F32 || d->location != PARGO_DEVICE)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "batch dem %d: must be F32 on the device", i);
+        if (slopes) {
+            if ((st = check_raster(ctx, &slopes[i], "batch slope")) != PARGO_OK) return st;
+            if ((st = check_same(ctx, d, &slopes[i], "batch slope")) != PARGO_OK) return st;
+            if (slopes[i].location != PARGO_DEVICE || (slopes[i].dtype != PARGO_F32 && slopes[i].dtype != PARGO_F64))
+                return fail(ctx, PARGO_ERR_INVALID_ARG, "batch slope %d: must be F32/F64 on the device", i);
+        }
+        if (d8s) {
+            if ((st = check_raster(ctx, &d8s[i], "batch d8")) != PARGO_OK) return st;
+            if ((st = check_same(ctx, d, &d8s[i], "batch d8")) != PARGO_OK) return st;
+            if (d8s[i].location != PARGO_DEVICE)
+                return fail(ctx, PARGO_ERR_INVALID_ARG, "batch d8 %d: must be on the device", i);
+            if ((st = check_d8_out(ctx, &d8s[i], dir_type)) != PARGO_OK) return st;
+        }
+        InView v{(const char*)d->data, pitch_of(d), d->dtype};
+        if (!tma_ok(v)) all_tma = false;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    // Order: largest rasters first (their tiles are claimed first).
+    std::vector<int> order(count);
+    for (int i = 0; i < count; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return dems[a].rows * dems[a].cols > dems[b].rows * dems[b].cols;
+    });
+    const int TH = focal_tma_tile_rows(), TW = focal_tma_tile_cols();
+    std::vector<FocalParams> params(count);
+    std::vector<int64_t> start(count + 1), ntx(count);
+    std::vector<InView> views(count);
+    int64_t total = 0;
+    bool fast = true;
+    for (int k = 0; k < count; k++) {
+        const int i = order[k];
+        const pargo_raster* d = &dems[i];
+        FocalParams& p = params[k];
+        p = FocalParams{};
+        p.rows = d->rows;
+        p.cols = d->cols;
+        p.nd6f = float_band(d->nodata, kEpsHydro);
+        p.nd7f = float_band(d->nodata, kEpsSlope);
+        p.sk = slope_consts(d->cellsize, method, units);
+        p.do_slope = slopes != nullptr;
+        p.do_d8 = d8s != nullptr;
+        p.dir_type = dir_type;
+        if (slopes) p.slope = OutView{(char*)slopes[i].data, pitch_of(&slopes[i]), slopes[i].dtype, slopes[i].nodata};
+        if (d8s) p.d8 = OutView{(char*)d8s[i].data, pitch_of(&d8s[i]), d8s[i].dtype, d8s[i].nodata};
+        p.fallbacks = &ctx->d_counters[0];
+        p.error_flag = ctx->d_error;
+        if (!fast_out_ok(p)) fast = false;
+        views[k] = InView{(const char*)d->data, pitch_of(d), d->dtype};
+        start[k] = total;
+        if (all_tma) {
+            ntx[k] = (d->cols + TW - 1) / TW;
+            total += ntx[k] * ((d->rows + TH - 1) / TH);
+        } else {
+            ntx[k] = 0;
+            total += d->rows * d->cols;
+        }
+    }
+    start[count] = total;
+    // Device tables (cached while the batch description is unchanged).
+    std::string key((const char*)params.data(), params.size() * sizeof(FocalParams));
+    key.append((const char*)dems, (size_t)count * sizeof(pargo_raster));
+    cudaError_t e;
+    CUtensorMap* dmaps = (CUtensorMap*)slot(ctx, kSlotBatchMaps, (size_t)count * sizeof(CUtensorMap), &e);
+    FocalParams* dparams = (FocalParams*)slot(ctx, kSlotBatchParams, (size_t)count * sizeof(FocalParams), &e);
+    int64_t* dstart = (int64_t*)slot(ctx, kSlotBatchStart, (size_t)(count + 1) * 8, &e);
+    int64_t* dntx = (int64_t*)slot(ctx, kSlotBatchNtx, (size_t)count * 8, &e);
+    InView* ddems = (InView*)slot(ctx, kSlotBatchDems, (size_t)count * sizeof(InView), &e);
+    unsigned long long* claim = (unsigned long long*)slot(ctx, kSlotClaim, 64, &e);
+    if (!dmaps || !dparams || !dstart || !dntx || !ddems || !claim) return cuda_fail(ctx, e, "batch tables");
+    if (ctx->batch_key != key) {
+        std::vector<CUtensorMap> maps(all_tma ? count : 0);
+        if (all_tma)
+            for (int k = 0; k < count; k++)
+                if ((st = make_tma_map(ctx, &maps[k], views[k].base, params[k].rows, params[k].cols, views[k].pitch)) !=
+                    PARGO_OK)
+                    return st;
+        CU(ctx, cudaStreamSynchronize(s));
+        if (all_tma) CU(ctx, cudaMemcpy(dmaps, maps.data(), count * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+        CU(ctx, cudaMemcpy(dparams, params.data(), count * sizeof(FocalParams), cudaMemcpyHostToDevice));
+        CU(ctx, cudaMemcpy(dstart, start.data(), (count + 1) * 8, cudaMemcpyHostToDevice));
+        CU(ctx, cudaMemcpy(dntx, ntx.data(), count * 8, cudaMemcpyHostToDevice));
+        CU(ctx, cudaMemcpy(ddems, views.data(), count * sizeof(InView), cudaMemcpyHostToDevice));
+        ctx->batch_key = key;
+    }
+    CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
+    if (all_tma)
+        CU(ctx, launch_batch_tma(dmaps, dparams, dstart, dntx, count, total, fast ? 1 : 0, claim, &ctx->d_counters[0],
+                                 ctx->d_error, ctx->num_sms, s));
+    else
+        CU(ctx, launch_batch_generic(dparams, ddems, dstart, count, total, &ctx->d_counters[0], ctx->num_sms, s));
+    ctx->last_fallbacks = -1;
+    return finish_call(ctx, s, false);
+}
+
+// ------------------------------------------------------------- gradients --
+static pargo_status grad_impl(pargo_ctx* ctx, const pargo_raster* z, const pargo_raster* zref,
+                              const pargo_raster* gslope, pargo_raster* gz, double* loss, const pargo_nbr* nbr,
+                              int mode, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if ((st = check_raster(ctx, z, "z")) != PARGO_OK) return st;
+    if (z->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "z must be F32");
+    if ((st = check_dims(ctx, z)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    const pargo_raster* other = mode == 0 ? zref : gslope;
+    if ((st = check_raster(ctx, other, mode == 0 ? "z_ref" : "gslope")) != PARGO_OK) return st;
+    if (other->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "z_ref / gslope must be F32");
+    if ((st = check_same(ctx, z, other, "z_ref / gslope")) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, gz, "gz")) != PARGO_OK) return st;
+    if (gz->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "gz must be F32");
+    if ((st = check_same(ctx, z, gz, "gz")) != PARGO_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sz, so, sg;
+    if ((st = stage_in(ctx, z, kSlotIn0, s, &sz)) != PARGO_OK) return st;
+    if ((st = stage_in(ctx, other, kSlotIn1, s, &so)) != PARGO_OK) return st;
+    if ((st = stage_out(ctx, gz, kSlotGradOut, &sg)) != PARGO_OK) return st;
+    cudaError_t e;
+    double* dloss = (double*)slot(ctx, kSlotLoss, 16, &e);
+    if (!dloss) return cuda_fail(ctx, e, "loss accumulator");
+    CU(ctx, cudaMemsetAsync(dloss, 0, sizeof(double), s));
+    GradParams p{};
+    p.rows = z->rows;
+    p.cols = z->cols;
+    p.z = sz.in;
+    if (mode == 0) p.zref = so.in; else p.gslope = so.in;
+    p.nd7f = float_band(z->nodata, kEpsSlope);
+    p.k_fd = (float)(1.0 / (8.0 * (double)(float)z->cellsize));
+    p.gz = (float*)sg.out.base;
+    p.gz_pitch = sg.out.pitch;
+    p.loss = dloss;
+    CU(ctx, launch_slope_loss_grad(p, mode, s));
+    if ((st = unstage_out(ctx, sg, s)) != PARGO_OK) return st;
+    const bool sync = sz.host || so.host || sg.host || loss;
+    if (loss) {
+        double* hp = (double*)pinned(ctx, 64, &e);
+        if (!hp) return cuda_fail(ctx, e, "pinned loss");
+        CU(ctx, cudaMemcpyAsync(hp, dloss, sizeof(double), cudaMemcpyDeviceToHost, s));
+        if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+        *loss = hp[0];
+        return PARGO_OK;
+    }
+    return finish_call(ctx, s, sync);
+}
+
+pargo_status pargo_slope_fwd(pargo_ctx* ctx, const pargo_raster* z, pargo_raster* slope, const pargo_nbr* nbr,
+                             void* stream) {
+    return focal_impl(ctx, z, slope, nullptr, nbr, PARGO_SLOPE_FD, PARGO_SLOPE_RATIO, 8, stream);
+}
+
+pargo_status pargo_slope_bwd(pargo_ctx* ctx, const pargo_raster* z, const pargo_raster* gslope, pargo_raster* gz,
+                             const pargo_nbr* nbr, void* stream) {
+    return grad_impl(ctx, z, nullptr, gslope, gz, nullptr, nbr, 1, stream);
+}
+
+pargo_status pargo_slope_loss_grad(pargo_ctx* ctx, const pargo_raster* z, const pargo_raster* z_ref, pargo_raster* gz,
+                                   double* loss, const pargo_nbr* nbr, void* stream) {
+    return grad_impl(ctx, z, z_ref, nullptr, gz, loss, nbr, 0, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,105 @@
+// kernels.h -- host-side launch interface between the C ABI (abi.cu) and the
+// kernel translation units.  Everything here takes device pointers only.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace pargo {
+
+// One raster as the kernels see it (device memory).
+struct DevRaster {
+    const char* base;  // input rasters
+    char* out;         // output rasters (same pointer, writable)
+    int64_t rows, cols, pitch;
+    int32_t dtype;
+    double nodata;
+};
+
+struct FocalParams {
+    int64_t rows, cols;
+    Band<float> nd6f, nd7f;   // nodata bands for float input (Eps 1e-6 D8/fill, 1e-7 slope)
+    Band<double> nd6d, nd7d;  // the same for double input
+    SlopeConsts sk;
+    int do_slope, do_d8, dir_type;
+    OutView slope, d8;
+    unsigned long long* fallbacks;  // device counter of exact-path D8 cells (may be null)
+    int* error_flag;                // device flag: a bounded wait gave up
+};
+
+// focal.cu
+cudaError_t launch_focal_tma(const CUtensorMap* map, const FocalParams& p, int fast_out, int num_sms,
+                             cudaStream_t s);
+cudaError_t launch_focal_generic(const InView& dem, const FocalParams& p, cudaStream_t s);
+size_t focal_tma_smem_bytes();
+int focal_tma_tile_rows();
+int focal_tma_tile_cols();
+int focal_tma_box_cols();
+int focal_tma_box_rows();
+
+// Batched slope+D8 (focal.cu): device tables of per-raster descriptors/params.
+cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params, const int64_t* tile_start,
+                             const int64_t* ntx_of, int count, int64_t total_tiles, int fast_out,
+                             unsigned long long* claim, unsigned long long* fallbacks, int* error_flag, int num_sms,
+                             cudaStream_t s);
+cudaError_t launch_batch_generic(const FocalParams* params, const InView* dems, const int64_t* cell_start, int count,
+                                 int64_t total_cells, unsigned long long* fallbacks, int num_sms, cudaStream_t s);
+
+// fill.cu
+struct FillParams {
+    int64_t rows, cols;
+    const float* dem;
+    int64_t dem_pitch;      // bytes
+    Band<float> nd6f;       // nodata band of the DEM (Eps 1e-6)
+    double gap, init_level;
+    double* w;              // working levels (rows x cols, dense), +inf marks nodata levels
+    int64_t tiles_y, tiles_x;
+};
+struct FillScratch {
+    int32_t* list_a;        // tile worklists (capacity tiles_y * tiles_x)
+    int32_t* list_b;
+    int32_t* counts;        // [0] = length of list_a, [1] = length of list_b, [2] = claim cursor
+    int32_t* queued;        // per-tile flag: already in the next worklist
+    unsigned long long* visits;
+    unsigned long long* changed;
+};
+cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st);
+cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st);
+cudaError_t fill_finish(const FillParams& p, const OutView& out, unsigned long long* raised, cudaStream_t st);
+int fill_tile_rows();
+int fill_tile_cols();
+
+// sca.cu
+struct ScaParams {
+    int64_t rows, cols;
+    InView d8;
+    double nodata;          // nodata of the D8 input
+    OutView out;
+    int shipped;            // 0 converged, 1 shipped single sweep
+};
+struct ScaScratch {
+    int32_t* indeg;         // remaining in-degree per cell
+    unsigned long long* conv;  // accumulated converged upstream counts
+    unsigned long long* ship;  // accumulated pulled counts (shipped contract)
+    uint8_t* flags;         // bit0 source, bit1 not-done, bit2 valid, bit3 completed
+    unsigned long long* counters;  // [0] completed cells, [1] valid cells, [2] last-cell conv, [3] last-cell ship
+};
+cudaError_t sca_run(const ScaParams& p, const ScaScratch& s, cudaStream_t st);
+
+// grad.cu
+struct GradParams {
+    int64_t rows, cols;
+    InView z, zref, gslope;
+    Band<float> nd7f;
+    float k_fd;             // 1 / (8 cs)
+    float* gz;
+    int64_t gz_pitch;
+    OutView slope;
+    double* loss;           // device accumulator (may be null)
+};
+cudaError_t launch_slope_loss_grad(const GradParams& p, int mode, cudaStream_t st);
+
+}  // namespace pargo

@@ -1,0 +1,177 @@
+"""Slope + D8 on the GPU through the C ABI, against the reference.
+
+Golden fixtures hold what the unmodified reference operators output; the C
+oracle (the restatement pinned to those fixtures) covers the larger and
+edge-case inputs.  D8 codes must be bit-exact; slope within 1e-5 relative.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN_CASES, bits_equal, load_golden
+from gpu_helpers import SLOPE_RTOL, d8_as_f64, dev, empty_dev, host, slope_close
+from pargo_gb300 import abi, synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("align", [0, 16])
+def test_golden_slope_all_methods(case, align, ctx):
+    g = load_golden(case)
+    dem, nd, cs = g["dem"], float(g["nodata"]), float(g["cellsize"])
+    d = dev(dem, align)
+    for m in range(7):
+        out = empty_dev(dem.shape, np.float32, align)
+        ctx.slope(abi.raster(d, nd, cs), abi.raster(out, nd, cs), method=m)
+        ok, mx, mean = slope_close(host(out), g["slope_m%d" % m], nd)
+        assert ok, "method %d max rel %g" % (m, mx)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+@pytest.mark.parametrize("align", [0, 16])
+def test_golden_d8_bit_exact(case, align, ctx):
+    g = load_golden(case)
+    dem, nd, cs = g["dem"], float(g["nodata"]), float(g["cellsize"])
+    d = dev(dem, align)
+    for dt in (8, 256):
+        out = empty_dev(dem.shape, np.float64, align)
+        ctx.d8(abi.raster(d, nd, cs), abi.raster(out, nd, cs), dir_type=dt)
+        assert bits_equal(host(out), g["d8_%d" % dt]), "dir_type %d" % dt
+    codes = empty_dev(dem.shape, np.int8, align)
+    ctx.d8(abi.raster(d, nd, cs), abi.raster(codes, -128, cs), dir_type=8)
+    assert bits_equal(d8_as_f64(host(codes), -128, nd), g["d8_8"])
+    codes16 = empty_dev(dem.shape, np.int16, align)
+    ctx.d8(abi.raster(d, nd, cs), abi.raster(codes16, -9999, cs), dir_type=256)
+    assert bits_equal(d8_as_f64(host(codes16), -9999, nd), g["d8_256"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_golden_fused_slope_d8_host_buffers(case, ctx):
+    """The reference-facing call shape: host buffers in and out (staged by the library)."""
+    g = load_golden(case)
+    dem, nd, cs = g["dem"], float(g["nodata"]), float(g["cellsize"])
+    slope = np.full(dem.shape, 5.0, np.float64)
+    d8 = np.full(dem.shape, 5.0, np.float64)
+    ctx.slope_d8(abi.raster(dem, nd, cs), abi.raster(slope, nd, cs), abi.raster(d8, nd, cs))
+    ok, mx, _ = slope_close(slope, g["slope_m0"], nd)
+    assert ok, mx
+    assert bits_equal(d8, g["d8_8"])
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_golden_d8_on_filled_surface(case, ctx):
+    """D8 on the float64 pit-removed surface (the reference pipeline's input)."""
+    g = load_golden(case)
+    w, nd = g["fill"], float(g["nodata"])
+    out = empty_dev(w.shape, np.float64)
+    ctx.d8(abi.raster(dev(w), nd), abi.raster(out, nd), dir_type=8)
+    assert bits_equal(host(out), g["d8w_8"])
+    s = empty_dev(w.shape, np.float32)
+    ctx.slope(abi.raster(dev(w), nd, float(g["cellsize"])), abi.raster(s, nd))
+    import oracle
+    ref = oracle.Oracle().slope(w, nd, float(g["cellsize"]))
+    ok, mx, _ = slope_close(host(s), ref, nd)
+    assert ok, mx
+
+
+def test_degrees_epilogue(ctx, oracle_lib):
+    dem = synth.slope_dem(300, 412, seed=0)
+    ref = oracle_lib.slope(dem, -9999.0, 30.0)
+    out = empty_dev(dem.shape, np.float32, 16)
+    ctx.slope(abi.raster(dev(dem, 16), -9999.0, 30.0), abi.raster(out, -9999.0), units=abi.DEGREES)
+    deg = np.where(ref == -9999.0, -9999.0, np.degrees(np.arctan(ref)))
+    ok, mx, _ = slope_close(host(out), deg, -9999.0)
+    assert ok, mx
+
+
+@pytest.mark.parametrize("shape", [(3, 3), (4, 5), (31, 127), (32, 128), (33, 129), (65, 257), (95, 383),
+                                   (1024, 1024)])
+@pytest.mark.parametrize("align", [0, 16])
+def test_sizes_against_oracle(shape, align, ctx, oracle_lib):
+    """Tile-boundary sizes +-1, the smallest raster the 3x3 window allows, the slope config (1024^2)."""
+    dem = synth.hydro_dem(shape[0], shape[1], seed=shape[0] * 7 + shape[1], relief=1500.0)
+    nd, cs = -9999.0, 30.0
+    s = empty_dev(shape, np.float32, align)
+    c = empty_dev(shape, np.int8, align)
+    ctx.slope_d8(abi.raster(dev(dem, align), nd, cs), abi.raster(s, nd), abi.raster(c, -128))
+    ok, mx, _ = slope_close(host(s), oracle_lib.slope(dem, nd, cs), nd)
+    assert ok, mx
+    assert bits_equal(d8_as_f64(host(c), -128, nd), oracle_lib.d8(dem, nd))
+
+
+def test_all_nodata_and_flat(ctx):
+    nd = -9999.0
+    dem = np.full((40, 150), nd, np.float32)
+    s = empty_dev(dem.shape, np.float32)
+    c = empty_dev(dem.shape, np.int8)
+    ctx.slope_d8(abi.raster(dev(dem), nd, 1.0), abi.raster(s, nd), abi.raster(c, -128))
+    assert (host(s) == nd).all() and (host(c) == -128).all()
+    flat = np.full((40, 150), 12.5, np.float32)
+    ctx.slope_d8(abi.raster(dev(flat), nd, 1.0), abi.raster(s, nd), abi.raster(c, -128))
+    hs, hc = host(s), host(c)
+    assert (hs[1:-1, 1:-1] == 0.0).all() and (hc[1:-1, 1:-1] == -1).all()
+    assert (hs[0] == nd).all() and (hc[:, -1] == -128).all()
+
+
+def test_near_nodata_values_use_the_reference_eps(ctx, oracle_lib):
+    """Values within 1e-7 / 1e-6 of nodata: slope uses Eps 1e-7, D8 uses 1e-6."""
+    dem = synth.fbm(64, 96, 9, 0.8, 0.0, 100.0)
+    dem[10, 10] = np.float32(-9999.0 + 5e-7)   # nodata for D8, not for slope... if representable
+    dem[20, 20] = np.float32(-9999.0)
+    dem[30, 30] = np.float32(-9998.999)
+    nd = -9999.0
+    s = empty_dev(dem.shape, np.float64)
+    c = empty_dev(dem.shape, np.float64)
+    ctx.slope_d8(abi.raster(dev(dem), nd, 10.0), abi.raster(s, nd), abi.raster(c, nd))
+    ok, mx, _ = slope_close(host(s), oracle_lib.slope(dem, nd, 10.0), nd)
+    assert ok, mx
+    assert bits_equal(host(c), oracle_lib.d8(dem, nd))
+
+
+def test_ties_and_quantised_terrain(ctx, oracle_lib):
+    """Integer-metre DEMs are full of exact ties: the middle-tie rule and the
+    bit sums must match exactly."""
+    rng = np.random.default_rng(5)
+    dem = rng.integers(0, 4, size=(300, 260)).astype(np.float32)
+    for dt in (8, 256):
+        c = empty_dev(dem.shape, np.float64)
+        ctx.d8(abi.raster(dev(dem), -9999.0), abi.raster(c, -9999.0), dir_type=dt)
+        assert bits_equal(host(c), oracle_lib.d8(dem, -9999.0, dir_type=dt))
+
+
+def test_rejects_bad_arguments(ctx):
+    dem = dev(np.zeros((10, 10), np.float32))
+    out = empty_dev((10, 10), np.float32)
+    with pytest.raises(abi.PargoError) as e:
+        ctx.slope(abi.raster(dem), abi.raster(out), nbr=abi.nbr_parse("1\n0 0 1\n"))
+    assert e.value.status_name == "PARGO_ERR_NBR_UNSUPPORTED"
+    with pytest.raises(abi.PargoError) as e:
+        ctx.slope(abi.raster(dev(np.zeros((2, 10), np.float32))), abi.raster(empty_dev((2, 10), np.float32)))
+    assert e.value.status_name == "PARGO_ERR_INVALID_ARG"
+    with pytest.raises(abi.PargoError):
+        ctx.slope(abi.raster(dem), abi.raster(empty_dev((10, 11), np.float32)))
+    with pytest.raises(abi.PargoError):
+        ctx.d8(abi.raster(dem), abi.raster(empty_dev((10, 10), np.int8), -128), dir_type=256)
+    with pytest.raises(abi.PargoError):
+        ctx.d8(abi.raster(dem), abi.raster(empty_dev((10, 10), np.int8), 3))
+
+
+def test_full_size_d8_bit_exact_and_fallback_rate(ctx, oracle_lib):
+    """8192^2 D8 on the pits+blob DEM against the (threaded) oracle, all cells."""
+    dem = synth.hydro_dem(8192, 8192, seed=1)
+    d = dev(dem)
+    c = empty_dev(dem.shape, np.int8)
+    s = empty_dev(dem.shape, np.float32)
+    ctx.slope_d8(abi.raster(d, -9999.0, 30.0), abi.raster(s, -9999.0), abi.raster(c, -128))
+    ref = oracle_lib.d8(dem, -9999.0, threads=16)
+    assert bits_equal(d8_as_f64(host(c), -128), ref)
+    sref = oracle_lib.slope(dem, -9999.0, 30.0, threads=16)
+    ok, mx, mean = slope_close(host(s), sref)
+    assert ok, mx
+    # host-buffer call to read the fallback count
+    sh = np.empty((512, 512), np.float32)
+    ch = np.empty((512, 512), np.int8)
+    ctx.slope_d8(abi.raster(np.ascontiguousarray(dem[:512, :512]), -9999.0, 30.0), abi.raster(sh, -9999.0),
+                 abi.raster(ch, -128))
+    assert 0 <= ctx.last_d8_fallbacks < 512 * 512 // 100

@@ -1,0 +1,97 @@
+"""Pins the CPU oracle (oracle/pargo_oracle.c) to the reference.
+
+1. Against the committed golden fixtures, which the unmodified reference
+   operators produced (tests/golden/make_golden.py): bit-exact, every case,
+   every operator output.
+2. Against the reference operators themselves (oracle/_ref), where the
+   reference tree is present, on extra seeded inputs.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, bits_equal, load_golden
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_oracle_matches_golden(case, oracle_lib):
+    g = load_golden(case)
+    dem, nd, cs = g["dem"], float(g["nodata"]), float(g["cellsize"])
+    O = oracle_lib
+    for m in range(7):
+        assert bits_equal(O.slope(dem, nd, cs, method=m), g["slope_m%d" % m]), "slope method %d" % m
+    assert bits_equal(O.d8(dem, nd, dir_type=8), g["d8_8"])
+    assert bits_equal(O.d8(dem, nd, dir_type=256), g["d8_256"])
+    w_gs, sweeps = O.fill_gs(dem, nd)
+    assert bits_equal(w_gs, g["fill"])
+    assert sweeps == int(g["fill_sweeps"])
+    assert bits_equal(O.fill(dem, nd), g["fill"]), "priority-flood fixpoint differs from the reference sweeps"
+    assert bits_equal(O.d8(g["fill"], nd, dir_type=8), g["d8w_8"])
+    ship, _ = O.sca_sweeps(g["d8w_8"], nd, 1)
+    assert bits_equal(ship, g["sca_ship"])
+    conv, _ = O.sca_sweeps(g["d8w_8"], nd, 1 << 30)
+    assert bits_equal(conv, g["sca_conv"])
+    assert bits_equal(O.sca(g["d8w_8"], nd), g["sca_conv"])
+    assert bits_equal(O.sca(g["d8w_8"], nd, shipped=True), g["sca_ship"])
+
+
+def test_golden_fixture_facts():
+    """Facts of dem.tif the reference itself printed when the fixtures were made."""
+    g = load_golden("demtif")
+    dem = g["dem"]
+    assert dem.shape == (124, 104)
+    assert float(g["cellsize"]) == 90.0
+    assert int(g["fill_sweeps"]) == 25
+    valid = g["slope_m0"] != -9999.0
+    assert valid.sum() == 6806
+    assert (g["fill"] > dem.astype(np.float64)).sum() > 0
+
+
+def _ref():
+    import oracle
+    if not oracle.Reference.available():
+        pytest.skip("reference tree absent: fixtures carry the reference results")
+    return oracle.Reference()
+
+
+@pytest.mark.parametrize("seed,shape", [(21, (57, 70)), (22, (33, 129)), (23, (120, 45))])
+def test_oracle_matches_reference_binary(seed, shape, oracle_lib):
+    from pargo_gb300 import synth
+    R = _ref()
+    O = oracle_lib
+    dem = synth.hydro_dem(shape[0], shape[1], seed=seed, hurst=0.7, relief=800.0)
+    nd, cs = -9999.0, 25.0
+    for m in range(7):
+        assert bits_equal(O.slope(dem, nd, cs, method=m), R.slope(dem, nd, cs, method=m))
+    for dt in (8, 256):
+        assert bits_equal(O.d8(dem, nd, dir_type=dt), R.d8(dem, nd, cs, dir_type=dt))
+    w_ref, sw_ref = R.fill(dem, nd, cs)
+    w_gs, sw = O.fill_gs(dem, nd)
+    assert bits_equal(w_gs, w_ref) and sw == sw_ref
+    assert bits_equal(O.fill(dem, nd), w_ref)
+    d8w = R.d8(w_ref, nd, cs)
+    assert bits_equal(O.d8(w_ref, nd), d8w)
+    assert bits_equal(O.sca(d8w, nd), R.sca(d8w, nd, cs, converged=True)[0])
+    assert bits_equal(O.sca(d8w, nd, shipped=True), R.sca(d8w, nd, cs, converged=False)[0])
+
+
+def test_oracle_openmp_matches_serial(oracle_lib):
+    """The threaded slope/D8 restatement (the CPU baseline) gives the serial bytes."""
+    from pargo_gb300 import synth
+    dem = synth.slope_dem(300, 257, seed=4)
+    O = oracle_lib
+    assert bits_equal(O.slope(dem, -9999.0, 30.0, threads=4), O.slope(dem, -9999.0, 30.0, threads=1))
+    assert bits_equal(O.d8(dem, -9999.0, threads=4), O.d8(dem, -9999.0, threads=1))
+
+
+def test_planted_mistake_is_caught(oracle_lib):
+    """A wrong oracle must fail the golden comparison: plant an off-by-one-ulp
+    change in the fixture's slope and in the fill, on the CPU."""
+    g = load_golden("fbm_slope")
+    s = oracle_lib.slope(g["dem"], -9999.0, 30.0)
+    bad = s.copy()
+    k = np.flatnonzero(bad != -9999.0)[10]
+    bad.flat[k] = np.nextafter(bad.flat[k], np.inf)
+    assert not bits_equal(bad, g["slope_m0"])
+    h = load_golden("fbm_hydro")
+    w = oracle_lib.fill(h["dem"], -9999.0, gap=0.0005 * (1 + 1e-9))
+    assert not bits_equal(w, h["fill"])
