@@ -112,9 +112,11 @@ typedef struct pargo_fill_opts {
 } pargo_fill_opts;
 
 typedef struct pargo_fill_stats {
-    int64_t rounds;       /* worklist rounds run */
-    int64_t tile_visits;  /* tiles relaxed, summed over rounds */
-    int64_t raised_cells; /* cells whose filled level is above the DEM */
+    int64_t rounds;        /* worklist rounds launched */
+    int64_t active_rounds; /* rounds whose worklist was not empty */
+    int64_t tile_visits;   /* tiles relaxed, summed over rounds */
+    int64_t raised_cells;  /* cells whose filled level is above the DEM */
+    double rounds_ms;      /* device time of all rounds (CUDA events on the round stream) */
 } pargo_fill_stats;
 
 typedef struct pargo_ctx pargo_ctx;
@@ -144,12 +146,33 @@ pargo_status pargo_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* d8,
 pargo_status pargo_slope_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
                             const pargo_nbr* nbr, int method, int units, int dir_type, void* stream);
 
+/* Autotuner of the fused slope+D8 kernel: times each tile-shape / occupancy
+ * variant `reps` times on `dem` (an F32 device raster with 16-byte aligned
+ * rows), keeps the fastest for rasters of the same size class (power of two of
+ * the cell count) in this context, and reports it in *best and the per-variant
+ * milliseconds in times_ms[0 .. max_times-1] (either may be NULL).  The
+ * environment variable PARGO_FOCAL_VARIANT, when set, overrides the choice.
+ * No reference counterpart. */
+pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps, int* best, float* times_ms,
+                              int max_times);
+
 /* Planchon-Darboux pit removal: the fixpoint the reference's Gauss-Seidel
  * sweeps reach (any visiting order reaches the same one).  dem: F32;
  * wdem: F64 (the reference's values) or F32 (those values rounded to float).
  * opts may be NULL (reference constants); stats may be NULL. */
 pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
                         const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream);
+
+/* Device-resident hydrology chain, as the reference runs it through files
+ * (pPitRemove.cpp:129 -> pD8.cpp:113 -> pSCA.cpp:59): pit removal, then slope
+ * and D8 on the float64 levels (what the reference D8 reads from the Float64
+ * pit-remove output), then SCA on those codes.  Every output may be NULL
+ * except that at least one must be given; wdem F64/F32, slope F32/F64,
+ * d8 I8/I16/I32/F32/F64 (dir_type 8), sca F64/F32.  Synchronous. */
+pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, pargo_raster* slope,
+                                  pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr,
+                                  const pargo_fill_opts* opts, int slope_method, int slope_units, int sca_contract,
+                                  pargo_fill_stats* stats, void* stream);
 
 /* D8 specific catchment area (upslope cell count, as the reference computes
  * it).  d8: F64 codes as the reference writes them, or I8/I16/I32 codes with

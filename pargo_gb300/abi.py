@@ -51,7 +51,8 @@ class FillOpts(ctypes.Structure):
 
 
 class FillStats(ctypes.Structure):
-    _fields_ = [("rounds", ctypes.c_int64), ("tile_visits", ctypes.c_int64), ("raised_cells", ctypes.c_int64)]
+    _fields_ = [("rounds", ctypes.c_int64), ("active_rounds", ctypes.c_int64), ("tile_visits", ctypes.c_int64),
+                ("raised_cells", ctypes.c_int64), ("rounds_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -76,14 +77,17 @@ def lib():
         L.pargo_slope_d8.argtypes = [vp, R, R, R, N, i, i, i, vp]
         L.pargo_fill.argtypes = [vp, R, R, N, P(FillOpts), P(FillStats), vp]
         L.pargo_sca.argtypes = [vp, R, R, N, i, vp]
+        L.pargo_hydro_pipeline.argtypes = [vp, R, R, R, R, R, N, P(FillOpts), i, i, i, P(FillStats), vp]
         L.pargo_batch_slope_d8.argtypes = [vp, i, R, R, R, N, i, i, i, vp]
         L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
         L.pargo_slope_bwd.argtypes = [vp, R, R, R, N, vp]
         L.pargo_slope_loss_grad.argtypes = [vp, R, R, R, P(ctypes.c_double), N, vp]
+        L.pargo_tune_focal.argtypes = [vp, R, i, P(i), P(ctypes.c_float), i]
+        L.pargo_tune_focal.restype = st
         L.pargo_last_d8_fallbacks.argtypes = [vp]
         L.pargo_last_d8_fallbacks.restype = ctypes.c_int64
         for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
-                     "pargo_fill", "pargo_sca", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
+                     "pargo_fill", "pargo_sca", "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
                      "pargo_slope_loss_grad"):
             getattr(L, name).restype = st
         _lib = L
@@ -115,12 +119,15 @@ def raster(a, nodata=-9999.0, cellsize=1.0):
         dt = {"torch.float32": F32, "torch.float64": F64, "torch.int8": I8, "torch.int16": I16,
               "torch.int32": I32}[str(a.dtype)]
         loc = DEVICE if a.is_cuda else HOST
-        return Raster(a.data_ptr(), dt, loc, a.shape[0], a.shape[1], a.stride(0) * a.element_size(),
-                      float(nodata), float(cellsize))
-    if a.ndim != 2 or a.strides[1] != a.itemsize:
-        raise ValueError("raster arrays must be 2-D with unit column stride")
-    return Raster(a.ctypes.data, _NP_DTYPES[a.dtype], HOST, a.shape[0], a.shape[1], a.strides[0],
-                  float(nodata), float(cellsize))
+        r = Raster(a.data_ptr(), dt, loc, a.shape[0], a.shape[1], a.stride(0) * a.element_size(),
+                   float(nodata), float(cellsize))
+    else:
+        if a.ndim != 2 or a.strides[1] != a.itemsize:
+            raise ValueError("raster arrays must be 2-D with unit column stride")
+        r = Raster(a.ctypes.data, _NP_DTYPES[a.dtype], HOST, a.shape[0], a.shape[1], a.strides[0],
+                   float(nodata), float(cellsize))
+    r._owner = a  # the buffer lives at least as long as its descriptor
+    return r
 
 
 def _stream_ptr(stream):
@@ -170,6 +177,13 @@ class Context:
                                          ctypes.byref(d8) if d8 else None, self._nbr(nbr), method, units, dir_type,
                                          _stream_ptr(stream)))
 
+    def tune_focal(self, dem, reps=5):
+        """Autotune the fused slope+D8 kernel on a device DEM; returns (best, ms per variant)."""
+        best = ctypes.c_int(0)
+        times = (ctypes.c_float * 16)()
+        self._check(lib().pargo_tune_focal(self._p, ctypes.byref(dem), reps, ctypes.byref(best), times, 16))
+        return best.value, [round(t, 4) for t in times if t > 0]
+
     def slope(self, dem, slope, method=SLOPE_FD, units=RATIO, nbr=None, stream=None):
         self._check(lib().pargo_slope(self._p, ctypes.byref(dem), ctypes.byref(slope), self._nbr(nbr), method, units,
                                       _stream_ptr(stream)))
@@ -183,6 +197,17 @@ class Context:
         stats = FillStats()
         self._check(lib().pargo_fill(self._p, ctypes.byref(dem), ctypes.byref(wdem), self._nbr(nbr),
                                      ctypes.byref(opts), ctypes.byref(stats), _stream_ptr(stream)))
+        return stats
+
+    def hydro_pipeline(self, dem, wdem=None, slope=None, d8=None, sca=None, gap=0.0005, init_level=10000.0,
+                       max_rounds=0, method=SLOPE_FD, units=RATIO, contract=SCA_CONVERGED, nbr=None, stream=None):
+        """Pit removal -> slope + D8 on the float64 levels -> SCA, device-resident."""
+        opts = FillOpts(gap, init_level, max_rounds)
+        stats = FillStats()
+        ref = lambda r: ctypes.byref(r) if r is not None else None
+        self._check(lib().pargo_hydro_pipeline(self._p, ctypes.byref(dem), ref(wdem), ref(slope), ref(d8), ref(sca),
+                                               self._nbr(nbr), ctypes.byref(opts), method, units, contract,
+                                               ctypes.byref(stats), _stream_ptr(stream)))
         return stats
 
     def sca(self, d8, sca, contract=SCA_CONVERGED, nbr=None, stream=None):

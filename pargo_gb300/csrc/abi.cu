@@ -26,7 +26,8 @@ struct pargo_ctx {
     int num_sms = 0;
     std::string err;
     cudaStream_t own = nullptr;  // stream for captured fill rounds
-    cudaEvent_t ev_a = nullptr, ev_b = nullptr;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // stream hand-off
+    cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // timing of the fill rounds
     // grow-only device scratch slots
     struct Slot {
         void* p = nullptr;
@@ -44,12 +45,18 @@ struct pargo_ctx {
     std::string fill_graph_key;
     // batch table cache
     std::string batch_key;
+    // autotuned focal kernel variant per size class (log2 of the cell count); -1 = untuned
+    int focal_variant[64];
+    pargo_ctx() {
+        for (int& v : focal_variant) v = -1;
+    }
 };
 
 enum SlotId {
     kSlotIn0 = 0, kSlotIn1, kSlotOut0, kSlotOut1, kSlotFillW, kSlotFillLists, kSlotFillQueued,
     kSlotScaIndeg, kSlotScaConv, kSlotScaShip, kSlotScaFlags, kSlotScaCounters, kSlotBatchMaps,
-    kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut
+    kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut,
+    kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes
 };
 
 namespace {
@@ -237,6 +244,7 @@ SlopeConsts slope_consts(double cellsize, int method, int units) {
     k.k_tfd = (float)(1.0 / (6.0 * cs));
     k.k_tfdw = (float)(1.0 / ((4.0 + sqrt(8.0)) * cs));
     k.sqrt2 = (float)sqrt(2.0);
+    k.sqrt2d = sqrt(2.0);
     k.k_md = (float)(1.0 / (cs * sqrt(2.0)));
     k.method = method;
     k.degrees = units == PARGO_SLOPE_DEGREES;
@@ -296,7 +304,7 @@ pargo_status unstage_out(pargo_ctx* ctx, const Staged& s, cudaStream_t st) {
 }
 
 pargo_status make_tma_map(pargo_ctx* ctx, CUtensorMap* map, const void* base, int64_t rows, int64_t cols,
-                          int64_t pitch) {
+                          int64_t pitch, int box_rows) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult q;
@@ -308,7 +316,7 @@ pargo_status make_tma_map(pargo_ctx* ctx, CUtensorMap* map, const void* base, in
     }
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)pitch};
-    cuuint32_t box[2] = {(cuuint32_t)focal_tma_box_cols(), (cuuint32_t)focal_tma_box_rows()};
+    cuuint32_t box[2] = {(cuuint32_t)focal_tma_box_cols(), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
     CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -358,6 +366,25 @@ pargo_status finish_call(pargo_ctx* ctx, cudaStream_t st, bool sync) {
         }
     }
     return PARGO_OK;
+}
+
+int size_class(int64_t cells) {
+    int c = 0;
+    while (c < 63 && ((int64_t)1 << (c + 1)) <= cells) c++;
+    return c;
+}
+
+// Focal kernel variant for a raster of `cells` cells: the environment
+// (PARGO_FOCAL_VARIANT) first, then the context's autotuned choice for the
+// size class, else variant 0.
+int pick_variant(pargo_ctx* ctx, int64_t cells) {
+    const char* env = getenv("PARGO_FOCAL_VARIANT");
+    if (env && *env) {
+        const int v = atoi(env);
+        if (v >= 0 && v < focal_num_variants()) return v;
+    }
+    const int v = ctx->focal_variant[size_class(cells)];
+    return v >= 0 ? v : 0;
 }
 
 pargo_status focal_impl(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
@@ -410,9 +437,12 @@ pargo_status focal_impl(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* s
     CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
 
     if (tma_ok(sdem.in)) {
+        const int v = pick_variant(ctx, p.rows * p.cols);
         CUtensorMap map;
-        if ((st = make_tma_map(ctx, &map, sdem.in.base, p.rows, p.cols, sdem.in.pitch)) != PARGO_OK) return st;
-        CU(ctx, launch_focal_tma(&map, p, fast_out_ok(p) ? 1 : 0, ctx->num_sms, s));
+        if ((st = make_tma_map(ctx, &map, sdem.in.base, p.rows, p.cols, sdem.in.pitch, focal_variant_rows(v) + 2)) !=
+            PARGO_OK)
+            return st;
+        CU(ctx, launch_focal_tma(&map, p, fast_out_ok(p) ? 1 : 0, v, ctx->num_sms, s));
     } else {
         CU(ctx, launch_focal_generic(sdem.in, p, s));
     }
@@ -454,6 +484,7 @@ pargo_status pargo_create(int device, pargo_ctx** out) {
         (e = cudaStreamCreateWithFlags(&ctx->own, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev_a, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&ctx->ev_b, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreate(&ctx->ev_t0)) != cudaSuccess || (e = cudaEventCreate(&ctx->ev_t1)) != cudaSuccess ||
         (e = cudaMalloc(&ctx->d_counters, 8 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMalloc(&ctx->d_error, sizeof(int))) != cudaSuccess ||
         (e = cudaMemset(ctx->d_counters, 0, 8 * sizeof(unsigned long long))) != cudaSuccess ||
@@ -477,6 +508,8 @@ pargo_status pargo_destroy(pargo_ctx* ctx) {
     if (ctx->d_error) cudaFree(ctx->d_error);
     if (ctx->ev_a) cudaEventDestroy(ctx->ev_a);
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
+    if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
+    if (ctx->ev_t1) cudaEventDestroy(ctx->ev_t1);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
     return PARGO_OK;
@@ -535,30 +568,70 @@ pargo_status pargo_slope_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raste
     return focal_impl(ctx, dem, slope, d8, nbr, method, units, dir_type, stream);
 }
 
-// ------------------------------------------------------------------ fill --
-pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
-                        const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream) {
+pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps, int* best, float* times_ms,
+                              int max_times) {
     if (!ctx) return PARGO_ERR_INVALID_ARG;
     ctx->err.clear();
     pargo_status st;
     if ((st = check_raster(ctx, dem, "dem")) != PARGO_OK) return st;
-    if (dem->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: dem must be F32");
     if ((st = check_dims(ctx, dem)) != PARGO_OK) return st;
-    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
-    if ((st = check_raster(ctx, wdem, "wdem")) != PARGO_OK) return st;
-    if ((st = check_same(ctx, dem, wdem, "wdem")) != PARGO_OK) return st;
-    if (wdem->dtype != PARGO_F64 && wdem->dtype != PARGO_F32)
-        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: wdem must be F64 or F32");
-    pargo_fill_opts o{0.0005, 10000.0, 0};
-    if (opts) o = *opts;
-    if (!(o.gap > 0.0) || !isfinite(o.gap) || !isfinite(o.init_level))
-        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: gap must be positive and finite");
-    cudaStream_t s = (cudaStream_t)stream;
+    if (dem->dtype != PARGO_F32 || dem->location != PARGO_DEVICE || (uintptr_t)dem->data % 16 || pitch_of(dem) % 16)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "tune: dem must be an F32 device raster with 16-byte aligned rows");
+    if (reps < 1) reps = 1;
     CU(ctx, cudaSetDevice(ctx->device));
-    Staged sdem, sw;
-    if ((st = stage_in(ctx, dem, kSlotIn0, s, &sdem)) != PARGO_OK) return st;
-    if ((st = stage_out(ctx, wdem, kSlotOut0, &sw)) != PARGO_OK) return st;
+    const int64_t rows = dem->rows, cols = dem->cols;
+    const int64_t sp = round16(cols * 4), cp = round16(cols);
+    cudaError_t e;
+    char* sbuf = (char*)slot(ctx, kSlotOut0, (size_t)(sp * rows), &e);
+    char* cbuf = sbuf ? (char*)slot(ctx, kSlotOut1, (size_t)(cp * rows), &e) : nullptr;
+    if (!sbuf || !cbuf) return cuda_fail(ctx, e, "tune outputs");
+    FocalParams p{};
+    p.rows = rows;
+    p.cols = cols;
+    p.nd6f = float_band(dem->nodata, kEpsHydro);
+    p.nd7f = float_band(dem->nodata, kEpsSlope);
+    p.sk = slope_consts(dem->cellsize, PARGO_SLOPE_FD, PARGO_SLOPE_RATIO);
+    p.do_slope = 1;
+    p.do_d8 = 1;
+    p.dir_type = 8;
+    p.slope = OutView{sbuf, sp, PARGO_F32, dem->nodata};
+    p.d8 = OutView{cbuf, cp, PARGO_I8, -128.0};
+    p.fallbacks = &ctx->d_counters[0];
+    p.error_flag = ctx->d_error;
+    float best_ms = 1e30f;
+    int best_v = 0;
+    for (int v = 0; v < focal_num_variants(); v++) {
+        CUtensorMap map;
+        if ((st = make_tma_map(ctx, &map, dem->data, rows, cols, pitch_of(dem), focal_variant_rows(v) + 2)) != PARGO_OK)
+            return st;
+        CU(ctx, launch_focal_tma(&map, p, 1, v, ctx->num_sms, ctx->own));  // warm
+        CU(ctx, cudaEventRecord(ctx->ev_t0, ctx->own));
+        for (int r = 0; r < reps; r++) CU(ctx, launch_focal_tma(&map, p, 1, v, ctx->num_sms, ctx->own));
+        CU(ctx, cudaEventRecord(ctx->ev_t1, ctx->own));
+        CU(ctx, cudaEventSynchronize(ctx->ev_t1));
+        float ms = 0.0f;
+        CU(ctx, cudaEventElapsedTime(&ms, ctx->ev_t0, ctx->ev_t1));
+        ms /= (float)reps;
+        if (times_ms && v < max_times) times_ms[v] = ms;
+        if (ms < best_ms) {
+            best_ms = ms;
+            best_v = v;
+        }
+    }
+    ctx->focal_variant[size_class(rows * cols)] = best_v;
+    if (best) *best = best_v;
+    return finish_call(ctx, ctx->own, true);
+}
 
+// ------------------------------------------------------------------ fill --
+}  // extern "C"
+
+namespace {
+
+// Runs the pit removal of `dem` (F32, staged) into the context's level buffer
+// (dense rows x cols doubles, +inf on nodata levels) and returns its params.
+pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* dem, const pargo_fill_opts& o,
+                       FillParams* out_p, pargo_fill_stats* stats, bool* converged, cudaStream_t s) {
     const int64_t rows = dem->rows, cols = dem->cols, n = rows * cols;
     const int T = fill_tile_rows();
     FillParams p{};
@@ -587,20 +660,24 @@ pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* w
     sc.queued = queued;
     sc.visits = &ctx->d_counters[1];
     sc.changed = &ctx->d_counters[2];
+    sc.active = &ctx->d_counters[4];
     CU(ctx, cudaMemsetAsync(ctx->d_counters, 0, 8 * sizeof(unsigned long long), s));
     {
         cudaError_t ee = fill_init(p, sc, s);
         if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill init");
     }
     // Rounds run on the context's own stream, as CUDA-graph launches of
-    // kRoundsPerGraph rounds (an even number, so list A is current again).
-    const int kRoundsPerGraph = 16;
+    // kRoundsPerGraph rounds (an even number, so list A is current again); a
+    // round cap below 16 shortens the graph so the cap is honoured exactly
+    // (rounded up to even).
+    int kRoundsPerGraph = 16;
+    if (o.max_rounds > 0 && o.max_rounds < 16) kRoundsPerGraph = (int)((o.max_rounds + 1) / 2 * 2);
     CU(ctx, cudaEventRecord(ctx->ev_a, s));
     CU(ctx, cudaStreamWaitEvent(ctx->own, ctx->ev_a, 0));
     char keybuf[256];
-    snprintf(keybuf, sizeof(keybuf), "%p %p %p %p %lld %lld %a %a %a %a %d", (void*)p.w, (void*)p.dem, (void*)lists,
-             (void*)queued, (long long)rows, (long long)cols, p.gap, p.init_level, (double)p.nd6f.lo,
-             (double)p.nd6f.hi, (int)p.dem_pitch);
+    snprintf(keybuf, sizeof(keybuf), "%p %p %p %p %lld %lld %a %a %a %a %lld %d", (void*)p.w, (void*)p.dem,
+             (void*)lists, (void*)queued, (long long)rows, (long long)cols, p.gap, p.init_level, (double)p.nd6f.lo,
+             (double)p.nd6f.hi, (long long)p.dem_pitch, kRoundsPerGraph);
     if (!ctx->fill_graph || ctx->fill_graph_key != keybuf) {
         if (ctx->fill_graph) {
             cudaGraphExecDestroy(ctx->fill_graph);
@@ -609,7 +686,8 @@ pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* w
         cudaGraph_t g;
         CU(ctx, cudaStreamBeginCapture(ctx->own, cudaStreamCaptureModeThreadLocal));
         cudaError_t ce = cudaSuccess;
-        for (int r = 0; r < kRoundsPerGraph && ce == cudaSuccess; r++) ce = fill_round(p, sc, r & 1, ctx->num_sms, ctx->own);
+        for (int r = 0; r < kRoundsPerGraph && ce == cudaSuccess; r++)
+            ce = fill_round(p, sc, r & 1, ctx->num_sms, ctx->own);
         cudaError_t ee = cudaStreamEndCapture(ctx->own, &g);
         if (ce != cudaSuccess) return cuda_fail(ctx, ce, "fill round capture");
         if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill graph capture");
@@ -618,38 +696,223 @@ pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* w
         if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill graph instantiate");
         ctx->fill_graph_key = keybuf;
     }
-    unsigned long long* hp = (unsigned long long*)pinned(ctx, 64, &e);
+    unsigned long long* hp = (unsigned long long*)pinned(ctx, 128, &e);
     if (!hp) return cuda_fail(ctx, e, "pinned counters");
+    int32_t* hc = (int32_t*)(hp + 8);
     int64_t rounds = 0;
-    bool converged = false;
+    *converged = false;
+    CU(ctx, cudaEventRecord(ctx->ev_t0, ctx->own));
     for (;;) {
         CU(ctx, cudaGraphLaunch(ctx->fill_graph, ctx->own));
         rounds += kRoundsPerGraph;
-        int32_t* hc = (int32_t*)hp;
         CU(ctx, cudaMemcpyAsync(hc, sc.counts, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->own));
         CU(ctx, cudaStreamSynchronize(ctx->own));
         if (hc[0] == 0 && hc[1] == 0) {
-            converged = true;
+            *converged = true;
             break;
         }
         if (o.max_rounds > 0 && rounds >= o.max_rounds) break;
     }
+    CU(ctx, cudaEventRecord(ctx->ev_t1, ctx->own));
     CU(ctx, cudaEventRecord(ctx->ev_b, ctx->own));
     CU(ctx, cudaStreamWaitEvent(s, ctx->ev_b, 0));
+    CU(ctx, cudaEventSynchronize(ctx->ev_t1));
+    float ms = 0.0f;
+    CU(ctx, cudaEventElapsedTime(&ms, ctx->ev_t0, ctx->ev_t1));
+    CU(ctx, cudaMemcpy(hp, ctx->d_counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    if (stats) {
+        stats->rounds = rounds;
+        stats->active_rounds = (int64_t)hp[4];
+        stats->tile_visits = (int64_t)hp[1];
+        stats->raised_cells = 0;
+        stats->rounds_ms = ms;
+    }
+    *out_p = p;
+    return PARGO_OK;
+}
+
+pargo_status check_fill_args(pargo_ctx* ctx, const pargo_raster* dem, const pargo_nbr* nbr,
+                             const pargo_fill_opts* opts, pargo_fill_opts* o) {
+    pargo_status st;
+    if ((st = check_raster(ctx, dem, "dem")) != PARGO_OK) return st;
+    if (dem->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: dem must be F32");
+    if ((st = check_dims(ctx, dem)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    *o = pargo_fill_opts{0.0005, 10000.0, 0};
+    if (opts) *o = *opts;
+    if (!(o->gap > 0.0) || !isfinite(o->gap) || !isfinite(o->init_level))
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: gap must be positive and finite");
+    return PARGO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
+                        const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    pargo_fill_opts o;
+    if ((st = check_fill_args(ctx, dem, nbr, opts, &o)) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, wdem, "wdem")) != PARGO_OK) return st;
+    if ((st = check_same(ctx, dem, wdem, "wdem")) != PARGO_OK) return st;
+    if (wdem->dtype != PARGO_F64 && wdem->dtype != PARGO_F32)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: wdem must be F64 or F32");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sdem, sw;
+    if ((st = stage_in(ctx, dem, kSlotIn0, s, &sdem)) != PARGO_OK) return st;
+    if ((st = stage_out(ctx, wdem, kSlotOut0, &sw)) != PARGO_OK) return st;
+    FillParams p;
+    bool converged = false;
+    pargo_fill_stats local{};
+    if ((st = fill_core(ctx, sdem, dem, o, &p, &local, &converged, s)) != PARGO_OK) return st;
     {
         cudaError_t ee = fill_finish(p, sw.out, &ctx->d_counters[3], s);
         if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill finish");
     }
     if ((st = unstage_out(ctx, sw, s)) != PARGO_OK) return st;
-    CU(ctx, cudaMemcpyAsync(hp, ctx->d_counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    cudaError_t e;
+    unsigned long long* hp = (unsigned long long*)pinned(ctx, 128, &e);
+    if (!hp) return cuda_fail(ctx, e, "pinned counters");
+    CU(ctx, cudaMemcpyAsync(hp, &ctx->d_counters[3], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
-    if (stats) {
-        stats->rounds = rounds;
-        stats->tile_visits = (int64_t)hp[1];
-        stats->raised_cells = (int64_t)hp[3];
-    }
+    local.raised_cells = (int64_t)hp[0];
+    if (stats) *stats = local;
     if (!converged)
-        return fail(ctx, PARGO_ERR_NOT_CONVERGED, "fill: worklist not empty after %lld rounds", (long long)rounds);
+        return fail(ctx, PARGO_ERR_NOT_CONVERGED, "fill: worklist not empty after %lld rounds",
+                    (long long)local.rounds);
+    return PARGO_OK;
+}
+
+pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, pargo_raster* slope,
+                                  pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr,
+                                  const pargo_fill_opts* opts, int slope_method, int slope_units, int sca_contract,
+                                  pargo_fill_stats* stats, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    pargo_fill_opts o;
+    if ((st = check_fill_args(ctx, dem, nbr, opts, &o)) != PARGO_OK) return st;
+    if (!wdem && !slope && !d8 && !sca) return fail(ctx, PARGO_ERR_INVALID_ARG, "pipeline: no output requested");
+    if (wdem) {
+        if ((st = check_raster(ctx, wdem, "wdem")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, wdem, "wdem")) != PARGO_OK) return st;
+        if (wdem->dtype != PARGO_F64 && wdem->dtype != PARGO_F32)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "pipeline: wdem must be F64 or F32");
+    }
+    if (slope) {
+        if ((st = check_raster(ctx, slope, "slope")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, slope, "slope")) != PARGO_OK) return st;
+        if (slope->dtype != PARGO_F32 && slope->dtype != PARGO_F64)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "pipeline: slope must be F32 or F64");
+        if (slope_method < 0 || slope_method > 6)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown slope method %d", slope_method);
+        if (slope_units != PARGO_SLOPE_RATIO && slope_units != PARGO_SLOPE_DEGREES)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown slope units %d", slope_units);
+    }
+    if (d8) {
+        if ((st = check_raster(ctx, d8, "d8")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, d8, "d8")) != PARGO_OK) return st;
+        if ((st = check_d8_out(ctx, d8, 8)) != PARGO_OK) return st;
+    }
+    if (sca) {
+        if ((st = check_raster(ctx, sca, "sca")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, sca, "sca")) != PARGO_OK) return st;
+        if (sca->dtype != PARGO_F64 && sca->dtype != PARGO_F32)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "pipeline: sca must be F64 or F32");
+        if (sca_contract != PARGO_SCA_CONVERGED && sca_contract != PARGO_SCA_SHIPPED)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown SCA contract %d", sca_contract);
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sdem, sw, ss, sd, sa;
+    if ((st = stage_in(ctx, dem, kSlotIn0, s, &sdem)) != PARGO_OK) return st;
+    if (wdem && (st = stage_out(ctx, wdem, kSlotOut0, &sw)) != PARGO_OK) return st;
+    if (slope && (st = stage_out(ctx, slope, kSlotOut1, &ss)) != PARGO_OK) return st;
+    if (d8 && (st = stage_out(ctx, d8, kSlotPipeD8, &sd)) != PARGO_OK) return st;
+    if (sca && (st = stage_out(ctx, sca, kSlotPipeSca, &sa)) != PARGO_OK) return st;
+    FillParams p;
+    bool converged = false;
+    pargo_fill_stats local{};
+    if ((st = fill_core(ctx, sdem, dem, o, &p, &local, &converged, s)) != PARGO_OK) return st;
+    if (!converged)
+        return fail(ctx, PARGO_ERR_NOT_CONVERGED, "pipeline fill: worklist not empty after %lld rounds",
+                    (long long)local.rounds);
+    if (wdem) {
+        cudaError_t ee = fill_finish(p, sw.out, &ctx->d_counters[3], s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill finish");
+    }
+    // slope + D8 on the float64 levels (+inf marks their nodata cells)
+    OutView codes{};
+    bool codes_internal = false;
+    if (d8) {
+        codes = sd.out;
+    } else if (sca) {
+        cudaError_t e;
+        char* buf = (char*)slot(ctx, kSlotPipeCodes, (size_t)(p.rows * p.cols), &e);
+        if (!buf) return cuda_fail(ctx, e, "pipeline codes");
+        codes = OutView{buf, p.cols, PARGO_I8, -128.0};
+        codes_internal = true;
+    }
+    if (slope || d8 || sca) {
+        FocalParams f{};
+        f.rows = p.rows;
+        f.cols = p.cols;
+        f.nd6f = Band<float>{INFINITY, INFINITY};
+        f.nd7f = f.nd6f;
+        f.nd6d = Band<double>{INFINITY, INFINITY};  // the levels' nodata is +inf
+        f.nd7d = f.nd6d;
+        f.sk = slope_consts(dem->cellsize, slope_method, slope_units);
+        f.do_slope = slope != nullptr;
+        f.do_d8 = d8 != nullptr || sca != nullptr;
+        f.dir_type = 8;
+        if (slope) f.slope = ss.out;
+        if (f.do_d8) f.d8 = codes;
+        f.fallbacks = &ctx->d_counters[0];
+        f.error_flag = ctx->d_error;
+        CU(ctx, launch_focal_generic(InView{(const char*)p.w, p.cols * 8, PARGO_F64}, f, s));
+    }
+    if (sca) {
+        const int64_t n = p.rows * p.cols;
+        cudaError_t e;
+        ScaScratch sc{};
+        sc.indeg = (int32_t*)slot(ctx, kSlotScaIndeg, (size_t)n * 4, &e);
+        sc.conv = (unsigned long long*)slot(ctx, kSlotScaConv, (size_t)n * 8, &e);
+        sc.ship = (unsigned long long*)slot(ctx, kSlotScaShip, (size_t)n * 8, &e);
+        sc.flags = (uint8_t*)slot(ctx, kSlotScaFlags, (size_t)((n + 3) / 4 * 4), &e);
+        sc.counters = (unsigned long long*)slot(ctx, kSlotScaCounters, 8 * sizeof(unsigned long long), &e);
+        if (!sc.indeg || !sc.conv || !sc.ship || !sc.flags || !sc.counters) return cuda_fail(ctx, e, "sca scratch");
+        ScaParams q{};
+        q.rows = p.rows;
+        q.cols = p.cols;
+        q.d8 = InView{codes.base, codes.pitch, codes.dtype};
+        q.nodata = codes.nodata;
+        q.out = sa.out;
+        q.shipped = sca_contract == PARGO_SCA_SHIPPED;
+        cudaError_t ee = sca_run(q, sc, s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "pipeline sca");
+    }
+    (void)codes_internal;
+    if (wdem && (st = unstage_out(ctx, sw, s)) != PARGO_OK) return st;
+    if (slope && (st = unstage_out(ctx, ss, s)) != PARGO_OK) return st;
+    if (d8 && (st = unstage_out(ctx, sd, s)) != PARGO_OK) return st;
+    if (sca && (st = unstage_out(ctx, sa, s)) != PARGO_OK) return st;
+    cudaError_t e;
+    unsigned long long* hp = (unsigned long long*)pinned(ctx, 128, &e);
+    if (!hp) return cuda_fail(ctx, e, "pinned counters");
+    CU(ctx, cudaMemcpyAsync(hp, &ctx->d_counters[3], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if (sca) {
+        unsigned long long* sc = (unsigned long long*)ctx->slots[kSlotScaCounters].p;
+        CU(ctx, cudaMemcpyAsync(hp + 1, sc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    }
+    if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+    local.raised_cells = wdem ? (int64_t)hp[0] : -1;
+    if (stats) *stats = local;
+    if (sca && hp[1] != hp[2])
+        return fail(ctx, PARGO_ERR_CYCLE, "pipeline sca: %llu of %llu valid cells completed", hp[1], hp[2]);
     return PARGO_OK;
 }
 
@@ -801,8 +1064,8 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
         std::vector<CUtensorMap> maps(all_tma ? count : 0);
         if (all_tma)
             for (int k = 0; k < count; k++)
-                if ((st = make_tma_map(ctx, &maps[k], views[k].base, params[k].rows, params[k].cols, views[k].pitch)) !=
-                    PARGO_OK)
+                if ((st = make_tma_map(ctx, &maps[k], views[k].base, params[k].rows, params[k].cols, views[k].pitch,
+                                       focal_tma_box_rows())) != PARGO_OK)
                     return st;
         CU(ctx, cudaStreamSynchronize(s));
         if (all_tma) CU(ctx, cudaMemcpy(dmaps, maps.data(), count * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
@@ -814,7 +1077,8 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
     }
     CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
     if (all_tma)
-        CU(ctx, launch_batch_tma(dmaps, dparams, dstart, dntx, count, total, fast ? 1 : 0, claim, &ctx->d_counters[0],
+        CU(ctx, launch_batch_tma(dmaps, dparams, dstart, dntx, count, total, fast ? 1 : 0,
+                                 (method == PARGO_SLOPE_FD || !slopes) ? 1 : 0, claim, &ctx->d_counters[0],
                                  ctx->d_error, ctx->num_sms, s));
     else
         CU(ctx, launch_batch_generic(dparams, ddems, dstart, count, total, &ctx->d_counters[0], ctx->num_sms, s));

@@ -71,6 +71,7 @@ struct SlopeConsts {
     float k_tfd;    // 1 / (6 cs)
     float k_tfdw;   // 1 / ((4 + sqrt 8) cs)
     float sqrt2;    // sqrt(2) as float
+    double sqrt2d;  // sqrt(2) as double
     float k_md;     // 1 / (cs * sqrt 2): MD divides by the last-visited (SE) distance
     int method;
     int degrees;
@@ -84,49 +85,96 @@ struct SlopeConsts {
 __device__ __forceinline__ float zdiff(const float* z, int i, int j) { return z[i] - z[j]; }
 __device__ __forceinline__ float zdiff(const double* z, int i, int j) { return (float)__dsub_rn(z[i], z[j]); }
 
+// Numerators of each method in the input's precision: float input keeps
+// them exact (sums of exact neighbour differences of nearby float elevations
+// fit in 24 bits); double input (pit-removed levels, differences of order the
+// gap) combines in FP64 so nothing cancels in float.
 template <typename T>
-__device__ __forceinline__ float slope_from_window(const T* z, const SlopeConsts& k) {
-    float dx, dy, s;
-    switch (k.method) {
-        case PARGO_SLOPE_FD: {  // slopeOperator.cpp:84-86
-            float nx = (zdiff(z, 2, 0) + zdiff(z, 8, 6)) + 2.0f * zdiff(z, 5, 3);
-            float ny = (zdiff(z, 0, 6) + zdiff(z, 2, 8)) + 2.0f * zdiff(z, 1, 7);
-            s = sqrtf(nx * nx + ny * ny) * k.k_fd;
+__device__ __forceinline__ void slope_numerators(const T* z, int method, T& nx, T& ny) {
+    switch (method) {
+        case PARGO_SLOPE_FD:  // slopeOperator.cpp:84-86
+            if constexpr (sizeof(T) == 4) {  // same rounding as the tiled kernel's shared differences
+                nx = __fmaf_rn(2.0f, __fsub_rn(z[5], z[3]), __fadd_rn(__fsub_rn(z[2], z[0]), __fsub_rn(z[8], z[6])));
+                ny = __fmaf_rn(2.0f, __fsub_rn(z[1], z[7]), __fadd_rn(__fsub_rn(z[0], z[6]), __fsub_rn(z[2], z[8])));
+            } else {
+                nx = ((z[2] - z[0]) + (z[8] - z[6])) + (T)2 * (z[5] - z[3]);
+                ny = ((z[0] - z[6]) + (z[2] - z[8])) + (T)2 * (z[1] - z[7]);
+            }
             break;
-        }
         case PARGO_SLOPE_FFD:  // :88-90
-            dx = (zdiff(z, 8, 6) + zdiff(z, 2, 0)) * k.k_ffd;
-            dy = (zdiff(z, 0, 6) + zdiff(z, 2, 8)) * k.k_ffd;
-            s = sqrtf(dx * dx + dy * dy);
+            nx = (z[8] - z[6]) + (z[2] - z[0]);
+            ny = (z[0] - z[6]) + (z[2] - z[8]);
             break;
-        case PARGO_SLOPE_MD: {  // :92-103, divided by the last-visited (SE) distance
-            float m = 0.0f;
+        case PARGO_SLOPE_MD: {  // :92-103 (max drop; divided by the last-visited SE distance below)
+            T m = 0;
 #pragma unroll
             for (int i = 0; i < 9; i++)
-                if (i != 4) m = fmaxf(m, zdiff(z, 4, i));
-            s = m * k.k_md;
+                if (i != 4 && z[4] - z[i] > m) m = z[4] - z[i];
+            nx = m;
+            ny = 0;
             break;
         }
         case PARGO_SLOPE_SD:  // :122-124
-            dx = zdiff(z, 4, 3) * k.k_sd;
-            dy = zdiff(z, 4, 7) * k.k_sd;
-            s = sqrtf(dx * dx + dy * dy);
+            nx = z[4] - z[3];
+            ny = z[4] - z[7];
             break;
         case PARGO_SLOPE_SFD:  // :126-128
-            dx = zdiff(z, 5, 3) * k.k_sfd;
-            dy = zdiff(z, 1, 7) * k.k_sfd;
-            s = sqrtf(dx * dx + dy * dy);
+            nx = z[5] - z[3];
+            ny = z[1] - z[7];
             break;
         case PARGO_SLOPE_TFD:  // :130-132; dy uses z[6] twice, as the reference does
-            dx = (zdiff(z, 8, 0) + zdiff(z, 5, 3) + zdiff(z, 2, 6)) * k.k_tfd;
-            dy = (zdiff(z, 2, 6) + zdiff(z, 1, 7) + zdiff(z, 0, 6)) * k.k_tfd;
-            s = sqrtf(dx * dx + dy * dy);
+            nx = (z[8] - z[0]) + (z[5] - z[3]) + (z[2] - z[6]);
+            ny = (z[2] - z[6]) + (z[1] - z[7]) + (z[0] - z[6]);
             break;
-        default:  // TFDW :134-136
-            dx = (zdiff(z, 8, 6) + zdiff(z, 2, 0) + k.sqrt2 * zdiff(z, 5, 3)) * k.k_tfdw;
-            dy = (zdiff(z, 2, 6) + zdiff(z, 0, 8) + k.sqrt2 * zdiff(z, 1, 7)) * k.k_tfdw;
-            s = sqrtf(dx * dx + dy * dy);
+        default:  // TFDW :134-136: sqrt(2) multiplies differences, not raw levels
+            nx = (z[8] - z[6]) + (z[2] - z[0]);
+            ny = (z[2] - z[6]) + (z[0] - z[8]);
             break;
+    }
+}
+
+// Square root by the SFU's approximate instruction (relative error ~2^-23,
+// far inside the 1e-5 slope tolerance); 0 stays 0.
+__device__ __forceinline__ float sqrt_sfu(float q) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(q));
+    return r;
+}
+
+// Horn slope from its two numerators: k sqrt(nx^2 + ny^2), with the rounding
+// pinned (explicit fma / mul) so every kernel produces the same bits.
+__device__ __forceinline__ float horn_slope(float nx, float ny, float k) {
+    return __fmul_rn(sqrt_sfu(__fmaf_rn(nx, nx, __fmul_rn(ny, ny))), k);
+}
+
+template <typename T>
+__device__ __forceinline__ float slope_from_window(const T* z, const SlopeConsts& k) {
+    T nx, ny;
+    slope_numerators(z, k.method, nx, ny);
+    float s;
+    switch (k.method) {
+        case PARGO_SLOPE_FD:
+            s = horn_slope((float)nx, (float)ny, k.k_fd);
+            break;
+        case PARGO_SLOPE_MD:
+            s = (float)nx * k.k_md;
+            break;
+        case PARGO_SLOPE_TFDW: {
+            const T s2 = (T)k.sqrt2d;
+            const float fx = (float)(nx + s2 * (z[5] - z[3])) * k.k_tfdw;
+            const float fy = (float)(ny + s2 * (z[1] - z[7])) * k.k_tfdw;
+            s = sqrtf(fx * fx + fy * fy);
+            break;
+        }
+        default: {
+            const float kk = k.method == PARGO_SLOPE_FFD ? k.k_ffd
+                           : k.method == PARGO_SLOPE_SD  ? k.k_sd
+                           : k.method == PARGO_SLOPE_SFD ? k.k_sfd
+                                                         : k.k_tfd;
+            const float fx = (float)nx * kk, fy = (float)ny * kk;
+            s = sqrtf(fx * fx + fy * fy);
+            break;
+        }
     }
     if (k.degrees) s = atanf(s) * 57.29577951308232f;
     return s;
@@ -171,47 +219,91 @@ __device__ __forceinline__ int d8_code_from_mask(unsigned mask, int dir_type) {
            ((mask >> 3) & 1) * 16 + ((mask >> 0) & 1) * 32 + ((mask >> 1) & 1) * 64 + ((mask >> 2) & 1) * 128;
 }
 
-// Certified FP32 D8 decision.
-//   c_i = fl32(z4 - z_i); diagonal x_i = fl32(c_i * fl32(1/sqrt 2)), cardinal x_i = c_i.
-// Against the reference's double r_i = fl64(d4 - d_i) [/ fl64(sqrt 2)],
-// |x_i - r_i| <= |x_i| 2^-22 (three float roundings of relative 2^-24 and the
-// constant's error; the double roundings are 2^-53).  With E = 2^-21 max|x_i|
-// (twice that bound), the reference max M_ref = max(0, r_i) is within E/2 of
-// M = max(0, x_i), and each tie test |r_i - M_ref| < 1e-6 is decided exactly
-// when u_i = x_i - (M - 1e-6) is further than 3E from zero (the float rounding
-// of u and of M - 1e-6 is below E/2 because E >= 2^-21 M).  Returns the code,
-// or kD8Unsure when some decision lies inside its error band.
+// Certified FP32 D8 decision, reproducing the reference's FP64 decisions.
+//
+// The reference (d8Operator.cpp:64-97) forms r_i = fl64(d4 - d_i), divides the
+// diagonals by fl64(sqrt 2), takes M = max(0, r_i), returns -1 when M < 1e-6
+// and otherwise the set T = { i : |r_i - M| < 1e-6 }.  Here
+//   x_i = fl32(d4 - d_i), times fl32(1/sqrt 2) for diagonals,
+// with |x_i - r_i| <= 2^-22 |x_i| (three float roundings of 2^-24 and the
+// constant's; the double roundings are 2^-53).  Decisions are taken in FP32
+// only where they are certain under those bounds:
+//  * every x_i <= 0: all r_i <= 0 (rounding keeps signs), M = 0, code -1;
+//  * M against 1e-6: |x_k - r_k| <= 2^-22 x_k for the argmax k;
+//  * a clear single maximum (second largest further than 1e-6 plus both
+//    error bounds below it): T = {k};
+//  * otherwise the near ties are re-measured from direct differences (exact
+//    for two cardinals or two diagonals, which is where exact ties occur) in
+//    d8_certified_ties below.
+// Anything still inside an error band returns kD8Unsure and the caller runs
+// the exact FP64 restatement d8_exact.
 constexpr int kD8Unsure = 0x7fff;
-__device__ __forceinline__ int d8_certified(const float c[9], int dir_type) {
+constexpr float kTLo = 0.99996948e-6f, kTHi = 1.0000305e-6f;  // 1e-6 widened by 2^-15 relative
+constexpr float k2m22 = 2.384185791015625e-07f;                 // 2^-22
+constexpr float k2m20 = 9.5367431640625e-07f;                   // 2^-20
+
+PARGO_HD bool is_diag(int i) { return i == 0 || i == 2 || i == 6 || i == 8; }
+
+__device__ __forceinline__ int d8_bit_code(int k) {
+    // ArcGIS-style weight of window index k (d8Operator.cpp:96-97)
+    const int w[9] = {32, 64, 128, 16, 0, 1, 8, 4, 2};
+    return w[k];
+}
+
+// Near-tie resolution: k is the FP32 argmax (value m); T is built from
+// g_i = r_k - r_i measured directly.  Same-type pairs: g = d_i - d_k (times
+// 1/sqrt 2 for diagonals), error <= 2^-22 g + 2^-48 m (the reference's own
+// roundings of r_i, r_k).  Mixed pairs: g = m - x_i, error <= 2^-21 (m + |x_i|).
+template <typename T>
+__device__ __noinline__ int d8_certified_ties(const T* z, const float* x, int k, float m, int dir_type) {
     const float kinv = 0.70710677f;
-    // Threshold 1e-6 widened by 2^-15 relative on each side: covers the
-    // distance between fl32(1e-6) and the double literal.
-    const float t_lo = 0.99996948e-6f, t_hi = 1.0000305e-6f;
-    float x[9];
-    float m = 0.0f, a = 0.0f;
-#pragma unroll
+    const bool kd = is_diag(k);
+    unsigned mask = 1u << k;
     for (int i = 0; i < 9; i++) {
-        if (i == 4) continue;
-        x[i] = (i == 0 || i == 2 || i == 6 || i == 8) ? c[i] * kinv : c[i];
-        m = fmaxf(m, x[i]);
-        a = fmaxf(a, fabsf(x[i]));
+        if (i == 4 || i == k) continue;
+        float g, err;
+        if (is_diag(i) == kd) {
+            g = zdiff(z, i, k);
+            if (kd) g *= kinv;
+            err = fabsf(g) * k2m22 + m * 3.5527136788005009e-15f;  // 2^-48 m
+            if (g < 0.0f || (g > 0.0f && g <= err)) return kD8Unsure;  // the reference max may be i
+        } else {
+            g = m - x[i];
+            err = (m + fabsf(x[i])) * 4.76837158203125e-07f;  // 2^-21
+            if (g <= err) return kD8Unsure;
+        }
+        if (g + err < kTLo) mask |= 1u << i;
+        else if (!(g - err > kTHi)) return kD8Unsure;
     }
-    const float e = a * 4.76837158203125e-07f;  // 2^-21
-    if (m + e < t_lo) return -1;
-    if (!(m - e > t_hi)) return kD8Unsure;
-    const float thr = m - 1.0e-6f;
-    const float err = 3.0f * e;
-    unsigned mask = 0;
-    float close = 3.0e38f;
-#pragma unroll
-    for (int i = 0; i < 9; i++) {
-        if (i == 4) continue;
-        float u = x[i] - thr;
-        close = fminf(close, fabsf(u));
-        mask |= (u > 0.0f ? 1u : 0u) << i;
-    }
-    if (close <= err) return kD8Unsure;
     return d8_code_from_mask(mask, dir_type);
+}
+
+template <typename T>
+__device__ __forceinline__ int d8_certified(const T* z, int dir_type) {
+    const float kinv = 0.70710677f;
+    float x[9];
+    float m = -3.0e38f, m2 = -3.0e38f;
+    int k = 0;
+#pragma unroll
+    for (int i = 0; i < 9; i++) {
+        if (i == 4) continue;
+        const float c = zdiff(z, 4, i);
+        x[i] = is_diag(i) ? c * kinv : c;
+        if (x[i] > m) {
+            m2 = m;
+            m = x[i];
+            k = i;
+        } else {
+            m2 = fmaxf(m2, x[i]);
+        }
+    }
+    if (m <= 0.0f) return -1;
+    const float em = m * k2m22;
+    if (m + em < kTLo) return -1;
+    if (!(m - em > kTHi)) return kD8Unsure;
+    if (m - m2 > kTHi + (m + fabsf(m2)) * k2m20) return dir_type == 8 ? k : d8_bit_code(k);
+    x[4] = 0.0f;
+    return d8_certified_ties(z, x, k, m, dir_type);
 }
 
 }  // namespace pargo

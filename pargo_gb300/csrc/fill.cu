@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
     int32_t* next_count = &s.counts[parity ^ 1];
     const int32_t ncur = *((volatile int32_t*)cur_count);
     const int tid = threadIdx.x;
+    if (blockIdx.x == 0 && tid == 0 && ncur > 0) atomicAdd(s.active, 1ULL);
     const int lr = tid >> 3;            // local row 0..31
     const int lc0 = (tid & 7) * 4;      // local cols lc0..lc0+3
 

@@ -31,8 +31,10 @@ struct FocalParams {
 };
 
 // focal.cu
-cudaError_t launch_focal_tma(const CUtensorMap* map, const FocalParams& p, int fast_out, int num_sms,
+cudaError_t launch_focal_tma(const CUtensorMap* map, const FocalParams& p, int fast_out, int variant, int num_sms,
                              cudaStream_t s);
+int focal_num_variants();
+int focal_variant_rows(int v);  // tile rows of variant v (its TMA box is that + 2)
 cudaError_t launch_focal_generic(const InView& dem, const FocalParams& p, cudaStream_t s);
 size_t focal_tma_smem_bytes();
 int focal_tma_tile_rows();
@@ -42,7 +44,7 @@ int focal_tma_box_rows();
 
 // Batched slope+D8 (focal.cu): device tables of per-raster descriptors/params.
 cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params, const int64_t* tile_start,
-                             const int64_t* ntx_of, int count, int64_t total_tiles, int fast_out,
+                             const int64_t* ntx_of, int count, int64_t total_tiles, int fast_out, int fd,
                              unsigned long long* claim, unsigned long long* fallbacks, int* error_flag, int num_sms,
                              cudaStream_t s);
 cudaError_t launch_batch_generic(const FocalParams* params, const InView* dems, const int64_t* cell_start, int count,
@@ -65,6 +67,7 @@ struct FillScratch {
     int32_t* queued;        // per-tile flag: already in the next worklist
     unsigned long long* visits;
     unsigned long long* changed;
+    unsigned long long* active;  // rounds that found a non-empty worklist
 };
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st);
 cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st);

@@ -36,9 +36,23 @@ def host(t):
     return t.cpu().numpy()
 
 
-def slope_close(gpu, ref, nodata=-9999.0, rtol=SLOPE_RTOL):
-    """Same nodata cells; relative error within rtol on the others.  Returns
-    (ok, max_rel, mean_rel)."""
+def ref_noise_floor(dem, cellsize):
+    """Absolute rounding bound of the reference's own FP64 slope: it sums raw
+    elevations (slopeOperator.cpp:84-136), so where the exact answer is ~0 its
+    result is rounding residue of order 2^-52 * (sum of |weights * elevations|)
+    / (denominator * cellsize).  The weights of every method sum to <= 8 in
+    magnitude, the denominators are >= 1; 2^-48 leaves a 16x margin."""
+    z = np.asarray(dem, np.float64)
+    v = z[np.isfinite(z) & (z != -9999.0)]
+    zmax = float(np.abs(v).max()) if v.size else 0.0
+    return 2.0 ** -48 * 8.0 * zmax / float(np.float32(cellsize))
+
+
+def slope_close(gpu, ref, nodata=-9999.0, rtol=SLOPE_RTOL, atol=0.0):
+    """Same nodata cells; |gpu - ref| <= rtol |ref| + atol on the others, where
+    atol is the reference's own rounding floor (ref_noise_floor).  Returns
+    (ok, max_rel, mean_rel) with the relative error taken over cells whose
+    reference value is above atol."""
     gpu = np.asarray(gpu, np.float64)
     ref = np.asarray(ref, np.float64)
     nd_g = gpu == nodata
@@ -50,8 +64,10 @@ def slope_close(gpu, ref, nodata=-9999.0, rtol=SLOPE_RTOL):
         return True, 0.0, 0.0
     err = np.abs(gpu[v] - ref[v])
     scale = np.abs(ref[v])
-    rel = np.where(scale > 0, err / np.where(scale > 0, scale, 1), np.where(err > 0, np.inf, 0.0))
-    return bool((rel <= rtol).all()), float(rel.max()), float(rel.mean())
+    ok = bool((err <= rtol * scale + atol).all())
+    big = scale > max(atol, 0.0) * 1e3 if atol > 0 else scale > 0
+    rel = err[big] / scale[big] if big.any() else np.zeros(1)
+    return ok, float(rel.max()), float(rel.mean())
 
 
 def d8_as_f64(codes, nodata_in, nodata_out=-9999.0):

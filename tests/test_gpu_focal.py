@@ -9,7 +9,7 @@ import pytest
 import torch
 
 from conftest import GOLDEN_CASES, bits_equal, load_golden
-from gpu_helpers import SLOPE_RTOL, d8_as_f64, dev, empty_dev, host, slope_close
+from gpu_helpers import SLOPE_RTOL, d8_as_f64, dev, empty_dev, host, ref_noise_floor, slope_close
 from pargo_gb300 import abi, synth
 
 pytestmark = pytest.mark.gpu
@@ -24,7 +24,7 @@ def test_golden_slope_all_methods(case, align, ctx):
     for m in range(7):
         out = empty_dev(dem.shape, np.float32, align)
         ctx.slope(abi.raster(d, nd, cs), abi.raster(out, nd, cs), method=m)
-        ok, mx, mean = slope_close(host(out), g["slope_m%d" % m], nd)
+        ok, mx, mean = slope_close(host(out), g["slope_m%d" % m], nd, atol=ref_noise_floor(dem, cs))
         assert ok, "method %d max rel %g" % (m, mx)
 
 
@@ -71,7 +71,7 @@ def test_golden_d8_on_filled_surface(case, ctx):
     ctx.slope(abi.raster(dev(w), nd, float(g["cellsize"])), abi.raster(s, nd))
     import oracle
     ref = oracle.Oracle().slope(w, nd, float(g["cellsize"]))
-    ok, mx, _ = slope_close(host(s), ref, nd)
+    ok, mx, _ = slope_close(host(s), ref, nd, atol=ref_noise_floor(w, float(g["cellsize"])))
     assert ok, mx
 
 

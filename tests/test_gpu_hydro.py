@@ -63,9 +63,15 @@ def test_fill_options_and_round_cap(ctx, oracle_lib):
     w = empty_dev(dem.shape, np.float64)
     ctx.fill(abi.raster(dev(dem), -9999.0), abi.raster(w, -9999.0), gap=1e-3)
     assert bits_equal(host(w), oracle_lib.fill(dem, -9999.0, gap=1e-3))
+    big = synth.hydro_dem(1024, 1024, seed=42, blob_fraction=0.0)
+    wb = empty_dev(big.shape, np.float64)
     with pytest.raises(abi.PargoError) as e:
-        ctx.fill(abi.raster(dev(dem), -9999.0), abi.raster(w, -9999.0), max_rounds=1)
+        ctx.fill(abi.raster(dev(big), -9999.0), abi.raster(wb, -9999.0), max_rounds=2)
     assert e.value.status_name == "PARGO_ERR_NOT_CONVERGED"
+    # the context stays usable, and an uncapped run converges to the oracle's bytes
+    st = ctx.fill(abi.raster(dev(big), -9999.0), abi.raster(wb, -9999.0))
+    assert st.rounds > 2
+    assert bits_equal(host(wb), oracle_lib.fill(big, -9999.0))
 
 
 def test_fill_edge_cases(ctx, oracle_lib):
@@ -164,3 +170,34 @@ def test_full_size_sca_conservation(ctx):
     tgt_valid[inside] = valid[tr[inside], tq[inside]]
     terminal = ~tgt_valid
     assert int(sca[r[terminal], q[terminal]].sum()) == int(valid.sum())
+
+
+@pytest.mark.parametrize("host_io", [False, True])
+def test_hydro_pipeline_matches_separate_calls_and_oracle(host_io, ctx, oracle_lib):
+    """pargo_hydro_pipeline (fill -> slope + D8 on the float64 levels -> SCA)
+    equals the oracle's chain, with device or host buffers."""
+    dem = synth.hydro_dem(700, 530, seed=51)
+    nd = -9999.0
+    shape = dem.shape
+    if host_io:
+        src = dem
+        w, s, c, a = (np.empty(shape, np.float32), np.empty(shape, np.float32), np.empty(shape, np.int8),
+                      np.empty(shape, np.float64))
+        get = lambda x: x
+    else:
+        src = dev(dem)
+        w, s, c, a = (empty_dev(shape, np.float32), empty_dev(shape, np.float32), empty_dev(shape, np.int8),
+                      empty_dev(shape, np.float64))
+        get = host
+    st = ctx.hydro_pipeline(abi.raster(src, nd, 30.0), wdem=abi.raster(w, nd), slope=abi.raster(s, nd),
+                            d8=abi.raster(c, -128), sca=abi.raster(a, nd), gap=1e-3)
+    wref = oracle_lib.fill(dem, nd, gap=1e-3)
+    assert np.array_equal(get(w), wref.astype(np.float32))
+    d8ref = oracle_lib.d8(wref, nd)
+    assert bits_equal(d8_as_f64(get(c), -128), d8ref)
+    from gpu_helpers import ref_noise_floor, slope_close
+    ok, mx, _ = slope_close(get(s), oracle_lib.slope(wref, nd, 30.0), nd, atol=ref_noise_floor(wref, 30.0))
+    assert ok, mx
+    assert bits_equal(get(a), oracle_lib.sca(d8ref, nd))
+    assert st.active_rounds >= 1 and st.rounds >= st.active_rounds and st.rounds_ms > 0
+    assert st.raised_cells == int((wref[wref != nd] > dem[wref != nd]).sum())
