@@ -201,6 +201,22 @@ pargo_status pargo_slope_bwd(pargo_ctx* ctx, const pargo_raster* z, const pargo_
 pargo_status pargo_slope_loss_grad(pargo_ctx* ctx, const pargo_raster* z, const pargo_raster* z_ref,
                                    pargo_raster* gz, double* loss, const pargo_nbr* nbr, void* stream);
 
+/* SCA without any device allocation, for callers that cannot allocate (a
+ * plugin handed only device buffers and a stream, a host runtime that owns the
+ * whole device-memory budget, code that must not take the allocator's locks).
+ * No counterpart in the reference: same results as pargo_sca, but the scratch
+ * is a fixed array inside the library's device image instead of a context, so
+ * there is no context argument.  Rasters must be on the device and hold at
+ * most PARGO_SCA_NOALLOC_MAX_CELLS cells (larger ones: PARGO_ERR_INVALID_ARG);
+ * the array (21 bytes per cell, ~22 MB) stays allocated on every GPU that loads
+ * the library until the process exits.  All calls share that array: calls that
+ * overlap on the GPU race, so serialise them.  The first call on a device looks
+ * up the array's address (once per device); make it before any stream capture.
+ * Synchronous: returns after the result and the completion count are known. */
+#define PARGO_SCA_NOALLOC_MAX_CELLS (1LL << 20)
+pargo_status pargo_sca_noalloc(const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr, int contract,
+                               void* stream);
+
 /* Number of D8 cells of the last slope+D8/D8 call that took the exact FP64
  * path (the FP32 decision was not certified), for diagnostics. */
 int64_t pargo_last_d8_fallbacks(const pargo_ctx* ctx);

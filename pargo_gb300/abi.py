@@ -82,6 +82,8 @@ def lib():
         L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
         L.pargo_slope_bwd.argtypes = [vp, R, R, R, N, vp]
         L.pargo_slope_loss_grad.argtypes = [vp, R, R, R, P(ctypes.c_double), N, vp]
+        L.pargo_sca_noalloc.argtypes = [R, R, N, i, vp]
+        L.pargo_sca_noalloc.restype = st
         L.pargo_tune_focal.argtypes = [vp, R, i, P(i), P(ctypes.c_float), i]
         L.pargo_tune_focal.restype = st
         L.pargo_last_d8_fallbacks.argtypes = [vp]
