@@ -157,7 +157,7 @@ pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps,
                               int max_times);
 
 /* Planchon-Darboux pit removal: the fixpoint the reference's Gauss-Seidel
- * sweeps reach (any visiting order reaches the same one).  dem: F32;
+ * sweeps reach (any visiting order reaches the same one).  dem: F32 or F64;
  * wdem: F64 (the reference's values) or F32 (those values rounded to float).
  * opts may be NULL (reference constants); stats may be NULL. */
 pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,

@@ -304,7 +304,7 @@ pargo_status unstage_out(pargo_ctx* ctx, const Staged& s, cudaStream_t st) {
 }
 
 pargo_status make_tma_map(pargo_ctx* ctx, CUtensorMap* map, const void* base, int64_t rows, int64_t cols,
-                          int64_t pitch, int box_rows) {
+                          int64_t pitch, int box_rows, int box_cols = 0, bool f64 = false) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         cudaDriverEntryPointQueryResult q;
@@ -316,9 +316,9 @@ pargo_status make_tma_map(pargo_ctx* ctx, CUtensorMap* map, const void* base, in
     }
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)pitch};
-    cuuint32_t box[2] = {(cuuint32_t)focal_tma_box_cols(), (cuuint32_t)box_rows};
+    cuuint32_t box[2] = {(cuuint32_t)(box_cols ? box_cols : focal_tma_box_cols()), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
+    CUresult r = encode(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(ctx, PARGO_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
@@ -436,7 +436,18 @@ pargo_status focal_impl(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* s
     p.error_flag = ctx->d_error;
     CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
 
-    if (tma_ok(sdem.in)) {
+    const bool f64_tma = sdem.in.dtype == PARGO_F64 && (uintptr_t)sdem.in.base % 16 == 0 && sdem.in.pitch % 16 == 0;
+    if (f64_tma) {
+        Focal64Params q{};
+        q.f = p;
+        q.wpitch = sdem.in.pitch;
+        q.nodata_is_inf = 0;
+        CUtensorMap map;
+        if ((st = make_tma_map(ctx, &map, sdem.in.base, p.rows, p.cols, sdem.in.pitch, focal64_tile_rows() + 2,
+                               focal64_box_cols(), true)) != PARGO_OK)
+            return st;
+        CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s));
+    } else if (tma_ok(sdem.in)) {
         const int v = pick_variant(ctx, p.rows * p.cols);
         CUtensorMap map;
         if ((st = make_tma_map(ctx, &map, sdem.in.base, p.rows, p.cols, sdem.in.pitch, focal_variant_rows(v) + 2)) !=
@@ -637,9 +648,11 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     FillParams p{};
     p.rows = rows;
     p.cols = cols;
-    p.dem = (const float*)sdem.in.base;
+    p.dem = sdem.in.base;
     p.dem_pitch = sdem.in.pitch;
+    p.dem_f64 = dem->dtype == PARGO_F64;
     p.nd6f = float_band(dem->nodata, kEpsHydro);
+    p.nd6d = double_band(dem->nodata, kEpsHydro);
     p.gap = o.gap;
     p.init_level = o.init_level;
     p.tiles_y = (rows + T - 1) / T;
@@ -647,7 +660,8 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     if (ntiles >= INT32_MAX) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: raster too large");
     cudaError_t e;
-    p.w = (double*)slot(ctx, kSlotFillW, (size_t)n * sizeof(double), &e);
+    p.w_stride = (cols + 1) / 2 * 2;  // 16-byte rows: the levels can be TMA-loaded
+    p.w = (double*)slot(ctx, kSlotFillW, (size_t)(rows * p.w_stride) * sizeof(double), &e);
     if (!p.w) return cuda_fail(ctx, e, "fill levels");
     int32_t* lists = (int32_t*)slot(ctx, kSlotFillLists, (size_t)(2 * ntiles + 8) * sizeof(int32_t), &e);
     if (!lists) return cuda_fail(ctx, e, "fill worklists");
@@ -675,9 +689,9 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     CU(ctx, cudaEventRecord(ctx->ev_a, s));
     CU(ctx, cudaStreamWaitEvent(ctx->own, ctx->ev_a, 0));
     char keybuf[256];
-    snprintf(keybuf, sizeof(keybuf), "%p %p %p %p %lld %lld %a %a %a %a %lld %d", (void*)p.w, (void*)p.dem,
+    snprintf(keybuf, sizeof(keybuf), "%p %p %p %p %lld %lld %a %a %a %a %a %a %lld %d %d", (void*)p.w, p.dem,
              (void*)lists, (void*)queued, (long long)rows, (long long)cols, p.gap, p.init_level, (double)p.nd6f.lo,
-             (double)p.nd6f.hi, (long long)p.dem_pitch, kRoundsPerGraph);
+             (double)p.nd6f.hi, p.nd6d.lo, p.nd6d.hi, (long long)p.dem_pitch, p.dem_f64, kRoundsPerGraph);
     if (!ctx->fill_graph || ctx->fill_graph_key != keybuf) {
         if (ctx->fill_graph) {
             cudaGraphExecDestroy(ctx->fill_graph);
@@ -735,7 +749,8 @@ pargo_status check_fill_args(pargo_ctx* ctx, const pargo_raster* dem, const parg
                              const pargo_fill_opts* opts, pargo_fill_opts* o) {
     pargo_status st;
     if ((st = check_raster(ctx, dem, "dem")) != PARGO_OK) return st;
-    if (dem->dtype != PARGO_F32) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: dem must be F32");
+    if (dem->dtype != PARGO_F32 && dem->dtype != PARGO_F64)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: dem must be F32 or F64");
     if ((st = check_dims(ctx, dem)) != PARGO_OK) return st;
     if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
     *o = pargo_fill_opts{0.0005, 10000.0, 0};
@@ -841,11 +856,13 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
     if (!converged)
         return fail(ctx, PARGO_ERR_NOT_CONVERGED, "pipeline fill: worklist not empty after %lld rounds",
                     (long long)local.rounds);
-    if (wdem) {
+    const bool focal = slope || d8 || sca;
+    if (wdem && !focal) {
         cudaError_t ee = fill_finish(p, sw.out, &ctx->d_counters[3], s);
         if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill finish");
     }
-    // slope + D8 on the float64 levels (+inf marks their nodata cells)
+    // slope + D8 on the float64 levels (+inf marks their nodata cells); the
+    // same pass copies the levels out as the filled DEM
     OutView codes{};
     bool codes_internal = false;
     if (d8) {
@@ -873,7 +890,21 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
         if (f.do_d8) f.d8 = codes;
         f.fallbacks = &ctx->d_counters[0];
         f.error_flag = ctx->d_error;
-        CU(ctx, launch_focal_generic(InView{(const char*)p.w, p.cols * 8, PARGO_F64}, f, s));
+        Focal64Params q{};
+        q.f = f;
+        q.wpitch = p.w_stride * 8;
+        q.nodata_is_inf = 1;
+        q.do_copy = wdem != nullptr;
+        if (wdem) q.copy = sw.out;
+        q.raised = &ctx->d_counters[3];
+        q.dem = p.dem;
+        q.dem_pitch = p.dem_pitch;
+        q.dem_f64 = p.dem_f64;
+        CUtensorMap map;
+        if ((st = make_tma_map(ctx, &map, p.w, p.rows, p.cols, q.wpitch, focal64_tile_rows() + 2, focal64_box_cols(),
+                               true)) != PARGO_OK)
+            return st;
+        CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s));
     }
     if (sca) {
         const int64_t n = p.rows * p.cols;

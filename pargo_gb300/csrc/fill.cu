@@ -61,8 +61,13 @@ __device__ __forceinline__ int64_t add_gap(int64_t k, double gap) {
     return dkey(__dadd_rn(dval(k), gap));
 }
 
-__device__ __forceinline__ const float* dem_row(const FillParams& p, int64_t r) {
-    return reinterpret_cast<const float*>(reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch);
+// DEM value (float32 or float64 input) and its nodata test (Eps 1e-6).
+__device__ __forceinline__ double dem_at(const FillParams& p, int64_t r, int64_t c) {
+    const char* row = reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch;
+    return p.dem_f64 ? reinterpret_cast<const double*>(row)[c] : (double)reinterpret_cast<const float*>(row)[c];
+}
+__device__ __forceinline__ bool dem_nodata(const FillParams& p, double z) {
+    return p.dem_f64 ? p.nd6d.has(z) : p.nd6f.has((float)z);
 }
 
 __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
@@ -72,22 +77,22 @@ __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
         double w = INFINITY;
         const bool inner = r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
         if (inner) {
-            const float z = dem_row(p, r)[c];
-            if (!p.nd6f.has(z)) {
+            const double z = dem_at(p, r, c);
+            if (!dem_nodata(p, z)) {
                 w = p.init_level;
-                if (p.init_level > (double)z) {
+                if (p.init_level > z) {
                     bool outlet = false;
                     for (int a = -1; a <= 1; a++)
                         for (int b = -1; b <= 1; b++) {
                             const int64_t rr = r + a, cc = c + b;
                             const bool ring = rr <= 0 || cc <= 0 || rr >= p.rows - 1 || cc >= p.cols - 1;
-                            if (ring || p.nd6f.has(dem_row(p, rr)[cc])) outlet = true;
+                            if (ring || dem_nodata(p, dem_at(p, rr, cc))) outlet = true;
                         }
-                    if (outlet) w = (double)z;
+                    if (outlet) w = z;
                 }
             }
         }
-        p.w[i] = w;
+        p.w[r * p.w_stride + c] = w;
     }
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
@@ -143,7 +148,7 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
             const int a = i / kH, b = i % kH;
             const int64_t r = y0 + a, c = x0 + b;
             int64_t k = kKeyInf;
-            if (r >= 0 && c >= 0 && r < p.rows && c < p.cols) k = dkey(((volatile double*)p.w)[r * p.cols + c]);
+            if (r >= 0 && c >= 0 && r < p.rows && c < p.cols) k = dkey(((volatile double*)p.w)[r * p.w_stride + c]);
             lv[a][b] = k;
         }
         __syncthreads();
@@ -158,8 +163,7 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
             act[j] = false;
             zk[j] = 0;
             if (gr < p.rows - 1 && gc < p.cols - 1 && gr > 0 && gc > 0) {
-                const float z = dem_row(p, gr)[gc];
-                zk[j] = dkey((double)z);
+                zk[j] = dkey(dem_at(p, gr, gc));
                 act[j] = orig[j] < kKeyInf && orig[j] > zk[j];
             }
         }
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
             const int a = lr + 1, b = lc0 + 1 + j;
             const int64_t v = lv[a][b];
             if (v != orig[j]) {
-                p.w[gr * p.cols + (x0 + b)] = dval(v);
+                p.w[gr * p.w_stride + (x0 + b)] = dval(v);
                 if (lr == 0) e |= 1;
                 if (lr == kT - 1) e |= 2;
                 if (b == 1) e |= 4;
@@ -256,9 +260,9 @@ __global__ void fill_finish_kernel(const FillParams p, const OutView out, unsign
     unsigned long long cnt = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = i / p.cols, c = i % p.cols;
-        const double w = p.w[i];
+        const double w = p.w[r * p.w_stride + c];
         const bool nd = isinf(w);
-        if (!nd && w > (double)dem_row(p, r)[c]) cnt++;
+        if (!nd && w > dem_at(p, r, c)) cnt++;
         put_value(out, r, c, nd ? out.nodata : w);
     }
     cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);

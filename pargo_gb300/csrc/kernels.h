@@ -50,14 +50,34 @@ cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params,
 cudaError_t launch_batch_generic(const FocalParams* params, const InView* dems, const int64_t* cell_start, int count,
                                  int64_t total_cells, unsigned long long* fallbacks, int num_sms, cudaStream_t s);
 
+// focal64.cu: slope + D8 over a float64 surface (the pit-removed levels),
+// TMA-tiled; optionally copies the levels to `copy` (the filled-DEM output).
+struct Focal64Params {
+    FocalParams f;          // rows, cols, outputs, slope constants, dir_type
+    int64_t wpitch;         // bytes per row of the levels
+    int nodata_is_inf;      // the levels mark nodata with +inf (the pipeline) instead of a band
+    int do_copy;
+    OutView copy;           // filled-DEM output (+inf written as copy.nodata)
+    unsigned long long* raised;  // cells whose level is above the DEM (needs dem), may be null
+    const void* dem;
+    int64_t dem_pitch;
+    int dem_f64;
+};
+cudaError_t launch_focal64_tma(const CUtensorMap* map, const Focal64Params& p, int num_sms, cudaStream_t s);
+int focal64_tile_rows();
+int focal64_box_cols();
+
 // fill.cu
 struct FillParams {
     int64_t rows, cols;
-    const float* dem;
+    const void* dem;        // float32 or float64 (dem_f64)
     int64_t dem_pitch;      // bytes
-    Band<float> nd6f;       // nodata band of the DEM (Eps 1e-6)
+    int dem_f64;
+    Band<float> nd6f;       // nodata band of the DEM (Eps 1e-6), float input
+    Band<double> nd6d;      // the same for float64 input
     double gap, init_level;
-    double* w;              // working levels (rows x cols, dense), +inf marks nodata levels
+    double* w;              // working levels, rows x w_stride doubles, +inf marks nodata levels
+    int64_t w_stride;       // elements per row of w (a multiple of 2: 16-byte rows for TMA)
     int64_t tiles_y, tiles_x;
 };
 struct FillScratch {

@@ -1,0 +1,3 @@
+// basicCell.h -- include name of the reference framework (gpro/basicCell.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// basicTypes.h -- include name of the reference framework (gpro/basicTypes.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

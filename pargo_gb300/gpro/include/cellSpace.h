@@ -1,0 +1,3 @@
+// cellSpace.h -- include name of the reference framework (gpro/cellSpace.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// communication.h -- include name of the reference framework (gpro/communication.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// metaData.h -- include name of the reference framework (gpro/metaData.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// neighborhood.h -- include name of the reference framework (gpro/neighborhood.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// rasterLayer.h -- include name of the reference framework (gpro/rasterLayer.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// rasterOperator.h -- include name of the reference framework (gpro/rasterOperator.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

@@ -1,0 +1,3 @@
+// weightedCell.h -- include name of the reference framework (gpro/weightedCell.h); the GPU
+// build's declarations all live in gpro/gpro.h.
+#include "gpro/gpro.h"

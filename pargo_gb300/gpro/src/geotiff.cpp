@@ -1,0 +1,356 @@
+// geotiff.cpp -- the GeoTIFF reading and writing RasterLayer needs, without GDAL.
+//
+// Reads classic (32-bit offset) TIFF, either byte order, one sample per pixel,
+// uncompressed strips or tiles of 8/16/32/64-bit integer or IEEE float
+// samples; the georeferencing is taken from ModelPixelScale (33550) and
+// ModelTiepoint (33922) as a GDAL geotransform, nodata from GDAL_NODATA
+// (42113); the GeoKey tags (34735-34737) are carried through untouched.
+// Writes little-endian uncompressed float32 or float64 strips with the same
+// tags, as the reference's GTiff output (gpro/rasterLayer.h:957-995) carries them.
+#include <cstdio>
+
+#include "gpro/gpro.h"
+
+namespace GPRO {
+
+namespace {
+
+struct Reader {
+    const std::vector<unsigned char>& b;
+    bool big;
+    uint16_t u16(size_t o) const {
+        return big ? (uint16_t)(b[o] << 8 | b[o + 1]) : (uint16_t)(b[o] | b[o + 1] << 8);
+    }
+    uint32_t u32(size_t o) const {
+        return big ? ((uint32_t)b[o] << 24 | (uint32_t)b[o + 1] << 16 | (uint32_t)b[o + 2] << 8 | b[o + 3])
+                   : ((uint32_t)b[o] | (uint32_t)b[o + 1] << 8 | (uint32_t)b[o + 2] << 16 | (uint32_t)b[o + 3] << 24);
+    }
+    uint64_t u64(size_t o) const {
+        return big ? ((uint64_t)u32(o) << 32 | u32(o + 4)) : ((uint64_t)u32(o + 4) << 32 | u32(o));
+    }
+};
+
+struct Entry {
+    uint16_t tag = 0, type = 0;
+    uint32_t count = 0;
+    size_t off = 0;  // where the values are (inline or out of line)
+};
+
+size_t type_size(uint16_t t) {
+    switch (t) {
+        case 1: case 2: case 6: case 7: return 1;
+        case 3: case 8: return 2;
+        case 4: case 9: case 11: return 4;
+        case 5: case 10: case 12: return 8;
+        default: return 0;
+    }
+}
+
+double sample(const Reader& r, size_t o, int bits, int fmt) {
+    switch (bits) {
+        case 8: return fmt == 2 ? (double)(int8_t)r.b[o] : (double)r.b[o];
+        case 16: return fmt == 2 ? (double)(int16_t)r.u16(o) : (double)r.u16(o);
+        case 32: {
+            const uint32_t v = r.u32(o);
+            if (fmt == 3) {
+                float f;
+                memcpy(&f, &v, 4);
+                return f;
+            }
+            return fmt == 2 ? (double)(int32_t)v : (double)v;
+        }
+        default: {
+            const uint64_t v = r.u64(o);
+            if (fmt == 3) {
+                double d;
+                memcpy(&d, &v, 8);
+                return d;
+            }
+            return fmt == 2 ? (double)(int64_t)v : (double)v;
+        }
+    }
+}
+
+}  // namespace
+
+bool read_geotiff(const char* path, GeoRaster* out, std::string* err) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) {
+        *err = std::string("cannot open ") + path;
+        return false;
+    }
+    std::vector<unsigned char> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    if (b.size() < 8 || !((b[0] == 'I' && b[1] == 'I') || (b[0] == 'M' && b[1] == 'M'))) {
+        *err = std::string(path) + ": not a TIFF file";
+        return false;
+    }
+    Reader r{b, b[0] == 'M'};
+    if (r.u16(2) != 42) {
+        *err = std::string(path) + ": only classic TIFF is supported";
+        return false;
+    }
+    const size_t ifd = r.u32(4);
+    if (ifd + 2 > b.size()) {
+        *err = std::string(path) + ": truncated";
+        return false;
+    }
+    const int n = r.u16(ifd);
+    std::vector<Entry> es;
+    for (int i = 0; i < n; i++) {
+        const size_t e = ifd + 2 + 12 * (size_t)i;
+        if (e + 12 > b.size()) break;
+        Entry x;
+        x.tag = r.u16(e);
+        x.type = r.u16(e + 2);
+        x.count = r.u32(e + 4);
+        const size_t bytes = type_size(x.type) * x.count;
+        x.off = bytes <= 4 ? e + 8 : r.u32(e + 8);
+        if (x.off + bytes > b.size()) continue;
+        es.push_back(x);
+    }
+    auto find = [&](uint16_t tag) -> const Entry* {
+        for (auto& e : es)
+            if (e.tag == tag) return &e;
+        return nullptr;
+    };
+    auto num = [&](const Entry* e, uint32_t k) -> double {
+        switch (e->type) {
+            case 3: return r.u16(e->off + 2 * k);
+            case 4: return r.u32(e->off + 4 * k);
+            case 12: {
+                uint64_t v = r.u64(e->off + 8 * k);
+                double d;
+                memcpy(&d, &v, 8);
+                return d;
+            }
+            case 1: return b[e->off + k];
+            default: return 0.0;
+        }
+    };
+    const Entry* w = find(256);
+    const Entry* h = find(257);
+    if (!w || !h) {
+        *err = std::string(path) + ": missing image size";
+        return false;
+    }
+    GeoRaster g;
+    g.cols = (int)num(w, 0);
+    g.rows = (int)num(h, 0);
+    const Entry* bps = find(258);
+    const int bits = bps ? (int)num(bps, 0) : 1;
+    const Entry* sf = find(339);
+    const int fmt = sf ? (int)num(sf, 0) : 1;
+    const Entry* comp = find(259);
+    const Entry* spp = find(277);
+    if ((comp && num(comp, 0) != 1) || (spp && num(spp, 0) != 1) ||
+        !(bits == 8 || bits == 16 || bits == 32 || bits == 64) || (fmt == 3 && bits < 32)) {
+        *err = std::string(path) + ": only uncompressed single-band 8/16/32/64-bit rasters are supported";
+        return false;
+    }
+    g.dtype = fmt == 3 ? (bits == 32 ? PARGO_F32 : PARGO_F64) : (bits == 8 ? PARGO_I8 : bits == 16 ? PARGO_I16 : PARGO_I32);
+    const size_t bpp = (size_t)bits / 8;
+    g.values.assign((size_t)g.rows * g.cols, 0.0);
+    const Entry* so = find(273);
+    const Entry* to = find(324);
+    if (so) {
+        const Entry* rps = find(278);
+        const Entry* sbc = find(279);
+        const int per = rps ? (int)num(rps, 0) : g.rows;
+        for (uint32_t s = 0; s < so->count; s++) {
+            const size_t base = (size_t)num(so, s);
+            const int r0 = (int)s * per;
+            const int nr = std::min(per, g.rows - r0);
+            const size_t need = (size_t)nr * g.cols * bpp;
+            if (sbc && (size_t)num(sbc, s) < need) {
+                *err = std::string(path) + ": short strip";
+                return false;
+            }
+            if (base + need > b.size()) {
+                *err = std::string(path) + ": truncated strip";
+                return false;
+            }
+            for (int i = 0; i < nr; i++)
+                for (int j = 0; j < g.cols; j++)
+                    g.values[(size_t)(r0 + i) * g.cols + j] = sample(r, base + ((size_t)i * g.cols + j) * bpp, bits, fmt);
+        }
+    } else if (to) {
+        const Entry* tw = find(322);
+        const Entry* tl = find(323);
+        if (!tw || !tl) {
+            *err = std::string(path) + ": tile size missing";
+            return false;
+        }
+        const int TW = (int)num(tw, 0), TL = (int)num(tl, 0);
+        const int across = (g.cols + TW - 1) / TW;
+        for (uint32_t t = 0; t < to->count; t++) {
+            const size_t base = (size_t)num(to, t);
+            const int ty = (int)t / across, tx = (int)t % across;
+            if (base + (size_t)TW * TL * bpp > b.size()) {
+                *err = std::string(path) + ": truncated tile";
+                return false;
+            }
+            for (int i = 0; i < TL; i++)
+                for (int j = 0; j < TW; j++) {
+                    const int rr = ty * TL + i, cc = tx * TW + j;
+                    if (rr < g.rows && cc < g.cols)
+                        g.values[(size_t)rr * g.cols + cc] = sample(r, base + ((size_t)i * TW + j) * bpp, bits, fmt);
+                }
+        }
+    } else {
+        *err = std::string(path) + ": no strips or tiles";
+        return false;
+    }
+    const Entry* scale = find(33550);
+    const Entry* tie = find(33922);
+    if (scale && scale->count >= 2 && tie && tie->count >= 6) {
+        const double sx = num(scale, 0), sy = num(scale, 1);
+        const double ti = num(tie, 0), tj = num(tie, 1), tx = num(tie, 3), ty = num(tie, 4);
+        const double t[6] = {tx - ti * sx, sx, 0.0, ty + tj * sy, 0.0, -sy};
+        memcpy(g.transform, t, sizeof(t));
+    }
+    if (const Entry* e = find(34735)) g.geokeys.assign(b.begin() + e->off, b.begin() + e->off + 2 * e->count);
+    if (const Entry* e = find(34736)) g.geodoubles.assign(b.begin() + e->off, b.begin() + e->off + 8 * e->count);
+    if (const Entry* e = find(34737)) g.geoascii.assign((const char*)&b[e->off], e->count);
+    if (const Entry* e = find(42113)) {
+        std::string s((const char*)&b[e->off], e->count);
+        g.nodata = atof(s.c_str());
+        g.has_nodata = true;
+    }
+    if (r.big) {  // carried tags are written little-endian
+        for (size_t k = 0; k + 1 < g.geokeys.size(); k += 2) std::swap(g.geokeys[k], g.geokeys[k + 1]);
+        for (size_t k = 0; k + 7 < g.geodoubles.size(); k += 8) std::reverse(g.geodoubles.begin() + k, g.geodoubles.begin() + k + 8);
+    }
+    *out = std::move(g);
+    return true;
+}
+
+namespace {
+
+struct Writer {
+    std::vector<unsigned char> ifd, extra;
+    struct E {
+        uint16_t tag, type;
+        uint32_t count;
+        std::vector<unsigned char> data;
+    };
+    std::vector<E> entries;
+    void add(uint16_t tag, uint16_t type, uint32_t count, const void* data, size_t bytes) {
+        E e{tag, type, count, std::vector<unsigned char>((const unsigned char*)data, (const unsigned char*)data + bytes)};
+        entries.push_back(e);
+    }
+    void u16(uint16_t tag, uint16_t v) { add(tag, 3, 1, &v, 2); }
+    void u32(uint16_t tag, uint32_t v) { add(tag, 4, 1, &v, 4); }
+};
+
+void put16(std::vector<unsigned char>& o, uint16_t v) {
+    o.push_back(v & 0xff);
+    o.push_back(v >> 8);
+}
+void put32(std::vector<unsigned char>& o, uint32_t v) {
+    for (int k = 0; k < 4; k++) o.push_back((v >> (8 * k)) & 0xff);
+}
+
+}  // namespace
+
+bool write_geotiff(const char* path, const GeoRaster& m, const double* values, int dtype, std::string* err) {
+    const size_t bpp = dtype == PARGO_F32 ? 4 : 8;
+    const size_t rowbytes = (size_t)m.cols * bpp;
+    const uint64_t total = (uint64_t)rowbytes * m.rows;
+    if (total > 0xF0000000ull) {
+        *err = std::string(path) + ": raster too large for classic TIFF";
+        return false;
+    }
+    const uint32_t per = (uint32_t)std::max<size_t>(1, std::min<size_t>(m.rows, 65536 / std::max<size_t>(rowbytes, 1)));
+    const uint32_t nstrips = (uint32_t)((m.rows + per - 1) / per);
+    Writer w;
+    w.u32(256, (uint32_t)m.cols);
+    w.u32(257, (uint32_t)m.rows);
+    w.u16(258, (uint16_t)(bpp * 8));
+    w.u16(259, 1);
+    w.u16(262, 1);
+    std::vector<uint32_t> offs(nstrips), counts(nstrips);
+    w.add(273, 4, nstrips, offs.data(), 4 * (size_t)nstrips);  // patched below
+    w.u16(277, 1);
+    w.u32(278, per);
+    for (uint32_t s = 0; s < nstrips; s++) counts[s] = (uint32_t)(std::min<uint64_t>(per, m.rows - (uint64_t)s * per) * rowbytes);
+    w.add(279, 4, nstrips, counts.data(), 4 * (size_t)nstrips);
+    w.u16(284, 1);
+    w.u16(339, 3);
+    const double scale[3] = {m.transform[1], -m.transform[5], 0.0};
+    const double tie[6] = {0.0, 0.0, 0.0, m.transform[0], m.transform[3], 0.0};
+    w.add(33550, 12, 3, scale, sizeof(scale));
+    w.add(33922, 12, 6, tie, sizeof(tie));
+    if (!m.geokeys.empty()) w.add(34735, 3, (uint32_t)(m.geokeys.size() / 2), m.geokeys.data(), m.geokeys.size());
+    if (!m.geodoubles.empty())
+        w.add(34736, 12, (uint32_t)(m.geodoubles.size() / 8), m.geodoubles.data(), m.geodoubles.size());
+    if (!m.geoascii.empty()) w.add(34737, 2, (uint32_t)m.geoascii.size(), m.geoascii.data(), m.geoascii.size());
+    char nd[64];
+    snprintf(nd, sizeof(nd), "%.17g", m.nodata);
+    std::string nds(nd);
+    nds.push_back('\0');
+    w.add(42113, 2, (uint32_t)nds.size(), nds.data(), nds.size());
+    // layout: header, IFD, out-of-line values, strips
+    const size_t n = w.entries.size();
+    const size_t ifd_off = 8, ifd_size = 2 + 12 * n + 4;
+    size_t cursor = ifd_off + ifd_size;
+    std::vector<size_t> value_off(n, 0);
+    for (size_t i = 0; i < n; i++) {
+        if (w.entries[i].data.size() > 4) {
+            value_off[i] = cursor;
+            cursor += (w.entries[i].data.size() + 1) & ~(size_t)1;
+        }
+    }
+    const size_t data_off = (cursor + 15) & ~(size_t)15;
+    for (uint32_t s = 0; s < nstrips; s++) offs[s] = (uint32_t)(data_off + (size_t)s * per * rowbytes);
+    memcpy(w.entries[5].data.data(), offs.data(), 4 * (size_t)nstrips);  // tag 273
+    std::vector<unsigned char> out;
+    out.reserve(data_off + total);
+    out.push_back('I');
+    out.push_back('I');
+    put16(out, 42);
+    put32(out, (uint32_t)ifd_off);
+    put16(out, (uint16_t)n);
+    for (size_t i = 0; i < n; i++) {
+        const auto& e = w.entries[i];
+        put16(out, e.tag);
+        put16(out, e.type);
+        put32(out, e.count);
+        if (e.data.size() > 4) {
+            put32(out, (uint32_t)value_off[i]);
+        } else {
+            unsigned char v[4] = {0, 0, 0, 0};
+            memcpy(v, e.data.data(), e.data.size());
+            out.insert(out.end(), v, v + 4);
+        }
+    }
+    put32(out, 0);
+    for (size_t i = 0; i < n; i++) {
+        const auto& e = w.entries[i];
+        if (e.data.size() > 4) {
+            out.insert(out.end(), e.data.begin(), e.data.end());
+            if (e.data.size() & 1) out.push_back(0);
+        }
+    }
+    out.resize(data_off, 0);
+    for (size_t i = 0; i < (size_t)m.rows * m.cols; i++) {
+        if (bpp == 4) {
+            const float v = (float)values[i];
+            unsigned char c[4];
+            memcpy(c, &v, 4);
+            out.insert(out.end(), c, c + 4);
+        } else {
+            unsigned char c[8];
+            memcpy(c, &values[i], 8);
+            out.insert(out.end(), c, c + 8);
+        }
+    }
+    std::ofstream f(path, std::ios::binary);
+    if (!f) {
+        *err = std::string("cannot create ") + path;
+        return false;
+    }
+    f.write((const char*)out.data(), (std::streamsize)out.size());
+    return (bool)f;
+}
+
+}  // namespace GPRO
