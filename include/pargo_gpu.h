@@ -115,6 +115,7 @@ typedef struct pargo_fill_stats {
     int64_t rounds;        /* worklist rounds launched */
     int64_t active_rounds; /* rounds whose worklist was not empty */
     int64_t tile_visits;   /* tiles relaxed, summed over rounds */
+    int64_t local_iterations; /* relaxation iterations inside tiles, summed over visits */
     int64_t raised_cells;  /* cells whose filled level is above the DEM */
     double rounds_ms;      /* device time of all rounds (CUDA events on the round stream) */
 } pargo_fill_stats;

@@ -52,7 +52,7 @@ class FillOpts(ctypes.Structure):
 
 class FillStats(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_int64), ("active_rounds", ctypes.c_int64), ("tile_visits", ctypes.c_int64),
-                ("raised_cells", ctypes.c_int64), ("rounds_ms", ctypes.c_double)]
+                ("local_iterations", ctypes.c_int64), ("raised_cells", ctypes.c_int64), ("rounds_ms", ctypes.c_double)]
 
 
 _lib = None

@@ -675,6 +675,7 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     sc.visits = &ctx->d_counters[1];
     sc.changed = &ctx->d_counters[2];
     sc.active = &ctx->d_counters[4];
+    sc.iters = &ctx->d_counters[5];
     CU(ctx, cudaMemsetAsync(ctx->d_counters, 0, 8 * sizeof(unsigned long long), s));
     {
         cudaError_t ee = fill_init(p, sc, s);
@@ -738,6 +739,7 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
         stats->rounds = rounds;
         stats->active_rounds = (int64_t)hp[4];
         stats->tile_visits = (int64_t)hp[1];
+        stats->local_iterations = (int64_t)hp[5];
         stats->raised_cells = 0;
         stats->rounds_ms = ms;
     }

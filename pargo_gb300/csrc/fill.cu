@@ -30,6 +30,9 @@
 
 #include <math.h>
 
+#include <map>
+#include <mutex>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -43,7 +46,11 @@ constexpr int kThreads = 256;     // 4 cells per thread
 constexpr int kLocalCap = 4096;   // relaxation sweeps per visit before the tile re-queues itself
 constexpr int64_t kKeyInf = 0x7FF0000000000000LL;  // key of +inf
 
-__device__ int64_t g_step[2048];  // per biased exponent: (x + gap) - x in ulps of x's binade
+// Per biased exponent e: fl64(x + gap) - x in ulps of x's binade when that
+// is the same for every x of the binade, else -1 (subnormals, inf/nan, a sum
+// that can leave the binade, and the binade in which gap is an odd number of
+// half-ulps, where the tie rounds by the parity of x): those use the double add.
+__device__ int64_t g_step[2048];
 
 __device__ __forceinline__ int64_t dkey(double x) {
     int64_t b = __double_as_longlong(x);
@@ -55,8 +62,11 @@ __device__ __forceinline__ double dval(int64_t k) { return __longlong_as_double(
 __device__ __forceinline__ int64_t add_gap(int64_t k, double gap) {
     if (k >= 0 && k < kKeyInf) {
         const int e = (int)(k >> 52);
-        const int64_t y = k + g_step[e];
-        if ((int)(y >> 52) == e) return y;
+        const int64_t st = g_step[e];
+        if (st >= 0) {
+            const int64_t y = k + st;
+            if ((int)(y >> 52) == e) return y;
+        }
     }
     return dkey(__dadd_rn(dval(k), gap));
 }
@@ -237,6 +247,7 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
                 atomicAdd(s.changed, 1ULL);
             }
             atomicAdd(s.visits, 1ULL);
+            atomicAdd(s.iters, (unsigned long long)it);
         }
         __syncthreads();
     }
@@ -278,26 +289,40 @@ int fill_tile_cols() { return kT; }
 // x = 2^(e-1023), (x + gap) - x is exact (both in the binade) and, divided by
 // the binade's ulp, is the integer step that fl64(y + gap) adds to any y of the
 // binade whose sum stays in it.
-static cudaError_t upload_steps(double gap) {
-    static double uploaded = -1.0;
-    if (uploaded == gap) return cudaSuccess;
+static cudaError_t upload_steps(double gap, cudaStream_t st) {
+    // The table lives in each device's memory: remember the gap per device.
+    static std::mutex mu;
+    static std::map<int, double> uploaded;
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) return err;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = uploaded.find(dev);
+    if (it != uploaded.end() && it->second == gap) return cudaSuccess;
     int64_t tab[2048];
     for (int e = 0; e < 2048; e++) {
-        tab[e] = 0;
-        if (e == 0 || e >= 2047) continue;       // subnormals / inf use the double add
+        tab[e] = -1;
+        if (e == 0 || e >= 2047 || !(gap >= 0.0)) continue;
         const double x = ldexp(1.0, e - 1023);
-        const volatile double sum = x + gap;     // one IEEE double add
-        if (!(sum < 2.0 * x)) continue;          // the step leaves the binade: double add
         const double ulp = ldexp(1.0, e - 1023 - 52);
-        tab[e] = (int64_t)((sum - x) / ulp);
+        const volatile double s0 = x + gap;  // one IEEE double add, even x
+        const volatile double x1 = x + ulp;
+        const volatile double s1 = x1 + gap;  // odd x
+        const int64_t d0 = (int64_t)((s0 - x) / ulp);
+        const int64_t d1 = (int64_t)((s1 - x1) / ulp);
+        // Same step for even and odd x: no tie in this binade.  A sum that
+        // leaves the binade is caught on the device by the result's exponent.
+        if (!(s0 < 2.0 * x) || d0 != d1) continue;
+        tab[e] = d0;
     }
-    cudaError_t err = cudaMemcpyToSymbol(g_step, tab, sizeof(tab));
-    if (err == cudaSuccess) uploaded = gap;
+    // Pageable source: staged at once, copied in stream order.
+    err = cudaMemcpyToSymbolAsync(g_step, tab, sizeof(tab), 0, cudaMemcpyHostToDevice, st);
+    if (err == cudaSuccess) uploaded[dev] = gap;
     return err;
 }
 
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st) {
-    cudaError_t e = upload_steps(p.gap);
+    cudaError_t e = upload_steps(p.gap, st);
     if (e != cudaSuccess) return e;
     const int64_t n = p.rows * p.cols;
     int64_t blocks = (n + 255) / 256;

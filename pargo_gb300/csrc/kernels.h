@@ -88,6 +88,7 @@ struct FillScratch {
     unsigned long long* visits;
     unsigned long long* changed;
     unsigned long long* active;  // rounds that found a non-empty worklist
+    unsigned long long* iters;   // local relaxation iterations, summed over tile visits
 };
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st);
 cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st);

@@ -41,3 +41,17 @@ def bits_equal(a, b):
     a = np.ascontiguousarray(a, np.float64)
     b = np.ascontiguousarray(b, np.float64)
     return a.shape == b.shape and np.array_equal(a.view(np.int64), b.view(np.int64))
+
+
+def near_zero_dem(rows, cols, seed):
+    """Sea-level flats (0.0), tiny heights around the gap (0 .. 5e-3, which
+    spans the binades where x + gap leaves x's binade or rounds on a tie) and
+    a few negative cells, with pits in all of them."""
+    rng = np.random.default_rng(seed)
+    dem = rng.uniform(0.0, 5e-3, (rows, cols)).astype(np.float32)
+    dem[:, : cols // 3] = 0.0
+    dem[rows // 2:, cols // 3: cols // 2] = -rng.uniform(0.0, 2e-3, (rows - rows // 2, cols // 2 - cols // 3))
+    pits = rng.random((rows, cols)) < 0.05
+    dem[pits] = np.float32(0.0)
+    dem[5:9, 5:9] = np.float32(2.0 ** -9)
+    return dem

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from conftest import GOLDEN_CASES, bits_equal, load_golden
+from conftest import GOLDEN_CASES, bits_equal, load_golden, near_zero_dem
 from gpu_helpers import d8_as_f64, dev, empty_dev, host
 from pargo_gb300 import abi, synth
 
@@ -87,6 +87,21 @@ def test_fill_edge_cases(ctx, oracle_lib):
     w = empty_dev(bowl.shape, np.float64)
     ctx.fill(abi.raster(dev(bowl), -9999.0), abi.raster(w, -9999.0))
     assert bits_equal(host(w), oracle_lib.fill(bowl, -9999.0))
+
+
+@pytest.mark.parametrize("gap", [1e-3, 2.0 ** -10, 3 * 2.0 ** -12, 5e-4])
+def test_fill_levels_near_zero(gap, ctx, oracle_lib):
+    dem = near_zero_dem(96, 130, seed=7)
+    ref = oracle_lib.fill(dem, -9999.0, gap=gap)
+    gs, _ = oracle_lib.fill_gs(dem, -9999.0, gap=gap)
+    assert bits_equal(ref, gs)
+    assert (ref > dem).any()
+    w = empty_dev(dem.shape, np.float64)
+    ctx.fill(abi.raster(dev(dem), -9999.0), abi.raster(w, -9999.0), gap=gap)
+    assert bits_equal(host(w), ref)
+    w64 = empty_dev(dem.shape, np.float64)   # float64 DEM: the same values, the same levels
+    ctx.fill(abi.raster(dev(dem.astype(np.float64)), -9999.0), abi.raster(w64, -9999.0), gap=gap)
+    assert bits_equal(host(w64), ref)
 
 
 def test_sca_cycle_is_reported(ctx):

@@ -95,3 +95,25 @@ def test_planted_mistake_is_caught(oracle_lib):
     h = load_golden("fbm_hydro")
     w = oracle_lib.fill(h["dem"], -9999.0, gap=0.0005 * (1 + 1e-9))
     assert not bits_equal(w, h["fill"])
+
+
+@pytest.mark.parametrize("gap", [1e-3, 2.0 ** -10, 3 * 2.0 ** -12])
+def test_oracle_fill_near_zero_levels(gap, oracle_lib):
+    """Levels at and just above 0, where x + gap leaves x's binade or ties:
+    the priority flood and the raster-order sweeps agree bit for bit."""
+    from conftest import near_zero_dem
+    dem = near_zero_dem(61, 77, seed=3)
+    w_pf = oracle_lib.fill(dem, -9999.0, gap=gap)
+    w_gs, _ = oracle_lib.fill_gs(dem, -9999.0, gap=gap)
+    assert bits_equal(w_pf, w_gs)
+    assert (w_pf > dem).sum() > 100
+
+
+def test_oracle_fill_near_zero_matches_reference_binary(oracle_lib):
+    from conftest import near_zero_dem
+    R = _ref()
+    dem = near_zero_dem(61, 77, seed=3)
+    w_ref, sw_ref = R.fill(dem, -9999.0, 1.0)
+    w_gs, sw = oracle_lib.fill_gs(dem, -9999.0)
+    assert bits_equal(w_gs, w_ref) and sw == sw_ref
+    assert bits_equal(oracle_lib.fill(dem, -9999.0), w_ref)
