@@ -223,22 +223,24 @@ def run_hydro(args, ws, rank, local):
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, ws, torch.device("cuda", local))
     e2e_value = ws * cells / e2e_s / 1e6
 
-    # roofline of the dominant kernel: the fill round kernel.  Algorithmic
-    # bytes: 8 B per cell a round visits (4 B DEM read + 4 B level written, the
-    # minimum of any pass), 1024 cells per tile visit; duration: the rounds'
-    # device time (CUDA events on the round stream) / rounds launched.
+    # roofline of the dominant kernel: the fill relaxation (one persistent
+    # launch per step; PARGO_FILL_ROUNDS=1 selects the round launches).
+    # Algorithmic bytes: 8 B per cell a visit covers (4 B DEM read + 4 B level
+    # written, the minimum of any pass), 1024 cells per tile visit; duration:
+    # the relaxation's device time (CUDA events on its stream) / launches.
     peak, peak_kind = hbm_peak()
     avg_round_ms = rounds_ms / max(rounds, 1)
     bytes_per_round = 8.0 * 1024 * visits / max(rounds, 1)
     achieved = bytes_per_round / (avg_round_ms * 1e-3) / 1e9 if avg_round_ms > 0 else 0.0
     fill_share = rounds_ms / (ms * args.steps) if ms > 0 else None
-    roofline = {"bound": "hbm", "kernel": "fill_round_kernel", "achieved": round(achieved, 2), "peak": peak,
+    roofline = {"bound": "hbm", "kernel": "fill_tiles_kernel<true> (persistent)" if rounds == args.steps
+                else "fill_tiles_kernel<false> (rounds)", "achieved": round(achieved, 2), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": peak_kind,
                 "traffic": None, "rounds_per_step": rounds // args.steps,
                 "tile_visits_per_step": visits // args.steps,
                 "local_iterations_per_visit": round(iters / max(visits, 1), 2), "fill_share_of_step": round(fill_share, 4)
                 if fill_share else None}
-    launches = args.steps * (3 + rounds // args.steps)
+    launches = args.steps * 2 + rounds  # fill init + relaxation launches + float64 slope/D8, per step
 
     cpu = None
     if rank == 0 and ws == 1:

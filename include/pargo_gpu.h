@@ -108,16 +108,17 @@ typedef enum pargo_sca_contract {
 typedef struct pargo_fill_opts {
     double gap;         /* reference: 0.0005 (pitRemoveOperator.cpp:36) */
     double init_level;  /* reference: 10000.0 (pitRemoveOperator.cpp:41) */
-    int64_t max_rounds; /* cap on relaxation rounds; <= 0 = no cap */
+    int64_t max_rounds; /* <= 0: no cap, one persistent launch over a device work queue;
+                           > 0: worklist rounds (CUDA graphs of round launches), at most this many */
 } pargo_fill_opts;
 
 typedef struct pargo_fill_stats {
-    int64_t rounds;        /* worklist rounds launched */
-    int64_t active_rounds; /* rounds whose worklist was not empty */
+    int64_t rounds;        /* worklist rounds launched (1 for the persistent launch) */
+    int64_t active_rounds; /* rounds whose worklist was not empty (1 for the persistent launch) */
     int64_t tile_visits;   /* tiles relaxed, summed over rounds */
     int64_t local_iterations; /* relaxation iterations inside tiles, summed over visits */
     int64_t raised_cells;  /* cells whose filled level is above the DEM */
-    double rounds_ms;      /* device time of all rounds (CUDA events on the round stream) */
+    double rounds_ms;      /* device time of the relaxation (CUDA events on the library's stream) */
 } pargo_fill_stats;
 
 typedef struct pargo_ctx pargo_ctx;
@@ -160,7 +161,11 @@ pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps,
 /* Planchon-Darboux pit removal: the fixpoint the reference's Gauss-Seidel
  * sweeps reach (any visiting order reaches the same one).  dem: F32 or F64;
  * wdem: F64 (the reference's values) or F32 (those values rounded to float).
- * opts may be NULL (reference constants); stats may be NULL. */
+ * opts may be NULL (reference constants); stats may be NULL.  Without a round
+ * cap the relaxation is one persistent launch whose tiles queue their
+ * neighbours on the device; PARGO_FILL_ROUNDS=1 in the environment selects the
+ * round form instead.  PARGO_ERR_DEVICE_TIMEOUT: a device-side wait found no
+ * progress for about two seconds. */
 pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
                         const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream);
 

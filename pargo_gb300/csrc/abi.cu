@@ -663,7 +663,8 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     p.w_stride = (cols + 1) / 2 * 2;  // 16-byte rows: the levels can be TMA-loaded
     p.w = (double*)slot(ctx, kSlotFillW, (size_t)(rows * p.w_stride) * sizeof(double), &e);
     if (!p.w) return cuda_fail(ctx, e, "fill levels");
-    int32_t* lists = (int32_t*)slot(ctx, kSlotFillLists, (size_t)(2 * ntiles + 8) * sizeof(int32_t), &e);
+    // two worklists (or one ring) of ntiles ids, 8 round counters, 8 queue words (u64)
+    int32_t* lists = (int32_t*)slot(ctx, kSlotFillLists, (size_t)(2 * ntiles + 8) * sizeof(int32_t) + 8 * 8 + 8, &e);
     if (!lists) return cuda_fail(ctx, e, "fill worklists");
     int32_t* queued = (int32_t*)slot(ctx, kSlotFillQueued, (size_t)ntiles * sizeof(int32_t), &e);
     if (!queued) return cuda_fail(ctx, e, "fill queue flags");
@@ -676,10 +677,49 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     sc.changed = &ctx->d_counters[2];
     sc.active = &ctx->d_counters[4];
     sc.iters = &ctx->d_counters[5];
+    sc.ring = lists;
+    sc.ring_cap = 2 * ntiles;
+    sc.q = (unsigned long long*)(((uintptr_t)(lists + 2 * ntiles + 8) + 7) & ~(uintptr_t)7);
+    const char* force_rounds = getenv("PARGO_FILL_ROUNDS");
+    const bool persistent = o.max_rounds <= 0 && !(force_rounds && force_rounds[0] == '1');
     CU(ctx, cudaMemsetAsync(ctx->d_counters, 0, 8 * sizeof(unsigned long long), s));
     {
         cudaError_t ee = fill_init(p, sc, s);
         if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill init");
+    }
+    if (persistent) {
+        // One launch: tiles pop from and push to a device ring until the
+        // pending count reaches zero.  Waits give up after ~2 s without progress.
+        const long long patience = 4000000000LL;  // SM cycles
+        unsigned long long* hp = (unsigned long long*)pinned(ctx, 128, &e);
+        if (!hp) return cuda_fail(ctx, e, "pinned counters");
+        CU(ctx, cudaEventRecord(ctx->ev_t0, s));
+        {
+            cudaError_t ee = fill_persistent(p, sc, patience, ctx->num_sms, s);
+            if (ee != cudaSuccess) return cuda_fail(ctx, ee, "fill persistent launch");
+        }
+        CU(ctx, cudaEventRecord(ctx->ev_t1, s));
+        CU(ctx, cudaMemcpyAsync(hp, sc.q, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CU(ctx, cudaMemcpyAsync(hp + 8, ctx->d_counters, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CU(ctx, cudaStreamSynchronize(s));
+        if (hp[4] != 0)
+            return fail(ctx, PARGO_ERR_DEVICE_TIMEOUT,
+                        hp[4] == 1   ? "fill: a device wait for queued tiles made no progress"
+                        : hp[4] == 2 ? "fill: a device wait for a free queue slot made no progress"
+                                     : "fill: a tile state did not settle");
+        *converged = hp[2] == 0;
+        float ms = 0.0f;
+        CU(ctx, cudaEventElapsedTime(&ms, ctx->ev_t0, ctx->ev_t1));
+        if (stats) {
+            stats->rounds = 1;
+            stats->active_rounds = 1;
+            stats->tile_visits = (int64_t)hp[8 + 1];
+            stats->local_iterations = (int64_t)hp[8 + 5];
+            stats->raised_cells = 0;
+            stats->rounds_ms = ms;
+        }
+        *out_p = p;
+        return PARGO_OK;
     }
     // Rounds run on the context's own stream, as CUDA-graph launches of
     // kRoundsPerGraph rounds (an even number, so list A is current again); a

@@ -45,6 +45,9 @@ constexpr int kH = kT + 2;        // with halo
 constexpr int kThreads = 256;     // 4 cells per thread
 constexpr int kLocalCap = 4096;   // relaxation sweeps per visit before the tile re-queues itself
 constexpr int64_t kKeyInf = 0x7FF0000000000000LL;  // key of +inf
+// FillScratch::q slots of the persistent form
+constexpr int kQHead = 0, kQTail = 1, kQPending = 2, kQProgress = 3, kQError = 4;
+constexpr int kQErrPop = 1, kQErrPush = 2, kQErrState = 3;
 
 // Per biased exponent e: fl64(x + gap) - x in ulps of x's binade when that
 // is the same for every x of the binade, else -1 (subnormals, inf/nan, a sum
@@ -106,7 +109,8 @@ __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
     }
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles; t += (int64_t)gridDim.x * blockDim.x) {
-        s.list_a[t] = (int32_t)t;
+        s.list_a[t] = (int32_t)t;  // also ring positions 0 .. ntiles-1
+        s.list_b[t] = -1;          // the ring's empty second half
         s.queued[t] = 1;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -114,6 +118,11 @@ __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
         s.counts[1] = 0;
         s.counts[2] = 0;
         s.counts[3] = 0;
+        s.q[kQHead] = 0;
+        s.q[kQTail] = (unsigned long long)ntiles;
+        s.q[kQPending] = (unsigned long long)ntiles;
+        s.q[kQProgress] = 0;
+        s.q[kQError] = 0;
     }
 }
 
@@ -124,7 +133,120 @@ __device__ __forceinline__ void enqueue(const FillScratch& s, int32_t* next, int
     if (atomicExch(&s.queued[t], 1) == 0) next[atomicAdd(next_count, 1)] = t;
 }
 
-__global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p, FillScratch s, int parity) {
+// ---- persistent form: one launch, a ring of tile ids ----------------------
+// The ring has 2 * ntiles slots (-1 = empty).  A tile is in the ring at most
+// once (its queued flag is set from its push until a visitor takes it), so
+// fewer than ntiles slots are ever full and a pusher finds its slot empty or
+// about to be emptied by the visitor that claimed that position.  q[kQPending]
+// counts tiles pushed and not yet finished: it is raised before a push and
+// lowered only after a visit has pushed its neighbours, so it reaches 0 only
+// when the ring is empty and no visit is in flight -- the device-side
+// convergence flag.  Every wait gives up after `patience` cycles without a
+// finished visit anywhere (or without its slot emptying), sets q[kQError] and
+// returns; the host reports that as a device timeout.
+
+__device__ __forceinline__ unsigned long long vload64(const unsigned long long* a) {
+    return *((const volatile unsigned long long*)a);
+}
+
+__device__ void ring_push(const FillScratch& s, int32_t t, long long patience) {
+    atomicAdd(&s.q[kQPending], 1ULL);
+    const unsigned long long pos = atomicAdd(&s.q[kQTail], 1ULL);
+    int32_t* slot = &s.ring[pos % (unsigned long long)s.ring_cap];
+    const long long t0 = clock64();
+    unsigned ns = 32;
+    while (atomicCAS(slot, -1, t) != -1) {
+        if (vload64(&s.q[kQError]) != 0) return;
+        if (clock64() - t0 > patience) {
+            atomicCAS(&s.q[kQError], 0ULL, (unsigned long long)kQErrPush);
+            return;
+        }
+        __nanosleep(ns);
+        if (ns < 1024) ns *= 2;
+    }
+}
+
+// Next tile to visit, or -1 once the work is done (or a wait gave up).
+__device__ int32_t ring_pop(const FillScratch& s, long long patience) {
+    const unsigned long long pos = atomicAdd(&s.q[kQHead], 1ULL);
+    int32_t* slot = &s.ring[pos % (unsigned long long)s.ring_cap];
+    unsigned long long seen = vload64(&s.q[kQProgress]);
+    long long t0 = clock64();
+    unsigned ns = 32;
+    for (;;) {
+        const int32_t v = *((volatile int32_t*)slot);
+        if (v >= 0) {
+            if (atomicCAS(slot, v, -1) == v) return v;
+            continue;  // another visitor that shares this slot took it
+        }
+        if (vload64(&s.q[kQPending]) == 0 || vload64(&s.q[kQError]) != 0) return -1;
+        const unsigned long long pr = vload64(&s.q[kQProgress]);
+        if (pr != seen) {
+            seen = pr;
+            t0 = clock64();
+        } else if (clock64() - t0 > patience) {
+            atomicCAS(&s.q[kQError], 0ULL, (unsigned long long)kQErrPop);
+            return -1;
+        }
+        __nanosleep(ns);
+        if (ns < 2048) ns *= 2;
+    }
+}
+
+// Tile states of the persistent form (in FillScratch::queued).  A tile has at
+// most one visitor: a request for a running tile only marks it dirty, and the
+// visitor queues it again when it finishes, so a visit that read a halo
+// before a neighbour's write is always followed by one that reads after it.
+constexpr int32_t kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3;
+
+__device__ void request_tile(const FillScratch& s, int32_t t, long long patience) {
+    int32_t st = *((volatile int32_t*)&s.queued[t]);
+    for (int guard = 0; guard < 64; guard++) {  // each failed CAS means another thread moved the state
+        int32_t want;
+        if (st == kIdle) want = kQueued;
+        else if (st == kRunning) want = kRunningDirty;
+        else return;  // already queued, or will be queued by its visitor
+        const int32_t old = atomicCAS(&s.queued[t], st, want);
+        if (old == st) {
+            if (want == kQueued) ring_push(s, t, patience);
+            return;
+        }
+        st = old;
+    }
+    atomicCAS(&s.q[kQError], 0ULL, (unsigned long long)kQErrState);
+}
+
+// End of a visit: back to idle, or queued again if it was requested meanwhile
+// (or if it stopped at the local iteration cap).
+__device__ void finish_tile(const FillScratch& s, int32_t t, bool again, long long patience) {
+    const int32_t old = atomicCAS(&s.queued[t], kRunning, again ? kQueued : kIdle);
+    if (old == kRunning) {
+        if (again) ring_push(s, t, patience);
+    } else {  // kRunningDirty: only this visitor moves it out of that state
+        atomicExch(&s.queued[t], kQueued);
+        ring_push(s, t, patience);
+    }
+}
+
+template <bool PERSIST>
+__device__ __forceinline__ void put_tile(const FillScratch& s, int32_t* next, int32_t* next_count, int64_t ty, int64_t tx,
+                                         const FillParams& p, long long patience) {
+    if (!PERSIST) {
+        enqueue(s, next, next_count, ty, tx, p);
+        return;
+    }
+    if (ty < 0 || tx < 0 || ty >= p.tiles_y || tx >= p.tiles_x) return;
+    request_tile(s, (int32_t)(ty * p.tiles_x + tx), patience);
+}
+
+// One CTA visits one 32 x 32 tile at a time: claim, load levels + halo into
+// shared memory, relax to stability against the halo, write back what changed
+// and queue the neighbours whose halo moved.  PERSIST = false: one round of
+// the current worklist (a launch per round).  PERSIST = true: the whole fill
+// in one launch over the ring.
+template <bool PERSIST>
+__global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p, FillScratch s, int parity,
+                                                              long long patience) {
     __shared__ int64_t lv[kH][kH];
     __shared__ int32_t claim;
     __shared__ int edges;  // bit 0 top, 1 bottom, 2 left, 3 right, 4 tl, 5 tr, 6 bl, 7 br
@@ -133,19 +255,23 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
     int32_t* next = parity ? s.list_a : s.list_b;
     int32_t* cur_count = &s.counts[parity];
     int32_t* next_count = &s.counts[parity ^ 1];
-    const int32_t ncur = *((volatile int32_t*)cur_count);
+    const int32_t ncur = PERSIST ? 0 : *((volatile int32_t*)cur_count);
     const int tid = threadIdx.x;
-    if (blockIdx.x == 0 && tid == 0 && ncur > 0) atomicAdd(s.active, 1ULL);
+    if (!PERSIST && blockIdx.x == 0 && tid == 0 && ncur > 0) atomicAdd(s.active, 1ULL);
     const int lr = tid >> 3;            // local row 0..31
     const int lc0 = (tid & 7) * 4;      // local cols lc0..lc0+3
 
     for (;;) {
         if (tid == 0) {
-            int32_t k = atomicAdd(&s.counts[2], 1);
-            claim = k < ncur ? cur[k] : -1;
+            if (PERSIST) {
+                claim = ring_pop(s, patience);
+            } else {
+                const int32_t k = atomicAdd(&s.counts[2], 1);
+                claim = k < ncur ? cur[k] : -1;
+            }
             edges = 0;
             if (claim >= 0) {
-                atomicExch(&s.queued[claim], 0);
+                atomicExch(&s.queued[claim], PERSIST ? kRunning : 0);
                 __threadfence();
             }
         }
@@ -232,25 +358,32 @@ __global__ void __launch_bounds__(kThreads) fill_round_kernel(const FillParams p
         if (e) atomicOr(&edges, e);
         __syncthreads();
         if (tid == 0) {
-            if (it >= kLocalCap) enqueue(s, next, next_count, ty, tx, p);
+            if (any || it >= kLocalCap) __threadfence();  // the writes above before any queueing
+            if (!PERSIST && it >= kLocalCap) put_tile<PERSIST>(s, next, next_count, ty, tx, p, patience);
             if (any) {
-                __threadfence();
                 const int ed = edges;
-                if (ed & 1) enqueue(s, next, next_count, ty - 1, tx, p);
-                if (ed & 2) enqueue(s, next, next_count, ty + 1, tx, p);
-                if (ed & 4) enqueue(s, next, next_count, ty, tx - 1, p);
-                if (ed & 8) enqueue(s, next, next_count, ty, tx + 1, p);
-                if (ed & 16) enqueue(s, next, next_count, ty - 1, tx - 1, p);
-                if (ed & 32) enqueue(s, next, next_count, ty - 1, tx + 1, p);
-                if (ed & 64) enqueue(s, next, next_count, ty + 1, tx - 1, p);
-                if (ed & 128) enqueue(s, next, next_count, ty + 1, tx + 1, p);
+                if (ed & 1) put_tile<PERSIST>(s, next, next_count, ty - 1, tx, p, patience);
+                if (ed & 2) put_tile<PERSIST>(s, next, next_count, ty + 1, tx, p, patience);
+                if (ed & 4) put_tile<PERSIST>(s, next, next_count, ty, tx - 1, p, patience);
+                if (ed & 8) put_tile<PERSIST>(s, next, next_count, ty, tx + 1, p, patience);
+                if (ed & 16) put_tile<PERSIST>(s, next, next_count, ty - 1, tx - 1, p, patience);
+                if (ed & 32) put_tile<PERSIST>(s, next, next_count, ty - 1, tx + 1, p, patience);
+                if (ed & 64) put_tile<PERSIST>(s, next, next_count, ty + 1, tx - 1, p, patience);
+                if (ed & 128) put_tile<PERSIST>(s, next, next_count, ty + 1, tx + 1, p, patience);
                 atomicAdd(s.changed, 1ULL);
             }
             atomicAdd(s.visits, 1ULL);
             atomicAdd(s.iters, (unsigned long long)it);
+            if (PERSIST) {
+                finish_tile(s, t, it >= kLocalCap, patience);
+                __threadfence();
+                atomicAdd(&s.q[kQProgress], 1ULL);
+                atomicAdd(&s.q[kQPending], ~0ULL);  // minus one, after the pushes above
+            }
         }
         __syncthreads();
     }
+    if (PERSIST) return;
     // The last CTA to finish resets the consumed list and the claim cursor.
     if (tid == 0) {
         __threadfence();
@@ -333,13 +466,25 @@ cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st
 
 cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_round_kernel, kThreads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_tiles_kernel<false>, kThreads, 0);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     int64_t grid = (int64_t)num_sms * per_sm;
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     if (grid > ntiles) grid = ntiles;
-    fill_round_kernel<<<(unsigned)grid, kThreads, 0, st>>>(p, s, parity);
+    fill_tiles_kernel<false><<<(unsigned)grid, kThreads, 0, st>>>(p, s, parity, 0);
+    return cudaGetLastError();
+}
+
+cudaError_t fill_persistent(const FillParams& p, const FillScratch& s, long long patience, int num_sms, cudaStream_t st) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_tiles_kernel<true>, kThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int64_t grid = (int64_t)num_sms * per_sm;  // every CTA resident
+    const int64_t ntiles = p.tiles_y * p.tiles_x;
+    if (grid > ntiles) grid = ntiles;
+    fill_tiles_kernel<true><<<(unsigned)grid, kThreads, 0, st>>>(p, s, 0, patience);
     return cudaGetLastError();
 }
 

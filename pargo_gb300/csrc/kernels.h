@@ -89,9 +89,15 @@ struct FillScratch {
     unsigned long long* changed;
     unsigned long long* active;  // rounds that found a non-empty worklist
     unsigned long long* iters;   // local relaxation iterations, summed over tile visits
+    // persistent form: list_a and list_b, contiguous, are one ring of ring_cap
+    // = 2 * tiles slots; q = [head, tail, pending, progress, error]
+    int32_t* ring;
+    int64_t ring_cap;
+    unsigned long long* q;
 };
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st);
 cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st);
+cudaError_t fill_persistent(const FillParams& p, const FillScratch& s, long long patience, int num_sms, cudaStream_t st);
 cudaError_t fill_finish(const FillParams& p, const OutView& out, unsigned long long* raised, cudaStream_t st);
 int fill_tile_rows();
 int fill_tile_cols();

@@ -70,8 +70,24 @@ def test_fill_options_and_round_cap(ctx, oracle_lib):
     assert e.value.status_name == "PARGO_ERR_NOT_CONVERGED"
     # the context stays usable, and an uncapped run converges to the oracle's bytes
     st = ctx.fill(abi.raster(dev(big), -9999.0), abi.raster(wb, -9999.0))
-    assert st.rounds > 2
+    assert st.rounds == 1 and st.tile_visits > 32 * 32   # one persistent launch, tiles visited again
     assert bits_equal(host(wb), oracle_lib.fill(big, -9999.0))
+
+
+def test_fill_persistent_and_round_forms_agree(ctx, oracle_lib, monkeypatch):
+    """The persistent launch (device work queue) and the round launches reach
+    the same bytes as the oracle; the persistent form is one launch."""
+    dem = synth.hydro_dem(700, 900, seed=43)
+    ref = oracle_lib.fill(dem, -9999.0, gap=1e-3)
+    w = empty_dev(dem.shape, np.float64)
+    st = ctx.fill(abi.raster(dev(dem), -9999.0), abi.raster(w, -9999.0), gap=1e-3)
+    assert st.rounds == 1 and st.tile_visits >= (700 // 32) * (900 // 32)
+    assert bits_equal(host(w), ref)
+    monkeypatch.setenv("PARGO_FILL_ROUNDS", "1")
+    w2 = empty_dev(dem.shape, np.float64)
+    st2 = ctx.fill(abi.raster(dev(dem), -9999.0), abi.raster(w2, -9999.0), gap=1e-3)
+    assert st2.rounds > 1
+    assert bits_equal(host(w2), ref)
 
 
 def test_fill_edge_cases(ctx, oracle_lib):
