@@ -9,8 +9,10 @@ pit removal with gap 1e-3 m -- one step = pit removal -> Horn slope + D8 on the
 float64 levels, outputs: filled DEM (float32), slope (float32), D8 (int8).
 Metric: Mcells/s of slope+D8+fill (whole job over all GPUs).
 
-Other workloads (secondary lines, --workload): slope32768 (fused slope+D8 on
-32768^2), slope1024, sca16384, batch512, grad8192.
+Other workloads (secondary lines, --workload): slope32768 / slope8192 /
+slope1024 (fused slope+D8), batch512 (512 uneven rasters, batched vs plain),
+sca16384 (SCA on the filled 16384^2 DEM), grad8192 (slope forward+adjoint);
+hydro2048 and sca4096 are small cases of the same code for profiler captures.
 
 Multi-GPU: replicas only -- each rank runs the same workload on its own GPU,
 nothing is exchanged on the data path; value = all ranks' cells / max time.
@@ -35,6 +37,9 @@ sys.path.insert(0, HERE)
 ND = -9999.0
 MEASURED_PEAKS = os.path.join(HERE, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# dram__bytes_read.sum + dram__bytes_write.sum per cell of focal_tma_kernel,
+# from its ncu capture on 8192^2 (301.3 MB + 289.3 MB over 67108864 cells)
+FOCAL_DRAM_BYTES_PER_CELL = (301.330688e6 + 289.264128e6) / 67108864
 
 
 def hbm_peak():
@@ -151,7 +156,9 @@ def cpu_sample_hydro(dem, threads):
     filled levels (OpenMP over rows)."""
     import oracle
     O = oracle.Oracle()
-    crop = np.ascontiguousarray(dem[2000:3024, 3000:4024])
+    r0 = max(0, min(2000, dem.shape[0] - 1024))
+    c0 = max(0, min(3000, dem.shape[1] - 1024))
+    crop = np.ascontiguousarray(dem[r0:r0 + 1024, c0:c0 + 1024])
     t0 = time.perf_counter()
     w, sweeps = O.fill_gs(crop, ND, gap=1e-3)
     O.slope(w, ND, 30.0, threads=threads)
@@ -160,12 +167,12 @@ def cpu_sample_hydro(dem, threads):
     return crop.size, dt, sweeps
 
 
-def run_hydro(args, ws, rank, local):
+def run_hydro(args, ws, rank, local, side=8192):
     import torch
     from pargo_gb300 import abi
     torch.cuda.set_device(local)
     ctx = abi.Context(local)
-    dem = make_hydro()
+    dem = make_hydro(side, side)
     rows, cols = dem.shape
     cells = rows * cols
     stream = torch.cuda.current_stream()
@@ -255,9 +262,12 @@ def run_hydro(args, ws, rank, local):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 levels (emulated on integer pipes), f32 slope",
         "data": "synthetic (seeded fBm, same shapes and value distributions as the named workload)",
-        "config": {"workload": "hydro8192: D8 + Planchon-Darboux fill (gap 1e-3 m) + Horn slope, 8192x8192 "
-                               "float32 fBm DEM (seed 1, H 0.75, 0-3000 m, 30 m), 1% pits, 10% nodata blob",
-                   "rows": rows, "cols": cols, "l2": "inputs larger than L2 (268 MB DEM, 537 MB float64 levels)",
+        "config": {"workload": "hydro%d: D8 + Planchon-Darboux fill (gap 1e-3 m) + Horn slope, %dx%d "
+                               "float32 fBm DEM (seed 1, H 0.75, 0-3000 m, 30 m), 1%% pits, 10%% nodata blob"
+                               % (side, side, side),
+                   "rows": rows, "cols": cols,
+                   "l2": "inputs larger than L2 (%d MB DEM, %d MB float64 levels)" % (cells * 4 >> 20, cells * 8 >> 20)
+                   if cells * 4 > (129 << 20) else "DEM smaller than L2 (profiling case)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "roofline": roofline, "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_value, 2), "unit": "Mcells/s", "h2d_bytes_per_step": cells * 4,
@@ -312,8 +322,11 @@ def run_slope(args, ws, rank, local, side):
         "config": {"workload": "slope%d: fused Horn slope + D8, %dx%d float32 fBm DEM" % (side, side, side),
                    "l2": "flushed between iterations" if flush is not None else "inputs larger than L2"},
         "roofline": {"bound": "hbm", "kernel": "focal_tma_kernel", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind, "traffic": None,
-                     "variant": best, "variant_ms": tune_ms},
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
+                     # DRAM read + write of one launch, scaled by cells from the 8192^2 ncu capture
+                     # (590.6 MB per 67.1 M cells; the traffic grows with the cell count)
+                     "traffic": round(FOCAL_DRAM_BYTES_PER_CELL * cells),
+                     "traffic_source": "ncu 8192^2 capture scaled per cell", "variant": best, "variant_ms": tune_ms},
         "gpu_launches": args.steps, "clocks": clk,
     }
 
@@ -399,6 +412,167 @@ def run_batch(args, ws, rank, local):
     }
 
 
+def timed_steps(fn, args, stream, flush=None):
+    """W untimed steps, then K steps bracketed by CUDA events on `stream`
+    (L2 flushed before each step when `flush` is given); mean ms per step."""
+    import torch
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        if flush is not None:
+            flush.fill_(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return float(np.mean(times))
+
+
+def run_sca(args, ws, rank, local, side=16384):
+    """D8 specific catchment area on the filled side^2 DEM of the hydro
+    generator (seed 2, 10 m cells): setup (untimed) fills the DEM and derives
+    the int8 D8 codes on the GPU; a step is one SCA call (topological
+    accumulation, float64 output)."""
+    import torch
+    from pargo_gb300 import abi
+    torch.cuda.set_device(local)
+    ctx = abi.Context(local)
+    from pargo_gb300 import synth
+    dem = synth.hydro_dem(side, side, seed=2, hurst=0.75, relief=3000.0)
+    cells = side * side
+    stream = torch.cuda.current_stream()
+    R = abi.raster
+    d = torch.from_numpy(dem).cuda()
+    del dem
+    codes = torch.empty((side, side), dtype=torch.int8, device="cuda")
+    ctx.hydro_pipeline(R(d, ND, 10.0), d8=R(codes, -128), gap=1e-3, stream=stream)
+    del d
+    out = torch.empty((side, side), dtype=torch.float64, device="cuda")
+    rc, ro = R(codes, -128), R(out, ND)
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed_steps(lambda: ctx.sca(rc, ro, stream=stream), args, stream)
+    clk = clocks.stop()
+    ms = max_over_ranks(ms, ws, torch.device("cuda", local))
+    # end to end with host buffers: codes in, float64 SCA out
+    hc = codes.cpu().pin_memory()
+    ho = torch.empty((side, side), dtype=torch.float64).pin_memory()
+    rh = (R(hc, -128), R(ho, ND))
+    ctx.sca(*rh, stream=stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        ctx.sca(*rh, stream=stream)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, ws, torch.device("cuda", local))
+    cpu = None
+    if rank == 0 and ws == 1:
+        import oracle
+        O = oracle.Oracle()
+        crop = host_codes_crop(hc, 2048)
+        t0 = time.perf_counter()
+        O.sca(crop, -128.0)
+        dt = time.perf_counter() - t0
+        cpu = {"value": round(crop.size / dt / 1e6, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
+               "sample": "2048x2048 crop of the same D8 codes: the oracle's topological SCA (serial), %.2f s" % dt}
+    peak, kind = hbm_peak()
+    achieved = cells * 9.0 / (ms * 1e-3) / 1e9
+    return {
+        "metric": "Mcells/s D8 SCA", "value": round(ws * cells / (ms * 1e-3) / 1e6, 1), "unit": "Mcells/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 accumulation (u64 counts)",
+        "data": "synthetic",
+        "config": {"workload": "sca%d: D8 SCA on the filled %dx%d hydro DEM (seed 2, 10 m cells), int8 codes in, "
+                               "float64 out" % (side, side, side), "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "kernel": "sca init + walk + finish (one call)", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
+                     "traffic": None, "algorithmic_bytes_per_cell": 9},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells,
+                "d2h_bytes_per_step": cells * 8},
+        "gpu_launches": args.steps * 3, "clocks": clk,
+    }
+
+
+def host_codes_crop(hc, n):
+    a = hc.numpy()
+    r0 = (a.shape[0] - n) // 2
+    c0 = (a.shape[1] - n) // 2
+    crop = np.ascontiguousarray(a[r0:r0 + n, c0:c0 + n]).astype(np.float64)
+    crop[0, :] = crop[-1, :] = crop[:, 0] = crop[:, -1] = -128.0
+    return crop
+
+
+def run_grad(args, ws, rank, local, side=8192):
+    """Differentiable slope: forward + hand-written adjoint of
+    L = sum (slope(z) - slope(z + N(0, 0.5 m)))^2 on a side^2 float32 fBm DEM
+    (seed 3); a step is one fused loss+gradient call (loss read back)."""
+    import torch
+    from pargo_gb300 import abi, synth
+    torch.cuda.set_device(local)
+    ctx = abi.Context(local)
+    z = synth.slope_dem(side, side, seed=3, hurst=0.8, relief=2000.0)
+    zr = synth.perturbed(z, sigma=0.5, seed=3)
+    cells = side * side
+    stream = torch.cuda.current_stream()
+    R = abi.raster
+    dz, dzr = torch.from_numpy(z).cuda(), torch.from_numpy(zr).cuda()
+    g = torch.empty((side, side), dtype=torch.float32, device="cuda")
+    rz, rzr, rg = R(dz, ND, 30.0), R(dzr, ND, 30.0), R(g, ND)
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed_steps(lambda: ctx.slope_loss_grad(rz, rzr, rg, stream=stream), args, stream)
+    clk = clocks.stop()
+    ms = max_over_ranks(ms, ws, torch.device("cuda", local))
+    hz, hzr = pinned(z), pinned(zr)
+    hg = torch.empty((side, side), dtype=torch.float32).pin_memory()
+    rh = (R(hz, ND, 30.0), R(hzr, ND, 30.0), R(hg, ND))
+    ctx.slope_loss_grad(*rh, stream=stream)
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        ctx.slope_loss_grad(*rh, stream=stream)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, ws, torch.device("cuda", local))
+    cpu = None
+    if rank == 0 and ws == 1:
+        import oracle
+        O = oracle.Oracle()
+        thr = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        O.slope(z[:2048], ND, 30.0, threads=thr)
+        O.slope(zr[:2048], ND, 30.0, threads=thr)
+        dt = time.perf_counter() - t0
+        cpu = {"value": round(2048 * side / dt / 1e6, 3), "unit": "Mcells/s", "cores": thr, "kind": "port",
+               "sample": "the reference has no adjoint: its forward Horn slope (oracle, OpenMP) on the first 2048 "
+                         "rows of z and z_ref, %.2f s" % dt}
+    peak, kind = hbm_peak()
+    achieved = cells * 12.0 / (ms * 1e-3) / 1e9
+    return {
+        "metric": "Mcells/s slope forward+backward", "value": round(ws * cells / (ms * 1e-3) / 1e6, 1),
+        "unit": "Mcells/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (loss summed in f64)",
+        "data": "synthetic",
+        "config": {"workload": "grad%d: fused Horn slope forward + adjoint of sum (slope(z) - slope(z_ref))^2, "
+                               "%dx%d float32 fBm DEM (seed 3), z_ref = z + N(0, 0.5 m)" % (side, side, side),
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "kernel": "grad fused forward+adjoint", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
+                     "traffic": None, "algorithmic_bytes_per_cell": 12},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells * 8,
+                "d2h_bytes_per_step": cells * 4 + 8},
+        "gpu_launches": args.steps, "clocks": clk,
+    }
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
@@ -431,14 +605,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hydro8192",
-                    choices=["hydro8192", "slope32768", "slope8192", "slope1024", "batch512"])
+                    choices=["hydro8192", "hydro2048", "slope32768", "slope8192", "slope1024", "batch512",
+                             "sca16384", "sca4096", "grad8192"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         out = run_reference(args, ws, rank)
-    elif args.workload == "hydro8192":
-        out = run_hydro(args, ws, rank, local)
+    elif args.workload.startswith("hydro"):
+        out = run_hydro(args, ws, rank, local, int(args.workload[5:]))
+    elif args.workload.startswith("sca"):
+        out = run_sca(args, ws, rank, local, int(args.workload[3:]))
+    elif args.workload == "grad8192":
+        out = run_grad(args, ws, rank, local)
     elif args.workload == "batch512":
         out = run_batch(args, ws, rank, local)
     else:

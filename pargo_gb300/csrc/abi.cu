@@ -1092,7 +1092,6 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
     std::vector<int64_t> start(count + 1), ntx(count);
     std::vector<InView> views(count);
     int64_t total = 0;
-    bool fast = true;
     for (int k = 0; k < count; k++) {
         const int i = order[k];
         const pargo_raster* d = &dems[i];
@@ -1110,7 +1109,8 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
         if (d8s) p.d8 = OutView{(char*)d8s[i].data, pitch_of(&d8s[i]), d8s[i].dtype, d8s[i].nodata};
         p.fallbacks = &ctx->d_counters[0];
         p.error_flag = ctx->d_error;
-        if (!fast_out_ok(p)) fast = false;
+        p.fast_out = fast_out_ok(p) ? 1 : 0;
+        p.fd = method == PARGO_SLOPE_FD || !slopes;
         views[k] = InView{(const char*)d->data, pitch_of(d), d->dtype};
         start[k] = total;
         if (all_tma) {
@@ -1150,8 +1150,8 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
     }
     CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
     if (all_tma)
-        CU(ctx, launch_batch_tma(dmaps, dparams, dstart, dntx, count, total, fast ? 1 : 0,
-                                 (method == PARGO_SLOPE_FD || !slopes) ? 1 : 0, claim, &ctx->d_counters[0],
+        CU(ctx, launch_batch_tma(dmaps, dparams, dstart, dntx, count, total, slopes ? 1 : 0, d8s ? 1 : 0, claim,
+                                 &ctx->d_counters[0],
                                  ctx->d_error, ctx->num_sms, s));
     else
         CU(ctx, launch_batch_generic(dparams, ddems, dstart, count, total, &ctx->d_counters[0], ctx->num_sms, s));

@@ -14,6 +14,8 @@
 // Everything else (other pitches, float64 input, other output types) runs the
 // generic one-cell-per-thread kernel below.
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "tma.cuh"
@@ -90,15 +92,12 @@ __device__ __forceinline__ void count_fallbacks(int fell_back, unsigned long lon
 }
 
 // Row `ty` (tile-local, -1 .. kTH) of the stage as this lane's 6 values:
-// columns 4l-1 .. 4l+4.  Centre four by one float4, the outer two by shuffle.
+// columns 4l-1 .. 4l+4 (box columns 4l+3 .. 4l+8): one 16-byte load and two
+// scalar loads.
 __device__ __forceinline__ void load_row(const float* s, int ty, int lane, float v[6]) {
-    const float* row = s + (ty + 1) * kBoxW;
-    const float4 q = *reinterpret_cast<const float4*>(row + 4 * lane + 4);
-    float left = __shfl_up_sync(0xffffffffu, q.w, 1);
-    float right = __shfl_down_sync(0xffffffffu, q.x, 1);
-    if (lane == 0) left = row[3];
-    if (lane == 31) right = row[4 * 31 + 8];
-    v[0] = left; v[1] = q.x; v[2] = q.y; v[3] = q.z; v[4] = q.w; v[5] = right;
+    const float* row = s + (ty + 1) * kBoxW + 4 * lane + 3;
+    const float4 q = *reinterpret_cast<const float4*>(row + 1);
+    v[0] = row[0]; v[1] = q.x; v[2] = q.y; v[3] = q.z; v[4] = q.w; v[5] = row[5];
 }
 
 // Whether some of the 6 values may lie in the wide (Eps 1e-6) nodata band.
@@ -110,24 +109,94 @@ __device__ __forceinline__ bool row_maybe_nodata(const float v[6], const Band<fl
     return mn <= b.hi && mx >= b.lo;
 }
 
-// FP32 D8 fast path on the eight drops x (window order, x4 unused): returns
-// the code when the maximum is single and certain, else kD8Unsure.
-//   M vs 1e-6: |x_k - r_k| <= 2^-22 x_k;
+// Packed FP32 pairs (one f32x2 instruction for two IEEE operations, each
+// rounded exactly as the scalar operation).
+#ifndef PARGO_PACK
+#define PARGO_PACK 0
+#endif
+#if PARGO_PACK == 0
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return make_float2(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    return make_float2(__fmaf_rn(a.x, b.x, c.x), __fmaf_rn(a.y, b.y, c.y));
+}
+#else
+#if PARGO_PACK == 1
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+#else
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+#endif
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+#endif
+__device__ __forceinline__ float2 pr(float a, float b) { return make_float2(a, b); }
+
+// Byte permute in the sign-replicating form: a selector nibble with bit 3
+// set yields the selected byte's top bit copied over all eight bits.
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+    return d;
+}
+
+// FP32 D8 fast path on the eight drops (window order; the centre is absent):
+// the window index of a certain single maximum, -1 when the maximum is
+// certainly below 1e-6, else kD8Unsure.
+//   M vs 1e-6: |x_k - r_k| <= 2^-22 x_k, so x < kLowCut gives M < 1e-6 and
+//   x > kHighCut gives M >= 1e-6 for certain;
 //   single maximum: every other x_i <= m - (1e-6 + 2^-19 m) is certainly
 //   outside the tie set (x_i >= 0: |x_i| <= m; x_i < 0: the gap exceeds m).
-__device__ __forceinline__ int d8_fast(float x0, float x1, float x2, float x3, float x5, float x6, float x7, float x8,
-                                       int dir_type) {
+constexpr float kLowCut = 0.99996924e-6f;   // kTLo (1 - 2^-21), rounded down
+constexpr float kHighCut = 1.0000329e-6f;   // kTHi (1 + 2^-21), rounded up
+constexpr float k2m19 = 1.9073486328125e-06f;
+#ifndef PARGO_D8MASK
+#define PARGO_D8MASK 0
+#endif
+#if PARGO_D8MASK
+__device__ __forceinline__ int d8_fast(float x0, float x1, float x2, float x3, float x5, float x6, float x7, float x8) {
     const float m = fmaxf(fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)), fmaxf(fmaxf(x5, x6), fmaxf(x7, x8)));
-    if (m <= 0.0f) return -1;
-    const float em = m * k2m22;
-    if (m + em < kTLo) return -1;
-    if (!(m - em > kTHi)) return kD8Unsure;
-    const float t = m - (kTHi + m * 1.9073486328125e-06f);  // 2^-19
+    const float t = __fadd_rn(__fmaf_rn(m, -k2m19, m), -kTHi);
     const unsigned mask = (x0 > t ? 1u : 0u) | (x1 > t ? 2u : 0u) | (x2 > t ? 4u : 0u) | (x3 > t ? 8u : 0u) |
                           (x5 > t ? 32u : 0u) | (x6 > t ? 64u : 0u) | (x7 > t ? 128u : 0u) | (x8 > t ? 256u : 0u);
-    if (mask & (mask - 1)) return kD8Unsure;
     const int k = __ffs(mask) - 1;
-    return dir_type == 8 ? k : d8_bit_code(k);
+    const bool single = (mask & (mask - 1)) == 0;
+    return m < kLowCut ? -1 : (m > kHighCut && single) ? k : kD8Unsure;
+}
+#else
+__device__ __forceinline__ int d8_fast(float x0, float x1, float x2, float x3, float x5, float x6, float x7, float x8) {
+    const float m = fmaxf(fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)), fmaxf(fmaxf(x5, x6), fmaxf(x7, x8)));
+    const float t = __fadd_rn(__fmaf_rn(m, -k2m19, m), -kTHi);
+    // x_i > t  <=>  t - x_i < 0: gather the eight sign bits, each replicated
+    // over one byte, for x0..x3 in `ua` and x5..x8 in `ub`; blend them into
+    // one word (ua on even bits, ub on odd bits).  A single x_i above t sets
+    // exactly four bits, and the highest of them gives i.
+    const float2 tt = pr(t, t);
+    const float2 d01 = sub2(tt, pr(x0, x1)), d23 = sub2(tt, pr(x2, x3));
+    const float2 d56 = sub2(tt, pr(x5, x6)), d78 = sub2(tt, pr(x7, x8));
+    const uint32_t ua = prmt(prmt(__float_as_uint(d01.x), __float_as_uint(d01.y), 0x00FB),
+                             prmt(__float_as_uint(d23.x), __float_as_uint(d23.y), 0x00FB), 0x5410);
+    const uint32_t ub = prmt(prmt(__float_as_uint(d56.x), __float_as_uint(d56.y), 0x00FB),
+                             prmt(__float_as_uint(d78.x), __float_as_uint(d78.y), 0x00FB), 0x5410);
+    const uint32_t w = (ua & 0x55555555u) | (ub & 0xAAAAAAAAu);
+    const int hb = 31 - __clz(w);
+    const int k = (hb >> 3) + (hb & 1) * 5;  // byte b of ua -> window b, of ub -> window b + 5
+    return m < kLowCut ? -1 : (m > kHighCut && __popc(w) == 4) ? k : kD8Unsure;
+}
+#endif
+
+// ArcGIS weight of a window index (d8Operator.cpp:96-97): 1 << shift, the
+// shifts packed as nibbles 0..8 = 5,6,7,4,-,0,3,2,1.
+__device__ __forceinline__ int d8_weight(int k) {
+    return (unsigned)k > 8u ? k : 1 << (int)((0x123004765ULL >> (4 * k)) & 15);  // -1 and kD8Unsure pass through
 }
 
 // One (4 ROWS) x 128 tile from its TMA stage `s` ((4 ROWS + 2) x 136 floats,
@@ -141,122 +210,160 @@ __device__ __forceinline__ int d8_fast(float x0, float x1, float x2, float x3, f
 //             e2[a] = (z(r, a+1) - z(r+1, a)) / sqrt 2        (SW of a, -NE of row r+1)
 // (negating an IEEE difference is exact, so each drop is bit-identical to
 // z4 - z_i computed per cell).  Horn numerators come from two-apart
-// differences sh (rows) and sv (columns).  Windows that may touch nodata, the
-// ring, other slope methods and uncertain D8 decisions take cell_general.
-template <int FAST_OUT, bool FD, int ROWS, int UNROLL>
+// differences sh (rows) and sv (columns).  Arithmetic runs on packed f32x2
+// pairs.  The main loop has no per-cell branch: cells whose window may touch
+// nodata or the raster's ring, any slope method but Horn, and D8 decisions the
+// FP32 bounds cannot certify are marked in a bit set and recomputed from the
+// stage by cell_general afterwards (overwriting what the loop stored).
+template <int ROWS, int UNROLL, bool SLOPE, bool D8>
 __device__ __forceinline__ void compute_tile(const float* s, int64_t y0, int64_t x0, const FocalParams& p,
                                              int& fell_back) {
-    constexpr int kRowsPerWarp = ROWS;
-    const float kinv = 0.70710677f;
+    const float2 kinv2 = pr(0.70710677f, 0.70710677f);
+    const float2 two2 = pr(2.0f, 2.0f);
+    const float2 kfd2 = pr(p.sk.k_fd, p.sk.k_fd);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r0 = warp * kRowsPerWarp;
+    const int r0 = warp * ROWS;
     const int64_t gx0 = x0 + 4 * lane, gy0 = y0 + r0;
-    const bool interior = gy0 >= 1 && gy0 + kRowsPerWarp <= p.rows - 1 && gx0 >= 1 && gx0 + 4 <= p.cols - 1;
+    const bool interior = p.fd && gy0 >= 1 && gy0 + ROWS <= p.rows - 1 && gx0 >= 1 && gx0 + 4 <= p.cols - 1;
+    const bool dir8 = p.dir_type == 8;
+    unsigned redo = 0;  // bit i: row i's four cells go to the general path
     float va[6], vb[6], vc[6];
     load_row(s, r0 - 1, lane, va);
     load_row(s, r0, lane, vb);
     bool nda = row_maybe_nodata(va, p.nd6f), ndb = row_maybe_nodata(vb, p.nd6f);
-    float shA[4], shB[4], vN[4], nw[4], ne[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        shA[j] = va[j + 2] - va[j];
-        shB[j] = vb[j + 2] - vb[j];
-        vN[j] = vb[j + 1] - va[j + 1];
-        nw[j] = (vb[j + 1] - va[j]) * kinv;
-        ne[j] = (vb[j + 1] - va[j + 2]) * kinv;
+    float shA[4], shB[4], nS[4], e1p[5], e2p[5];  // nS, e1p, e2p: the previous row's vS, e1, e2
+    {
+        const float2 a01 = sub2(pr(va[2], va[3]), pr(va[0], va[1])), a23 = sub2(pr(va[4], va[5]), pr(va[2], va[3]));
+        const float2 b01 = sub2(pr(vb[2], vb[3]), pr(vb[0], vb[1])), b23 = sub2(pr(vb[4], vb[5]), pr(vb[2], vb[3]));
+        shA[0] = a01.x; shA[1] = a01.y; shA[2] = a23.x; shA[3] = a23.y;
+        shB[0] = b01.x; shB[1] = b01.y; shB[2] = b23.x; shB[3] = b23.y;
+        // previous-row quantities seen from row b: vS = va[j+1] - vb[j+1],
+        // e1[a] = (va[a] - vb[a+1]) / sqrt 2, e2[a] = (va[a+1] - vb[a]) / sqrt 2
+        const float2 s01 = sub2(pr(va[1], va[2]), pr(vb[1], vb[2])), s23 = sub2(pr(va[3], va[4]), pr(vb[3], vb[4]));
+        nS[0] = s01.x; nS[1] = s01.y; nS[2] = s23.x; nS[3] = s23.y;
+        const float2 p01 = mul2(sub2(pr(va[0], va[1]), pr(vb[1], vb[2])), kinv2);
+        const float2 p23 = mul2(sub2(pr(va[2], va[3]), pr(vb[3], vb[4])), kinv2);
+        const float2 q01 = mul2(sub2(pr(va[1], va[2]), pr(vb[0], vb[1])), kinv2);
+        const float2 q23 = mul2(sub2(pr(va[3], va[4]), pr(vb[2], vb[3])), kinv2);
+        const float2 pq4 = mul2(sub2(pr(va[4], va[5]), pr(vb[5], vb[4])), kinv2);
+        e1p[0] = p01.x; e1p[1] = p01.y; e1p[2] = p23.x; e1p[3] = p23.y; e1p[4] = pq4.x;
+        e2p[0] = q01.x; e2p[1] = q01.y; e2p[2] = q23.x; e2p[3] = q23.y; e2p[4] = pq4.y;
     }
+    char* srow = SLOPE ? p.slope.base + gy0 * p.slope.pitch : nullptr;
+    char* drow = D8 ? p.d8.base + gy0 * p.d8.pitch : nullptr;
+    const bool vec = p.fast_out && gx0 + 3 < p.cols;
 #pragma unroll UNROLL
-    for (int i = 0; i < kRowsPerWarp; i++) {
+    for (int i = 0; i < ROWS; i++) {
         load_row(s, r0 + i + 1, lane, vc);
         const bool ndc = row_maybe_nodata(vc, p.nd6f);
-        float shC[4], h[5], vS[4], e1[5], e2[5], sv[6];
-#pragma unroll
-        for (int a = 0; a < 5; a++) {
-            h[a] = vb[a + 1] - vb[a];
-            e1[a] = (vb[a] - vc[a + 1]) * kinv;
-            e2[a] = (vb[a + 1] - vc[a]) * kinv;
-        }
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            shC[j] = vc[j + 2] - vc[j];
-            vS[j] = vb[j + 1] - vc[j + 1];
-        }
-#pragma unroll
-        for (int a = 0; a < 6; a++) sv[a] = va[a] - vc[a];
-        const bool slow_row = !FD || nda || ndb || ndc || !interior;
-        const int64_t gy = gy0 + i;
+        // row-b / row-c differences
+        const float2 c01 = sub2(pr(vc[2], vc[3]), pr(vc[0], vc[1])), c23 = sub2(pr(vc[4], vc[5]), pr(vc[2], vc[3]));
+        const float2 v01 = sub2(pr(va[0], va[1]), pr(vc[0], vc[1])), v23 = sub2(pr(va[2], va[3]), pr(vc[2], vc[3]));
+        const float2 v45 = sub2(pr(va[4], va[5]), pr(vc[4], vc[5]));
+        const float2 h01 = sub2(pr(vb[1], vb[2]), pr(vb[0], vb[1])), h23 = sub2(pr(vb[3], vb[4]), pr(vb[2], vb[3]));
+        const float2 s01 = sub2(pr(vb[1], vb[2]), pr(vc[1], vc[2])), s23 = sub2(pr(vb[3], vb[4]), pr(vc[3], vc[4]));
+        const float2 p01 = mul2(sub2(pr(vb[0], vb[1]), pr(vc[1], vc[2])), kinv2);
+        const float2 p23 = mul2(sub2(pr(vb[2], vb[3]), pr(vc[3], vc[4])), kinv2);
+        const float2 q01 = mul2(sub2(pr(vb[1], vb[2]), pr(vc[0], vc[1])), kinv2);
+        const float2 q23 = mul2(sub2(pr(vb[3], vb[4]), pr(vc[2], vc[3])), kinv2);
+        const float2 pq4 = mul2(sub2(pr(vb[4], vb[5]), pr(vc[5], vc[4])), kinv2);
+        const float2 h4s = sub2(pr(vb[5], 0.0f), pr(vb[4], 0.0f));
+        const float h[5] = {h01.x, h01.y, h23.x, h23.y, h4s.x};
+        const float vS[4] = {s01.x, s01.y, s23.x, s23.y};
+        const float e1[5] = {p01.x, p01.y, p23.x, p23.y, pq4.x};
+        const float e2[5] = {q01.x, q01.y, q23.x, q23.y, pq4.y};
+        const bool slow = !interior || nda || ndb || ndc;
         float sl[4];
         int cd[4];
-        int fl[4];
+        if (SLOPE) {
+            const float2 nx01 = fma2(two2, pr(shB[0], shB[1]), add2(pr(shA[0], shA[1]), c01));
+            const float2 nx23 = fma2(two2, pr(shB[2], shB[3]), add2(pr(shA[2], shA[3]), c23));
+            const float2 ny01 = fma2(two2, pr(v01.y, v23.x), add2(v01, pr(v23.x, v23.y)));
+            const float2 ny23 = fma2(two2, pr(v23.y, v45.x), add2(v23, v45));
+            const float2 q01s = fma2(nx01, nx01, mul2(ny01, ny01));
+            const float2 q23s = fma2(nx23, nx23, mul2(ny23, ny23));
+            const float2 r01 = mul2(pr(sqrt_sfu(q01s.x), sqrt_sfu(q01s.y)), kfd2);
+            const float2 r23 = mul2(pr(sqrt_sfu(q23s.x), sqrt_sfu(q23s.y)), kfd2);
+            sl[0] = r01.x; sl[1] = r01.y; sl[2] = r23.x; sl[3] = r23.y;
+            if (p.sk.degrees) {
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            int code = kD8Unsure;
-            float slope = 0.0f;
-            fl[j] = 0;
-            if (!slow_row) {
-                if (p.do_slope) {
-                    const float nx = __fmaf_rn(2.0f, shB[j], __fadd_rn(shA[j], shC[j]));
-                    const float ny = __fmaf_rn(2.0f, sv[j + 1], __fadd_rn(sv[j], sv[j + 2]));
-                    slope = horn_slope(nx, ny, p.sk.k_fd);
-                    if (p.sk.degrees) slope = atanf(slope) * 57.29577951308232f;
-                }
-                code = p.do_d8 ? d8_fast(nw[j], vN[j], ne[j], h[j], -h[j + 1], e2[j], vS[j], e1[j + 1], p.dir_type)
-                               : 0;
+                for (int j = 0; j < 4; j++) sl[j] = atanf(sl[j]) * 57.29577951308232f;
             }
-            if (code == kD8Unsure) {
-                const int64_t gx = gx0 + j;
-                const bool ring = gy <= 0 || gx <= 0 || gy >= p.rows - 1 || gx >= p.cols - 1;
-                const CellOut o = cell_general<float>(va[j], va[j + 1], va[j + 2], vb[j], vb[j + 1], vb[j + 2],
-                                                      vc[j], vc[j + 1], vc[j + 2], &p, ring);
-                slope = o.slope;
-                code = o.code;
-                fl[j] = o.flags;
-                fell_back += (o.flags >> 2) & 1;
-            }
-            sl[j] = (fl[j] & 1) ? (float)p.slope.nodata : slope;
-            cd[j] = (fl[j] & 2) ? (int)(int8_t)p.d8.nodata : code;
         }
+        if (D8) {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                cd[j] = d8_fast(-e1p[j], -nS[j], -e2p[j + 1], h[j], -h[j + 1], e2[j], vS[j], e1[j + 1]);
+        }
+        bool rb = slow;
+        if (D8) {
+            rb = rb || cd[0] == kD8Unsure || cd[1] == kD8Unsure || cd[2] == kD8Unsure || cd[3] == kD8Unsure;
+            if (!dir8) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) cd[j] = d8_weight(cd[j]);
+            }
+        }
+        redo |= (rb ? 1u : 0u) << i;
+        const int64_t gy = gy0 + i;
         if (gy < p.rows) {
-            if (FAST_OUT && gx0 + 3 < p.cols) {
-                if (p.do_slope) {
-                    float4* o = reinterpret_cast<float4*>(p.slope.base + gy * p.slope.pitch) + (gx0 >> 2);
-                    *o = make_float4(sl[0], sl[1], sl[2], sl[3]);
-                }
-                if (p.do_d8) {
-                    const uint32_t w = (uint32_t)(uint8_t)cd[0] | ((uint32_t)(uint8_t)cd[1] << 8) |
-                                       ((uint32_t)(uint8_t)cd[2] << 16) | ((uint32_t)(uint8_t)cd[3] << 24);
-                    reinterpret_cast<uint32_t*>(p.d8.base + gy * p.d8.pitch)[gx0 >> 2] = w;
-                }
-            } else {
+            if (vec) {
+                if (SLOPE) *reinterpret_cast<float4*>(srow + 4 * gx0) = make_float4(sl[0], sl[1], sl[2], sl[3]);
+                if (D8)
+                    *reinterpret_cast<uint32_t*>(drow + gx0) = __byte_perm(
+                        __byte_perm((uint32_t)cd[0], (uint32_t)cd[1], 0x0040), __byte_perm((uint32_t)cd[2], (uint32_t)cd[3], 0x0040),
+                        0x5410);
+            } else if (!rb) {
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int64_t gx = gx0 + j;
                     if (gx >= p.cols) break;
-                    if (p.do_slope) put_value(p.slope, gy, gx, (fl[j] & 1) ? p.slope.nodata : (double)sl[j]);
-                    if (p.do_d8) put_value(p.d8, gy, gx, (fl[j] & 2) ? p.d8.nodata : (double)cd[j]);
+                    if (SLOPE) put_value(p.slope, gy, gx, (double)sl[j]);
+                    if (D8) put_value(p.d8, gy, gx, (double)cd[j]);
                 }
             }
         }
+        if (SLOPE) srow += p.slope.pitch;
+        if (D8) drow += p.d8.pitch;
         // roll the window down one row
 #pragma unroll
         for (int a = 0; a < 6; a++) {
             va[a] = vb[a];
             vb[a] = vc[a];
         }
+        shA[0] = shB[0]; shA[1] = shB[1]; shA[2] = shB[2]; shA[3] = shB[3];
+        shB[0] = c01.x; shB[1] = c01.y; shB[2] = c23.x; shB[3] = c23.y;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            shA[j] = shB[j];
-            shB[j] = shC[j];
-            vN[j] = -vS[j];
-            nw[j] = -e1[j];
-            ne[j] = -e2[j + 1];
+        for (int j = 0; j < 4; j++) nS[j] = vS[j];
+#pragma unroll
+        for (int a = 0; a < 5; a++) {
+            e1p[a] = e1[a];
+            e2p[a] = e2[a];
         }
         nda = ndb;
         ndb = ndc;
     }
+    // Cells the loop could not finish: the general path on the staged window.
+    while (redo) {
+        const int i = __ffs(redo) - 1;
+        redo &= redo - 1;
+        const int64_t gy = gy0 + i;
+        if (gy >= p.rows) break;  // rows only grow from here
+#pragma unroll 1
+        for (int j = 0; j < 4; j++) {
+            const int64_t gx = gx0 + j;
+            if (gx >= p.cols) break;
+            const bool ring = gy <= 0 || gx <= 0 || gy >= p.rows - 1 || gx >= p.cols - 1;
+            const float* w = s + (r0 + i) * kBoxW + 4 * lane + j + 3;  // window's top-left: stage row r0+i, col 4l+j+3
+            const CellOut o = cell_general<float>(w[0], w[1], w[2], w[kBoxW], w[kBoxW + 1], w[kBoxW + 2], w[2 * kBoxW],
+                                                  w[2 * kBoxW + 1], w[2 * kBoxW + 2], &p, ring);
+            fell_back += (o.flags >> 2) & 1;
+            if (SLOPE) put_value(p.slope, gy, gx, (o.flags & 1) ? p.slope.nodata : (double)o.slope);
+            if (D8) put_value(p.d8, gy, gx, (o.flags & 2) ? p.d8.nodata : (double)o.code);
+        }
+    }
 }
 
-template <int FAST_OUT, bool FD, int ROWS, int UNROLL, int MINB>
+template <int ROWS, int UNROLL, int MINB, bool SLOPE, bool D8>
 __global__ void __launch_bounds__(kThreads, MINB) focal_tma_kernel(const __grid_constant__ CUtensorMap map,
                                                                 const __grid_constant__ FocalParams p, int64_t ntx,
                                                                 int64_t ntiles) {
@@ -293,7 +400,7 @@ __global__ void __launch_bounds__(kThreads, MINB) focal_tma_kernel(const __grid_
             if (p.error_flag) atomicExch(p.error_flag, 1);
             return;
         }
-        compute_tile<FAST_OUT, FD, ROWS, UNROLL>(reinterpret_cast<const float*>(smem + st * kStageStride),
+        compute_tile<ROWS, UNROLL, SLOPE, D8>(reinterpret_cast<const float*>(smem + st * kStageStride),
                                                  (t / ntx) * kTH, (t % ntx) * kTW, p, fell_back);
         __syncthreads();  // every thread is done with stage st before it is refilled
     }
@@ -332,7 +439,7 @@ __global__ void __launch_bounds__(256) focal_generic_kernel(const InView dem, co
 // own TMA descriptor in global memory; the next tile's load is in flight while
 // the current one is computed.
 constexpr int kBatchRows = 8;
-template <int FAST_OUT, bool FD>
+template <bool SLOPE, bool D8>
 __global__ void __launch_bounds__(kThreads, 5) batch_tma_kernel(const CUtensorMap* maps, const FocalParams* params,
                                                              const int64_t* tile_start, const int64_t* ntx_of,
                                                              int count, int64_t total, unsigned long long* claim,
@@ -381,7 +488,7 @@ __global__ void __launch_bounds__(kThreads, 5) batch_tma_kernel(const CUtensorMa
             return;
         }
         const int64_t local = t - tile_start[item], ntx = ntx_of[item];
-        compute_tile<FAST_OUT, FD, kBatchRows, 1>(reinterpret_cast<const float*>(smem + st * kStageStride),
+        compute_tile<kBatchRows, 1, SLOPE, D8>(reinterpret_cast<const float*>(smem + st * kStageStride),
                                                   (local / ntx) * kTH, (local % ntx) * kTW, params[item], fell_back);
         __syncthreads();
     }
@@ -428,7 +535,7 @@ __global__ void __launch_bounds__(256) batch_generic_kernel(const FocalParams* p
 struct Variant {
     int rows, unroll, minb;
 };
-static const Variant kVariants[] = {{8, 1, 5}, {9, 3, 4}, {12, 3, 4}, {6, 3, 5}, {6, 1, 6}};
+static const Variant kVariants[] = {{8, 1, 5}, {9, 3, 4}, {6, 3, 5}, {6, 6, 5}, {12, 1, 4}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int focal_num_variants() { return kNumVariants; }
@@ -439,14 +546,14 @@ int focal_tma_tile_cols() { return kTW; }
 int focal_tma_box_cols() { return kBoxW; }
 int focal_tma_box_rows() { return Shape<kBatchRows>::kBoxH; }
 
-template <int FAST_OUT, bool FD, int ROWS, int UNROLL, int MINB>
+template <int ROWS, int UNROLL, int MINB, bool SLOPE, bool D8>
 static cudaError_t launch_variant(const CUtensorMap* map, const FocalParams& p, int num_sms, cudaStream_t s) {
     using S = Shape<ROWS>;
     const int64_t ntx = (p.cols + kTW - 1) / kTW, nty = (p.rows + S::kTH - 1) / S::kTH;
     const int64_t ntiles = ntx * nty;
     if (ntiles == 0) return cudaSuccess;
     const size_t smem = 2 * S::kStageStride;
-    auto kern = focal_tma_kernel<FAST_OUT, FD, ROWS, UNROLL, MINB>;
+    auto kern = focal_tma_kernel<ROWS, UNROLL, MINB, SLOPE, D8>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -459,32 +566,38 @@ static cudaError_t launch_variant(const CUtensorMap* map, const FocalParams& p, 
     return cudaGetLastError();
 }
 
+template <bool SLOPE, bool D8>
+static cudaError_t launch_variants(const CUtensorMap* map, const FocalParams& p, int variant, int num_sms,
+                                   cudaStream_t s) {
+    switch (variant) {
+        case 1: return launch_variant<9, 3, 4, SLOPE, D8>(map, p, num_sms, s);
+        case 2: return launch_variant<6, 3, 5, SLOPE, D8>(map, p, num_sms, s);
+        case 3: return launch_variant<6, 6, 5, SLOPE, D8>(map, p, num_sms, s);
+        case 4: return launch_variant<12, 1, 4, SLOPE, D8>(map, p, num_sms, s);
+        default: return launch_variant<8, 1, 5, SLOPE, D8>(map, p, num_sms, s);
+    }
+}
+
 // The tensor map's box must be (kBoxW, focal_variant_rows(variant) + 2).
 cudaError_t launch_focal_tma(const CUtensorMap* map, const FocalParams& p, int fast_out, int variant, int num_sms,
                              cudaStream_t s) {
-    const bool fd = p.sk.method == PARGO_SLOPE_FD || !p.do_slope;
-    if (fast_out && fd) {
-        switch (variant) {
-            case 1: return launch_variant<1, true, 9, 3, 4>(map, p, num_sms, s);
-            case 2: return launch_variant<1, true, 12, 3, 4>(map, p, num_sms, s);
-            case 3: return launch_variant<1, true, 6, 3, 5>(map, p, num_sms, s);
-            case 4: return launch_variant<1, true, 6, 1, 6>(map, p, num_sms, s);
-            default: return launch_variant<1, true, 8, 1, 5>(map, p, num_sms, s);
-        }
-    }
-    if (fast_out) return launch_variant<1, false, 8, 1, 5>(map, p, num_sms, s);
-    return fd ? launch_variant<0, true, 8, 1, 5>(map, p, num_sms, s)
-              : launch_variant<0, false, 8, 1, 5>(map, p, num_sms, s);
+    FocalParams q = p;
+    q.fast_out = fast_out;
+    q.fd = p.sk.method == PARGO_SLOPE_FD || !p.do_slope;
+    if (q.do_slope && q.do_d8) return launch_variants<true, true>(map, q, variant, num_sms, s);
+    if (q.do_slope) return launch_variants<true, false>(map, q, variant, num_sms, s);
+    if (q.do_d8) return launch_variants<false, true>(map, q, variant, num_sms, s);
+    return cudaSuccess;
 }
 
 cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params, const int64_t* tile_start,
-                             const int64_t* ntx_of, int count, int64_t total_tiles, int fast_out, int fd,
+                             const int64_t* ntx_of, int count, int64_t total_tiles, int do_slope, int do_d8,
                              unsigned long long* claim, unsigned long long* fallbacks, int* error_flag, int num_sms,
                              cudaStream_t s) {
     if (total_tiles == 0) return cudaSuccess;
     const size_t smem = focal_tma_smem_bytes();
-    auto kern = fast_out ? (fd ? batch_tma_kernel<1, true> : batch_tma_kernel<1, false>)
-                         : (fd ? batch_tma_kernel<0, true> : batch_tma_kernel<0, false>);
+    auto kern = do_slope ? (do_d8 ? batch_tma_kernel<true, true> : batch_tma_kernel<true, false>)
+                         : batch_tma_kernel<false, true>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;

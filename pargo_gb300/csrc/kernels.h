@@ -25,6 +25,8 @@ struct FocalParams {
     Band<double> nd6d, nd7d;  // the same for double input
     SlopeConsts sk;
     int do_slope, do_d8, dir_type;
+    int fast_out;  // slope F32 / D8 I8 with 16- / 4-byte aligned rows: vector stores
+    int fd;        // Horn (FD) slope or no slope: the tiled fast path applies
     OutView slope, d8;
     unsigned long long* fallbacks;  // device counter of exact-path D8 cells (may be null)
     int* error_flag;                // device flag: a bounded wait gave up
@@ -44,7 +46,7 @@ int focal_tma_box_rows();
 
 // Batched slope+D8 (focal.cu): device tables of per-raster descriptors/params.
 cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params, const int64_t* tile_start,
-                             const int64_t* ntx_of, int count, int64_t total_tiles, int fast_out, int fd,
+                             const int64_t* ntx_of, int count, int64_t total_tiles, int do_slope, int do_d8,
                              unsigned long long* claim, unsigned long long* fallbacks, int* error_flag, int num_sms,
                              cudaStream_t s);
 cudaError_t launch_batch_generic(const FocalParams* params, const InView* dems, const int64_t* cell_start, int count,
