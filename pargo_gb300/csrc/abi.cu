@@ -33,7 +33,7 @@ struct pargo_ctx {
         void* p = nullptr;
         size_t n = 0;
     };
-    Slot slots[24];
+    Slot slots[32];
     // pinned host scratch (counter read-back, table staging)
     void* pinned = nullptr;
     size_t pinned_n = 0;
@@ -56,8 +56,9 @@ enum SlotId {
     kSlotIn0 = 0, kSlotIn1, kSlotOut0, kSlotOut1, kSlotFillW, kSlotFillLists, kSlotFillQueued,
     kSlotScaIndeg, kSlotScaConv, kSlotScaShip, kSlotScaFlags, kSlotScaCounters, kSlotBatchMaps,
     kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut,
-    kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes
+    kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotCount
 };
+static_assert(kSlotCount <= 32, "context slot table");
 
 namespace {
 
@@ -844,6 +845,38 @@ pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* w
     return PARGO_OK;
 }
 
+// SCA by tiled subtree sums: scratch, launches (stream-ordered), and the
+// check of the completion counts once the stream has been synchronised.
+pargo_status sca_launch(pargo_ctx* ctx, const ScaParams& q, cudaStream_t s, const char* what) {
+    const int64_t n = q.rows * q.cols;
+    const int64_t nodes = ((q.rows + kScaTile - 1) / kScaTile) * ((q.cols + kScaTile - 1) / kScaTile) * kScaSlots;
+    if (nodes >= INT32_MAX) return fail(ctx, PARGO_ERR_INVALID_ARG, "%s: raster too large", what);
+    cudaError_t e;
+    ScaScratch sc{};
+    sc.conv = (unsigned long long*)slot(ctx, kSlotScaConv, (size_t)n * 8, &e);
+    if (!sc.conv) return cuda_fail(ctx, e, "sca totals");
+    sc.ship = (unsigned long long*)slot(ctx, kSlotScaShip, (size_t)n * 8, &e);
+    if (!sc.ship) return cuda_fail(ctx, e, "sca flags");
+    sc.counters = (unsigned long long*)slot(ctx, kSlotScaCounters, 8 * sizeof(unsigned long long), &e);
+    if (!sc.counters) return cuda_fail(ctx, e, "sca counters");
+    void* tb = slot(ctx, kSlotScaTiles, sca_tiles_bytes(q.rows, q.cols), &e);
+    if (!tb) return cuda_fail(ctx, e, "sca tile forest");
+    const ScaTiles T = sca_tiles_layout(tb, q.rows, q.cols);
+    cudaError_t ee = sca_run_tiled(q, sc, T, s);
+    if (ee != cudaSuccess) return cuda_fail(ctx, ee, what);
+    return PARGO_OK;
+}
+
+// hp: the 8 SCA counters copied to the host after the stream finished.
+pargo_status sca_check(pargo_ctx* ctx, const unsigned long long* hp, const char* what) {
+    if (hp[6] != 0)
+        return fail(ctx, PARGO_ERR_CYCLE, "%s: %llu inflows from the raster's ring (never released)", what, hp[6]);
+    if (hp[0] != hp[1] || hp[4] != hp[5])
+        return fail(ctx, PARGO_ERR_CYCLE, "%s: %llu of %llu valid cells and %llu of %llu tile exits completed (cycle)",
+                    what, hp[0], hp[1], hp[5], hp[4]);
+    return PARGO_OK;
+}
+
 pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, pargo_raster* slope,
                                   pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr,
                                   const pargo_fill_opts* opts, int slope_method, int slope_units, int sca_contract,
@@ -949,15 +982,6 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
         CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s));
     }
     if (sca) {
-        const int64_t n = p.rows * p.cols;
-        cudaError_t e;
-        ScaScratch sc{};
-        sc.indeg = (int32_t*)slot(ctx, kSlotScaIndeg, (size_t)n * 4, &e);
-        sc.conv = (unsigned long long*)slot(ctx, kSlotScaConv, (size_t)n * 8, &e);
-        sc.ship = (unsigned long long*)slot(ctx, kSlotScaShip, (size_t)n * 8, &e);
-        sc.flags = (uint8_t*)slot(ctx, kSlotScaFlags, (size_t)((n + 3) / 4 * 4), &e);
-        sc.counters = (unsigned long long*)slot(ctx, kSlotScaCounters, 8 * sizeof(unsigned long long), &e);
-        if (!sc.indeg || !sc.conv || !sc.ship || !sc.flags || !sc.counters) return cuda_fail(ctx, e, "sca scratch");
         ScaParams q{};
         q.rows = p.rows;
         q.cols = p.cols;
@@ -965,8 +989,7 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
         q.nodata = codes.nodata;
         q.out = sa.out;
         q.shipped = sca_contract == PARGO_SCA_SHIPPED;
-        cudaError_t ee = sca_run(q, sc, s);
-        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "pipeline sca");
+        if ((st = sca_launch(ctx, q, s, "pipeline sca")) != PARGO_OK) return st;
     }
     (void)codes_internal;
     if (wdem && (st = unstage_out(ctx, sw, s)) != PARGO_OK) return st;
@@ -979,13 +1002,12 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
     CU(ctx, cudaMemcpyAsync(hp, &ctx->d_counters[3], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     if (sca) {
         unsigned long long* sc = (unsigned long long*)ctx->slots[kSlotScaCounters].p;
-        CU(ctx, cudaMemcpyAsync(hp + 1, sc, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        CU(ctx, cudaMemcpyAsync(hp + 1, sc, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     }
     if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
     local.raised_cells = wdem ? (int64_t)hp[0] : -1;
     if (stats) *stats = local;
-    if (sca && hp[1] != hp[2])
-        return fail(ctx, PARGO_ERR_CYCLE, "pipeline sca: %llu of %llu valid cells completed", hp[1], hp[2]);
+    if (sca) return sca_check(ctx, hp + 1, "pipeline sca");
     return PARGO_OK;
 }
 
@@ -1009,19 +1031,7 @@ pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca
     Staged sd8, so;
     if ((st = stage_in(ctx, d8, kSlotIn0, s, &sd8)) != PARGO_OK) return st;
     if ((st = stage_out(ctx, sca, kSlotOut0, &so)) != PARGO_OK) return st;
-    const int64_t n = d8->rows * d8->cols;
     cudaError_t e;
-    ScaScratch sc{};
-    sc.indeg = (int32_t*)slot(ctx, kSlotScaIndeg, (size_t)n * 4, &e);
-    if (!sc.indeg) return cuda_fail(ctx, e, "sca in-degrees");
-    sc.conv = (unsigned long long*)slot(ctx, kSlotScaConv, (size_t)n * 8, &e);
-    if (!sc.conv) return cuda_fail(ctx, e, "sca totals");
-    sc.ship = (unsigned long long*)slot(ctx, kSlotScaShip, (size_t)n * 8, &e);
-    if (!sc.ship) return cuda_fail(ctx, e, "sca pulled totals");
-    sc.flags = (uint8_t*)slot(ctx, kSlotScaFlags, (size_t)((n + 3) / 4 * 4), &e);
-    if (!sc.flags) return cuda_fail(ctx, e, "sca flags");
-    sc.counters = (unsigned long long*)slot(ctx, kSlotScaCounters, 8 * sizeof(unsigned long long), &e);
-    if (!sc.counters) return cuda_fail(ctx, e, "sca counters");
     ScaParams p{};
     p.rows = d8->rows;
     p.cols = d8->cols;
@@ -1029,19 +1039,14 @@ pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca
     p.nodata = d8->nodata;
     p.out = so.out;
     p.shipped = contract == PARGO_SCA_SHIPPED;
-    {
-        cudaError_t ee = sca_run(p, sc, s);
-        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "sca");
-    }
+    if ((st = sca_launch(ctx, p, s, "sca")) != PARGO_OK) return st;
     if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
     unsigned long long* hp = (unsigned long long*)pinned(ctx, 64, &e);
     if (!hp) return cuda_fail(ctx, e, "pinned counters");
-    CU(ctx, cudaMemcpyAsync(hp, sc.counters, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CU(ctx, cudaMemcpyAsync(hp, ctx->slots[kSlotScaCounters].p, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            s));
     if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
-    if (hp[0] != hp[1])
-        return fail(ctx, PARGO_ERR_CYCLE, "sca: %llu of %llu valid cells completed (cycle or inflow from the ring)",
-                    hp[0], hp[1]);
-    return PARGO_OK;
+    return sca_check(ctx, hp, "sca");
 }
 
 // ------------------------------------------------------------------ batch --

@@ -121,6 +121,29 @@ struct ScaScratch {
 };
 cudaError_t sca_run(const ScaParams& p, const ScaScratch& s, cudaStream_t st);
 
+// Tiled SCA (sca_tiled.cu): per 64 x 64 tile, tree sums in shared memory;
+// across tiles, a forest of tile exits.  Node = tile * 256 + border slot.
+struct ScaTiles {
+    int64_t tiles_x, tiles_y;
+    int32_t* exit_of;   // border cell -> exit node its in-tile path reaches (-1: ends in the tile)
+    int32_t* yslot;     // exit node -> entry node its flow enters (-1: not an exit)
+    int32_t* xpar;      // exit node -> exit-forest parent (-1: root)
+    int32_t* xdeg;      // exit-forest in-degree
+    unsigned long long* tot;   // exit: own in-tile total, then the total through it
+    unsigned long long* tin;   // entry: external inflow total
+    uint32_t* totb;     // the same for the "some inflow not pulled" flag
+    uint32_t* tinb;
+};
+constexpr int kScaTile = 64;
+constexpr int kScaSlots = 256;
+size_t sca_tiles_bytes(int64_t rows, int64_t cols);  // node arrays for a raster
+ScaTiles sca_tiles_layout(void* base, int64_t rows, int64_t cols);
+// conv[c] = upslope count incl. c; ship[c] = 1 if some cell of c's subtree has
+// an inflow the single raster-order sweep does not pull, else 0.
+// counters: [0] completed cells, [1] valid cells, [2] last-cell conv, [3]
+// last-cell ship, [4] exits, [5] exits completed, [6] inflows from the ring.
+cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTiles& t, cudaStream_t st);
+
 // grad.cu
 struct GradParams {
     int64_t rows, cols;

@@ -1,0 +1,418 @@
+// sca_tiled.cu -- D8 specific catchment area as subtree sums over the flow
+// forest, tiled so that the long serial chains stay in shared memory.
+//
+// Reference: SCAOperator::Operator (apps/hydrology/scad8/scaOperator.cpp:37-131).
+// Flow forest: the parent of a valid work cell c is the cell its code names,
+// when that cell is a valid work cell that does not name c back (a mutual
+// pair is no inflow, :71).  Converged SCA = subtree size (counts are integers:
+// exact in any summation order).  The shipped single raster-order sweep pulls
+// the inflow p -> c when p is a source or p precedes c and p is "done"; p is
+// done exactly when no cell u of p's subtree has a non-source inflow q that
+// follows u in raster order ("bad" cells), so done is an OR over the subtree
+// -- a second subtree reduction -- and shipped(c) = 1 + the pulled children's
+// subtree sizes, gathered in the output pass.
+//
+// Phases (one launch each):
+//  1. per 64 x 64 tile (codes with a 2-cell halo in shared memory): the in-tile
+//     forest, its subtree sums by a shared-memory topological walk (in-degree
+//     counters; the last contributor continues), and for every border cell the
+//     exit its in-tile path reaches.  Exits (cells whose parent lies in another
+//     tile) record their in-tile sum and the entry cell they feed.
+//  2. the exit forest: exit x's parent is the exit reached from the entry x
+//     feeds; its in-degrees.
+//  3. subtree sums over the exit forest (its leaves marked first, then a
+//     global-memory walk; chains are as long as the tiles a river crosses);
+//     each exit adds its total to the inflow of the entry it feeds.
+//  4. per tile again: the in-tile sums with the entries' inflows added -> the
+//     final counts and flags.
+//  5. output: converged counts, or the shipped sums; the reference's last-cell
+//     quirk (a nodata last work cell accumulates what flows into it).
+// Cycles (inside a tile or across tiles) and inflows from the raster's ring,
+// which the reference never releases, leave cells or exits uncompleted; the
+// host compares the completion counts.
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pargo {
+
+namespace {
+
+constexpr int kT = kScaTile;       // tile side
+constexpr int kH = kT + 4;         // codes with a 2-cell halo
+constexpr int kCells = kT * kT;
+constexpr int kThreads = 256;
+constexpr int8_t kNodata = -1, kNoFlow = -2;
+
+__device__ __forceinline__ int8_t decode8(const ScaParams& p, int64_t r, int64_t c) {
+    if (r < 0 || c < 0 || r >= p.rows || c >= p.cols) return kNodata;
+    const char* row = p.d8.base + r * p.d8.pitch;
+    double v;
+    switch (p.d8.dtype) {
+        case PARGO_F64: v = reinterpret_cast<const double*>(row)[c]; break;
+        case PARGO_F32: v = (double)reinterpret_cast<const float*>(row)[c]; break;
+        case PARGO_I8: v = (double)reinterpret_cast<const int8_t*>(row)[c]; break;
+        case PARGO_I16: v = (double)reinterpret_cast<const int16_t*>(row)[c]; break;
+        default: v = (double)reinterpret_cast<const int32_t*>(row)[c]; break;
+    }
+    const bool nd = (p.d8.dtype == PARGO_F64 || p.d8.dtype == PARGO_F32) ? fabs(v - p.nodata) < kEpsHydro
+                                                                        : v == p.nodata;  // scaOperator.cpp:48
+    if (nd) return kNodata;
+    const int k = (int)v;
+    return ((double)k == v && k >= 0 && k <= 8 && k != 4) ? (int8_t)k : kNoFlow;
+}
+
+__device__ __forceinline__ bool in_work(const ScaParams& p, int64_t r, int64_t c) {
+    return r >= 1 && c >= 1 && r <= p.rows - 2 && c <= p.cols - 2;
+}
+
+// Border slot of tile-local (lr, lc) in a th x tw tile, or -1 inside.
+__device__ __forceinline__ int slot_of(int lr, int lc, int th, int tw) {
+    if (lr == 0) return lc;
+    if (lr == th - 1) return tw + lc;
+    if (lc == 0) return 2 * tw + (lr - 1);
+    if (lc == tw - 1) return 2 * tw + (th - 2) + (lr - 1);
+    return -1;
+}
+
+struct TileSmem {
+    int8_t cd[kH * kH];          // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
+    int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
+    int32_t ldeg[kCells];        // in-tile children not yet folded in
+    unsigned long long acc[kCells];
+    uint32_t accb[kCells];
+    uint8_t lflag[kCells];       // bit0 valid work cell, bit1 bad, bit2 completed, bit3 in-tile leaf
+    unsigned long long cnt[3];   // valid, completed, ring inflows
+};
+
+// Whether the neighbour at (a, b) of the cell at codes position (ca, cb)
+// flows into it: its code names the cell and the cell does not name it back.
+__device__ __forceinline__ bool flows_in(const TileSmem& S, int ca, int cb, int a, int b) {
+    const int k = (a + 1) * 3 + (b + 1);  // window index of the neighbour seen from the cell
+    const int8_t q = S.cd[(ca + a) * kH + (cb + b)];
+    return q == 8 - k && S.cd[ca * kH + cb] != k;
+}
+
+// Reference in-degree of the cell at codes position (ca, cb) is zero.
+__device__ __forceinline__ bool is_source(const TileSmem& S, int ca, int cb) {
+#pragma unroll
+    for (int a = -1; a <= 1; a++)
+#pragma unroll
+        for (int b = -1; b <= 1; b++)
+            if ((a || b) && flows_in(S, ca, cb, a, b)) return false;
+    return true;
+}
+
+template <bool FINAL>
+__global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
+    extern __shared__ __align__(16) unsigned char sca_smem[];
+    TileSmem& S = *reinterpret_cast<TileSmem*>(sca_smem);
+    const int tid = threadIdx.x;
+    const int64_t ntiles = T.tiles_x * T.tiles_y;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int64_t r0 = (t / T.tiles_x) * kT, c0 = (t % T.tiles_x) * kT;
+        const int th = (int)min((int64_t)kT, p.rows - r0), tw = (int)min((int64_t)kT, p.cols - c0);
+        if (tid < 3) S.cnt[tid] = 0;
+        if (!FINAL && tid < kScaSlots) {  // every slot starts as "no exit"; the exit forest's accumulators empty
+            const int64_t node = t * kScaSlots + tid;
+            T.exit_of[node] = -1;
+            T.yslot[node] = -1;
+            T.xdeg[node] = 0;
+            T.tin[node] = 0;
+            T.tinb[node] = 0;
+        }
+        for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
+        __syncthreads();
+        // The in-tile forest.
+        unsigned long long nvalid = 0, nring = 0;
+        for (int i = tid; i < kCells; i += kThreads) {
+            const int lr = i / kT, lc = i % kT;
+            const int64_t r = r0 + lr, c = c0 + lc;
+            const int ca = lr + 2, cb = lc + 2;
+            int16_t lp = -1;
+            int deg = 0;
+            uint8_t f = 0;
+            if (lr < th && lc < tw && in_work(p, r, c) && S.cd[ca * kH + cb] != kNodata) {
+                f = 1;
+                nvalid++;
+                const int8_t k = S.cd[ca * kH + cb];
+                if (k >= 0) {
+                    const int a = k / 3 - 1, b = k % 3 - 1;
+                    const int8_t tk = S.cd[(ca + a) * kH + (cb + b)];
+                    if (in_work(p, r + a, c + b) && tk != kNodata && tk != 8 - k) {
+                        const int tr = lr + a, tc = lc + b;
+                        lp = (tr >= 0 && tc >= 0 && tr < th && tc < tw) ? (int16_t)(tr * kT + tc) : (int16_t)-2;
+                    }
+                }
+                // children: in-tile ones count towards the walk; an inflow from
+                // the ring is never released; a non-source child that follows
+                // the cell in raster order is not pulled by the single sweep.
+#pragma unroll 1
+                for (int a = -1; a <= 1; a++)
+#pragma unroll 1
+                    for (int b = -1; b <= 1; b++) {
+                        if (!(a || b) || !flows_in(S, ca, cb, a, b)) continue;
+                        if (!in_work(p, r + a, c + b)) {
+                            nring++;
+                            continue;
+                        }
+                        const int qr = lr + a, qc = lc + b;
+                        if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
+                        if ((a > 0 || (a == 0 && b > 0)) && !is_source(S, ca + a, cb + b)) f |= 2;
+                    }
+            }
+            S.lpar[i] = lp;
+            S.ldeg[i] = deg;
+            S.lflag[i] = (f && deg == 0) ? (uint8_t)(f | 8) : f;  // leaves fixed before any walk decrements
+            unsigned long long w = 0;
+            uint32_t wb = 0;
+            if (FINAL && f) {
+                const int sl = slot_of(lr, lc, th, tw);
+                if (sl >= 0) {
+                    w = T.tin[t * kScaSlots + sl];
+                    wb = T.tinb[t * kScaSlots + sl];
+                }
+            }
+            S.acc[i] = w;  // external inflow (final pass) plus, later, the in-tile children
+            S.accb[i] = wb;
+        }
+        atomicAdd(&S.cnt[0], nvalid);
+        if (nring) atomicAdd(&S.cnt[2], nring);
+        __syncthreads();
+        // Topological walk from the in-tile leaves.
+        unsigned long long ndone = 0;
+        for (int i = tid; i < kCells; i += kThreads) {
+            if (!(S.lflag[i] & 8)) continue;
+            int cur = i;
+            for (;;) {
+                const unsigned long long tot = 1 + atomicAdd(&S.acc[cur], 0ULL);
+                const uint32_t bad = ((S.lflag[cur] >> 1) & 1) | atomicOr(&S.accb[cur], 0u);
+                S.acc[cur] = tot;
+                S.accb[cur] = bad;
+                S.lflag[cur] |= 4;
+                ndone++;
+                const int par = S.lpar[cur];
+                if (par < 0) break;
+                atomicAdd(&S.acc[par], tot);
+                if (bad) atomicOr(&S.accb[par], 1u);
+                __threadfence_block();
+                if (atomicSub(&S.ldeg[par], 1) != 1) break;
+                __threadfence_block();
+                cur = par;
+            }
+        }
+        atomicAdd(&S.cnt[1], ndone);
+        __syncthreads();
+        if (!FINAL) {
+            // Border cells: the exit each in-tile path reaches; exits record
+            // their in-tile totals and the entry they feed.
+            for (int i = tid; i < kCells; i += kThreads) {
+                const int lr = i / kT, lc = i % kT;
+                if (lr >= th || lc >= tw) continue;
+                const int sl = slot_of(lr, lc, th, tw);
+                if (sl < 0) continue;
+                const int64_t node = t * kScaSlots + sl;
+                int32_t ex = -1, ys = -1;
+                if (S.lflag[i] & 4) {  // completed: its path is acyclic
+                    int cur = i;
+                    for (int step = 0; step < kCells && S.lpar[cur] >= 0; step++) cur = S.lpar[cur];
+                    if (S.lpar[cur] == -2) {
+                        const int er = cur / kT, ec = cur % kT;
+                        ex = (int32_t)(t * kScaSlots + slot_of(er, ec, th, tw));
+                    }
+                    if (S.lpar[i] == -2) {  // this cell is an exit: where its flow enters
+                        const int8_t k = S.cd[(lr + 2) * kH + (lc + 2)];
+                        const int64_t yr = r0 + lr + k / 3 - 1, yc = c0 + lc + k % 3 - 1;
+                        const int64_t yt = (yr / kT) * T.tiles_x + (yc / kT);
+                        const int yth = (int)min((int64_t)kT, p.rows - (yr / kT) * kT);
+                        const int ytw = (int)min((int64_t)kT, p.cols - (yc / kT) * kT);
+                        ys = (int32_t)(yt * kScaSlots + slot_of((int)(yr % kT), (int)(yc % kT), yth, ytw));
+                        T.tot[node] = S.acc[i];
+                        T.totb[node] = S.accb[i];
+                    }
+                }
+                T.exit_of[node] = ex;
+                T.yslot[node] = ys;
+            }
+            if (tid == 0 && S.cnt[2]) atomicAdd(&s.counters[6], S.cnt[2]);
+        } else {
+            for (int i = tid; i < kCells; i += kThreads) {
+                const int lr = i / kT, lc = i % kT;
+                if (lr >= th || lc >= tw) continue;
+                const int64_t g = (r0 + lr) * p.cols + (c0 + lc);
+                const bool ok = (S.lflag[i] & 5) == 5;
+                s.conv[g] = ok ? S.acc[i] : 0ULL;
+                s.ship[g] = ok ? (unsigned long long)S.accb[i] : 0ULL;
+            }
+            if (tid == 0) {
+                atomicAdd(&s.counters[1], S.cnt[0]);
+                atomicAdd(&s.counters[0], S.cnt[1]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Exit forest: parents and in-degrees.
+__global__ void sca_exit_links_kernel(ScaScratch s, ScaTiles T) {
+    const int64_t n = T.tiles_x * T.tiles_y * kScaSlots;
+    unsigned long long nexit = 0;
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t y = T.yslot[x];
+        int32_t px = -1;
+        if (y >= 0) {
+            nexit++;
+            px = T.exit_of[y];
+            if (px >= 0) atomicAdd(&T.xdeg[px], 1);
+        }
+        T.xpar[x] = px;
+    }
+    nexit = __reduce_add_sync(0xffffffffu, (unsigned)nexit);
+    if ((threadIdx.x & 31) == 0 && nexit) atomicAdd(&s.counters[4], nexit);
+}
+
+// Exit forest: mark its leaves (bit 1 of totb) once every in-degree is known,
+// so that the walk below starts from them only.
+__global__ void sca_exit_leaves_kernel(ScaTiles T) {
+    const int64_t n = T.tiles_x * T.tiles_y * kScaSlots;
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+        if (T.yslot[x] >= 0 && T.xdeg[x] == 0) T.totb[x] |= 2u;
+}
+
+// Exit forest: totals by a topological walk from its leaves; each exit feeds
+// its total into the entry it flows into.
+__global__ void sca_exit_walk_kernel(ScaScratch s, ScaTiles T) {
+    const int64_t n = T.tiles_x * T.tiles_y * kScaSlots;
+    unsigned long long ndone = 0;
+    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+        if (T.yslot[x] < 0 || !(T.totb[x] & 2u)) continue;
+        int64_t cur = x;
+        for (;;) {
+            const unsigned long long tot = atomicAdd(&T.tot[cur], 0ULL);
+            const uint32_t bad = atomicOr(&T.totb[cur], 0u) & 1u;
+            const int32_t y = T.yslot[cur];
+            atomicAdd(&T.tin[y], tot);
+            if (bad) atomicOr(&T.tinb[y], 1u);
+            ndone++;
+            const int32_t px = T.xpar[cur];
+            if (px < 0) break;
+            atomicAdd(&T.tot[px], tot);
+            if (bad) atomicOr(&T.totb[px], 1u);
+            __threadfence();
+            if (atomicSub(&T.xdeg[px], 1) != 1) break;
+            __threadfence();
+            cur = px;
+        }
+    }
+    ndone = __reduce_add_sync(0xffffffffu, (unsigned)ndone);
+    if ((threadIdx.x & 31) == 0 && ndone) atomicAdd(&s.counters[5], ndone);
+}
+
+// Output: converged counts, or the shipped sweep's pulled sums.
+__global__ void sca_output_kernel(const ScaParams p, ScaScratch s) {
+    const int64_t n = p.rows * p.cols;
+    const int64_t last = (p.rows - 2) * p.cols + (p.cols - 2);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / p.cols, c = i % p.cols;
+        const bool work = in_work(p, r, c);
+        const int8_t me = work ? decode8(p, r, c) : kNodata;
+        const bool is_last = i == last && p.rows >= 3 && p.cols >= 3;
+        double v = p.out.nodata;
+        if (me != kNodata || is_last) {
+            unsigned long long sum = 0;
+            if (me != kNodata && !p.shipped) {
+                sum = s.conv[i];
+            } else {
+                // children: neighbours whose code names this cell (and, for a
+                // valid cell, that it does not name back)
+                for (int a = -1; a <= 1; a++)
+                    for (int b = -1; b <= 1; b++) {
+                        if (!(a || b)) continue;
+                        const int k = (a + 1) * 3 + (b + 1);
+                        if (!in_work(p, r + a, c + b) || (me != kNodata && me == k)) continue;
+                        if (decode8(p, r + a, c + b) != 8 - k) continue;
+                        const int64_t q = i + a * p.cols + b;
+                        const unsigned long long cq = s.conv[q];
+                        const bool pulled = cq == 1 || (q < i && s.ship[q] == 0);
+                        if (!p.shipped || pulled) sum += cq;
+                    }
+                if (me != kNodata) sum += 1;
+            }
+            v = me != kNodata ? (double)sum : p.out.nodata + (double)sum;
+        }
+        put_value(p.out, r, c, v);
+    }
+}
+
+}  // namespace
+
+size_t sca_tiles_bytes(int64_t rows, int64_t cols) {
+    const int64_t nodes = ((rows + kT - 1) / kT) * ((cols + kT - 1) / kT) * kScaSlots;
+    return (size_t)nodes * (4 * 4 + 2 * 8 + 2 * 4) + 256;
+}
+
+ScaTiles sca_tiles_layout(void* base, int64_t rows, int64_t cols) {
+    ScaTiles T{};
+    T.tiles_y = (rows + kT - 1) / kT;
+    T.tiles_x = (cols + kT - 1) / kT;
+    const int64_t nodes = T.tiles_x * T.tiles_y * kScaSlots;
+    char* b = (char*)(((uintptr_t)base + 15) & ~(uintptr_t)15);
+    T.tot = (unsigned long long*)b;
+    b += nodes * 8;
+    T.tin = (unsigned long long*)b;
+    b += nodes * 8;
+    T.exit_of = (int32_t*)b;
+    b += nodes * 4;
+    T.yslot = (int32_t*)b;
+    b += nodes * 4;
+    T.xpar = (int32_t*)b;
+    b += nodes * 4;
+    T.xdeg = (int32_t*)b;
+    b += nodes * 4;
+    T.totb = (uint32_t*)b;
+    b += nodes * 4;
+    T.tinb = (uint32_t*)b;
+    return T;
+}
+
+cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTiles& T, cudaStream_t st) {
+    const int64_t n = p.rows * p.cols;
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    const size_t smem = sizeof(TileSmem);
+    if ((e = cudaFuncSetAttribute(sca_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(sca_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+        cudaSuccess)
+        return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sca_tile_kernel<false>, kThreads, smem)) !=
+        cudaSuccess)
+        return e;
+    const int64_t ntiles = T.tiles_x * T.tiles_y;
+    int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    if (grid > ntiles) grid = ntiles;
+    sca_tile_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(p, s, T);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const int64_t nodes = ntiles * kScaSlots;
+    int64_t nb = (nodes + 255) / 256;
+    if (nb > 8192) nb = 8192;
+    sca_exit_links_kernel<<<(unsigned)nb, 256, 0, st>>>(s, T);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    sca_exit_leaves_kernel<<<(unsigned)nb, 256, 0, st>>>(T);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    sca_exit_walk_kernel<<<(unsigned)nb, 256, 0, st>>>(s, T);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    sca_tile_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(p, s, T);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    sca_output_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, s);
+    return cudaGetLastError();
+}
+
+}  // namespace pargo

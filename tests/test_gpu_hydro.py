@@ -132,6 +132,39 @@ def test_sca_cycle_is_reported(ctx):
     assert e.value.status_name == "PARGO_ERR_CYCLE"
 
 
+@pytest.mark.parametrize("shape", [(1500, 1700), (130, 4000), (4000, 70)])
+def test_sca_tiles_against_oracle(shape, ctx, oracle_lib):
+    """SCA across many 64 x 64 tiles (rivers crossing tile borders, partial
+    edge tiles, thin rasters), both contracts, against the oracle."""
+    dem = synth.hydro_dem(shape[0], shape[1], seed=17, blob_fraction=0.05)
+    w = oracle_lib.fill(dem, -9999.0, gap=1e-3)
+    d8 = oracle_lib.d8(w, -9999.0)
+    codes = np.where(d8 == -9999.0, -128, d8).astype(np.int8)
+    for contract, shipped in ((abi.SCA_CONVERGED, False), (abi.SCA_SHIPPED, True)):
+        out = empty_dev(shape, np.float64)
+        ctx.sca(abi.raster(dev(codes), -128), abi.raster(out, -9999.0), contract=contract)
+        assert bits_equal(host(out), oracle_lib.sca(d8, -9999.0, shipped=shipped)), contract
+
+
+def test_sca_cycle_across_tiles_and_ring_inflow(ctx):
+    d8 = np.full((130, 130), 6.0)   # every cell drains SW ... into the ring
+    d8[0, :] = d8[-1, :] = d8[:, 0] = d8[:, -1] = -9999.0
+    cyc = d8.copy()
+    # a 4-cycle on the corner of four tiles: (63,63) E, (63,64) S, (64,64) W, (64,63) N
+    cyc[63, 63], cyc[63, 64], cyc[64, 64], cyc[64, 63] = 5, 7, 3, 1
+    out = np.empty(cyc.shape, np.float64)
+    with pytest.raises(abi.PargoError) as e:
+        ctx.sca(abi.raster(cyc, -9999.0), abi.raster(out, -9999.0))
+    assert e.value.status_name == "PARGO_ERR_CYCLE"
+    ring = d8.copy()
+    ring[0, 5] = 7.0   # a ring cell that names a work cell below it
+    with pytest.raises(abi.PargoError) as e:
+        ctx.sca(abi.raster(ring, -9999.0), abi.raster(out, -9999.0))
+    assert e.value.status_name == "PARGO_ERR_CYCLE"
+    ctx.sca(abi.raster(d8, -9999.0), abi.raster(out, -9999.0))   # the context stays usable
+    assert out[1:-1, 1:-1].min() == 1.0
+
+
 def test_full_size_fill_properties(ctx, oracle_lib):
     """8192^2 (the D8 + fill workload): the result is a fixpoint of the
     reference update, no level is below the DEM, and a 2048^2 crop run on its
