@@ -52,6 +52,55 @@ __device__ __forceinline__ void put_value(const OutView& o, int64_t r, int64_t c
     }
 }
 
+// Typed stores that keep float and integer values off the FP64 pipe (a
+// conversion through double costs an FP64 instruction on each side).
+__device__ __forceinline__ void put_float(const OutView& o, int64_t r, int64_t c, float v) {
+    char* p = o.base + r * o.pitch;
+    if (o.dtype == PARGO_F32) reinterpret_cast<float*>(p)[c] = v;
+    else put_value(o, r, c, (double)v);
+}
+__device__ __forceinline__ void put_int(const OutView& o, int64_t r, int64_t c, int v) {
+    char* p = o.base + r * o.pitch;
+    switch (o.dtype) {
+        case PARGO_I8: reinterpret_cast<int8_t*>(p)[c] = (int8_t)v; break;
+        case PARGO_I16: reinterpret_cast<int16_t*>(p)[c] = (int16_t)v; break;
+        case PARGO_I32: reinterpret_cast<int32_t*>(p)[c] = v; break;
+        case PARGO_F32: reinterpret_cast<float*>(p)[c] = (float)v; break;
+        default: put_value(o, r, c, (double)v); break;
+    }
+}
+
+// Double -> float, round to nearest even, on the integer pipes for results
+// in the normal float range (else the hardware conversion).
+__device__ __forceinline__ float dbl2flt_rn(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e < 1 || e > 253) return __double2float_rn(x);
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFULL;
+    const unsigned long long rem = m & 0x1FFFFFFFULL;  // the 29 dropped bits
+    unsigned int f = (unsigned int)(b >> 63) << 31 | (unsigned int)e << 23 | (unsigned int)(m >> 29);
+    f += (rem > 0x10000000ULL || (rem == 0x10000000ULL && (f & 1u))) ? 1u : 0u;  // a carry moves into the exponent
+    return __uint_as_float(f);
+}
+
+// Order-preserving integer keys: a double's, and a float's as the same
+// double's (exact: every float is a double), without a conversion.
+__device__ __forceinline__ long long dkey64(double v) {
+    const long long b = __double_as_longlong(v);
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+__device__ __forceinline__ long long fkey64(float f) {
+    const unsigned int u = __float_as_uint(f);
+    const unsigned int ef = (u >> 23) & 0xFF;
+    long long b;
+    if (ef == 0 || ef == 0xFF) {
+        b = __double_as_longlong((double)f);  // zero, subnormal, inf, NaN: the hardware conversion
+    } else {
+        b = (long long)(u >> 31) << 63 | (long long)(ef - 127 + 1023) << 52 | (long long)(u & 0x7FFFFF) << 29;
+    }
+    return b ^ ((b >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+}
+
 // The set { x : |x - nodata| < eps } as a closed interval of the input type.
 // |(double)x - nodata| is monotone in x, so the set is an interval; the host
 // finds its exact float/double end points (see host_nodata_band in abi.cu).

@@ -317,8 +317,8 @@ __device__ __forceinline__ void compute_tile(const float* s, int64_t y0, int64_t
                 for (int j = 0; j < 4; j++) {
                     const int64_t gx = gx0 + j;
                     if (gx >= p.cols) break;
-                    if (SLOPE) put_value(p.slope, gy, gx, (double)sl[j]);
-                    if (D8) put_value(p.d8, gy, gx, (double)cd[j]);
+                    if (SLOPE) put_float(p.slope, gy, gx, sl[j]);
+                    if (D8) put_int(p.d8, gy, gx, cd[j]);
                 }
             }
         }
@@ -357,8 +357,14 @@ __device__ __forceinline__ void compute_tile(const float* s, int64_t y0, int64_t
             const CellOut o = cell_general<float>(w[0], w[1], w[2], w[kBoxW], w[kBoxW + 1], w[kBoxW + 2], w[2 * kBoxW],
                                                   w[2 * kBoxW + 1], w[2 * kBoxW + 2], &p, ring);
             fell_back += (o.flags >> 2) & 1;
-            if (SLOPE) put_value(p.slope, gy, gx, (o.flags & 1) ? p.slope.nodata : (double)o.slope);
-            if (D8) put_value(p.d8, gy, gx, (o.flags & 2) ? p.d8.nodata : (double)o.code);
+            if (SLOPE) {
+                if (o.flags & 1) put_value(p.slope, gy, gx, p.slope.nodata);
+                else put_float(p.slope, gy, gx, o.slope);
+            }
+            if (D8) {
+                if (o.flags & 2) put_value(p.d8, gy, gx, p.d8.nodata);
+                else put_int(p.d8, gy, gx, o.code);
+            }
         }
     }
 }

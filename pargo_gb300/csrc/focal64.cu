@@ -3,16 +3,16 @@
 // The surface is the pit-removed levels of the hydrology chain: the reference
 // D8 reads the Float64 output of pit removal (pPitRemove.cpp:129 writes it,
 // pD8.cpp:113 reads it), so the codes must come from the float64 levels.
-// Their differences are of order the gap (5e-4 m), so every neighbour
-// difference is formed in FP64 -- once per row, shared by the two cells it
-// joins -- and only then rounded to float for the certified D8 decision
-// (common.cuh: the same bounds hold, r_i = fl64(d4 - d_i) is what the
-// reference computes).  Horn numerators are combined in FP64 too.
-//
+// Their differences are of order the gap (5e-4 m) and must be exact before
+// rounding.  GB300's FP64 rate is a small fraction of its FP32 rate, so the
+// differences are taken on integer keys instead: within one binade a key
+// difference is the exact value difference in ulps.  Windows that span
+// binades or touch nodata fall back to FP64 (cell_general64).
+
 // Layout: CTAs of 4 warps walk 32 x 64-cell tiles; the box (34 x 68 doubles,
 // x starting 2 cells left so x * 8 bytes stays a multiple of 16) is TMA-loaded
 // into a double-buffered stage.  A lane owns 2 columns and walks 8 rows with a
-// rolling three-row window (values kept as doubles, drops as floats).  The
+// rolling three-row window of integer keys.  The
 // kernel can also copy the levels out as the filled-DEM raster (float32 or
 // float64, +inf levels written as that raster's nodata), so the chain reads
 // the levels once.
@@ -53,11 +53,17 @@ __device__ __noinline__ CellOut cell_general64(double z0, double z1, double z2, 
         return o;
     }
     const double z[9] = {z0, z1, z2, z3, z4, z5, z6, z7, z8};
+    // nodata bands as order-preserving integer keys (the same sets; no FP64 compares)
+    const long long k7lo = dkey64(p.nd7d.lo), k7hi = dkey64(p.nd7d.hi);
+    const long long k6lo = dkey64(p.nd6d.lo), k6hi = dkey64(p.nd6d.hi);
+    const bool empty7 = !(p.nd7d.lo <= p.nd7d.hi), empty6 = !(p.nd6d.lo <= p.nd6d.hi);
     bool nd_slope = false, nd_d8 = false;
 #pragma unroll
     for (int q = 0; q < 9; q++) {
-        nd_slope |= p.nd7d.has(z[q]);
-        nd_d8 |= p.nd6d.has(z[q]);
+        const long long k = dkey64(z[q]);
+        const bool nan = (k & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL;
+        nd_slope |= !empty7 && !nan && k >= k7lo && k <= k7hi;
+        nd_d8 |= !empty6 && !nan && k >= k6lo && k <= k6hi;
     }
     if (nd_slope) o.flags |= 1;
     if (nd_d8) o.flags |= 2;
@@ -76,54 +82,80 @@ __device__ __noinline__ CellOut cell_general64(double z0, double z1, double z2, 
     return o;
 }
 
-// Conservative "some value may be nodata" test of a row.  Pipeline levels
-// mark nodata with +inf: any inf/NaN high word.  Otherwise the high 32 bits of
-// the order-preserving key against the band's.
-__device__ __forceinline__ bool row_maybe_nodata64(const double v[4], const Focal64Params& p, int klo, int khi) {
-    bool m = false;
+constexpr int kNoBinade = -1000000;
+
+// Keys of row `ty` (tile-local) for this lane's columns 2l-1 .. 2l+2, and the
+// row's common binade (kNoBinade when the four differ, when one may be nodata,
+// or when the binade's ulp scale does not fit a normal float).  Within one
+// binade (equal key >> 52: sign and exponent) key differences are the exact
+// value differences in units of the binade's ulp, of either sign.
+constexpr long long kInfKey = 0x7FF0000000000000LL;  // key of +inf: the pipeline levels' nodata
+
+__device__ __forceinline__ int load_keys(const double* s, int ty, int lane, long long k[4], const Focal64Params& P,
+                                         int klo, int khi, bool& all_inf) {
+    const double* row = s + (ty + 1) * kBoxW + 2 * lane + 1;  // column 2l-1 sits at box column 2l+1
+    const double2 q = *reinterpret_cast<const double2*>(row + 1);
+    k[0] = dkey64(row[0]);
+    k[1] = dkey64(q.x);
+    k[2] = dkey64(q.y);
+    k[3] = dkey64(row[3]);
+    all_inf = k[0] == kInfKey && k[1] == kInfKey && k[2] == kInfKey && k[3] == kInfKey;
+    const int t = (int)(k[0] >> 52);
+    bool ok = (int)(k[1] >> 52) == t && (int)(k[2] >> 52) == t && (int)(k[3] >> 52) == t;
+    const int e = t >= 0 ? t : -1 - t;  // biased exponent
+    ok = ok && e >= 960 && e <= 1190;   // 2^(1075 - e) and 2^(e - 1075) are normal floats; no inf/NaN
+    if (!P.nodata_is_inf) {
 #pragma unroll
-    for (int a = 0; a < 4; a++) {
-        const int hi = __double2hiint(v[a]);
-        if (p.nodata_is_inf) {
-            m |= (hi & 0x7FFFFFFF) >= 0x7FF00000;
-        } else {
-            const int k = hi ^ ((hi >> 31) & 0x7FFFFFFF);
-            m |= k >= klo && k <= khi;
+        for (int a = 0; a < 4; a++) {
+            const int hi = (int)(k[a] >> 32);
+            ok = ok && !(hi >= klo && hi <= khi);
         }
     }
-    return m;
+    return ok ? t : kNoBinade;
 }
 
-__device__ __forceinline__ void load_row64(const double* s, int ty, int lane, double v[4]) {
-    const double* row = s + (ty + 1) * kBoxW;
-    const double2 q = *reinterpret_cast<const double2*>(row + 2 * lane + 2);
-    double left = __shfl_up_sync(0xffffffffu, q.y, 1);
-    double right = __shfl_down_sync(0xffffffffu, q.x, 1);
-    if (lane == 0) left = row[1];
-    if (lane == 31) right = row[2 * 31 + 4];
-    v[0] = left; v[1] = q.x; v[2] = q.y; v[3] = right;
+// An exact int64 difference (|d| < 2^53) as a float without the 64-bit
+// conversion (an FP64-pipe instruction): the magnitude's two 32-bit halves
+// converted separately and joined by one fma.  Below 2^32 this is the single
+// correct rounding; above, the error is at most 2^-23 |d| (the low half's
+// rounding, 2^8, is below 2^-24 |d|), which keeps the certified D8 bound
+// |x - r| <= 2^-22 |x| with the diagonal's extra roundings.
+__device__ __forceinline__ float i64f(long long d) {
+    const unsigned long long a = (unsigned long long)(d < 0 ? -d : d);
+    const float f = __fmaf_rn(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.0f, __uint2float_rn((unsigned int)a));
+    return d < 0 ? -f : f;
 }
 
 __device__ __forceinline__ void put_copy(const OutView& o, int64_t r, int64_t c, double w) {
-    put_value(o, r, c, isinf(w) ? o.nodata : w);
+    const bool nd = (__double_as_longlong(w) & 0x7FFFFFFFFFFFFFFFLL) == 0x7FF0000000000000LL;  // +-inf, bit test
+    if (o.dtype == PARGO_F32) reinterpret_cast<float*>(o.base + r * o.pitch)[c] = nd ? (float)o.nodata : dbl2flt_rn(w);
+    else put_value(o, r, c, nd ? o.nodata : w);
 }
 
-// same decision as focal.cu's d8_fast (see the bounds there)
-__device__ __forceinline__ int d8_fast64(float x0, float x1, float x2, float x3, float x5, float x6, float x7,
-                                         float x8, int dir_type) {
+// The FP32 fast decision of focal.cu (bounds there) on drops measured in
+// units of the binade's ulp: the 1e-6 thresholds scale by inv_unit, an exact
+// power of two.  Index of a certain single maximum, -1 when the maximum is
+// certainly below 1e-6, else kD8Unsure.
+__device__ __forceinline__ int d8_fast_scaled(float x0, float x1, float x2, float x3, float x5, float x6, float x7,
+                                              float x8, float inv_unit) {
     const float m = fmaxf(fmaxf(fmaxf(x0, x1), fmaxf(x2, x3)), fmaxf(fmaxf(x5, x6), fmaxf(x7, x8)));
-    if (m <= 0.0f) return -1;
-    const float em = m * k2m22;
-    if (m + em < kTLo) return -1;
-    if (!(m - em > kTHi)) return kD8Unsure;
-    const float t = m - (kTHi + m * 1.9073486328125e-06f);
+    const float t = __fadd_rn(__fmaf_rn(m, -1.9073486328125e-06f, m), -kTHi * inv_unit);
     const unsigned mask = (x0 > t ? 1u : 0u) | (x1 > t ? 2u : 0u) | (x2 > t ? 4u : 0u) | (x3 > t ? 8u : 0u) |
                           (x5 > t ? 32u : 0u) | (x6 > t ? 64u : 0u) | (x7 > t ? 128u : 0u) | (x8 > t ? 256u : 0u);
-    if (mask & (mask - 1)) return kD8Unsure;
     const int k = __ffs(mask) - 1;
-    return dir_type == 8 ? k : d8_bit_code(k);
+    const bool single = (mask & (mask - 1)) == 0;
+    return m < 0.99996924e-6f * inv_unit ? -1 : (m > 1.0000329e-6f * inv_unit && single) ? k : kD8Unsure;
 }
 
+// One 32 x 64 tile.  Lane l owns columns 2l, 2l+1 and walks 8 rows with a
+// rolling three-row window of keys.  Rows whose 3 x 4 window shares one
+// binade (and holds no nodata) take the integer path: every neighbour
+// difference is an exact int64 key difference, formed once per row for the
+// two cells it joins and rounded to float in ulp units; the Horn numerators
+// are summed exactly in int64 before rounding.  No FP64 instruction runs on
+// that path.  Other rows (binade crossings, nodata), the ring, other slope
+// methods and uncertain D8 decisions are recomputed afterwards by
+// cell_general64 from the staged doubles.
 __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int64_t x0, const Focal64Params& P,
                                                int klo, int khi, int& fell_back, unsigned long long& raised) {
     const FocalParams& p = P.f;
@@ -131,103 +163,127 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r0 = warp * kRows;
     const int64_t gx0 = x0 + 2 * lane, gy0 = y0 + r0;
-    const bool interior = gy0 >= 1 && gy0 + kRows <= p.rows - 1 && gx0 >= 1 && gx0 + 2 <= p.cols - 1;
-    double va[4], vb[4], vc[4];
-    load_row64(s, r0 - 1, lane, va);
-    load_row64(s, r0, lane, vb);
-    bool nda = row_maybe_nodata64(va, P, klo, khi), ndb = row_maybe_nodata64(vb, P, klo, khi);
-    double shA[2], shB[2];
-    float vN[2], nw[2], ne[2];
+    const bool interior = (p.sk.method == PARGO_SLOPE_FD || !p.do_slope) && gy0 >= 1 && gy0 + kRows <= p.rows - 1 &&
+                          gx0 >= 1 && gx0 + 2 <= p.cols - 1;
+    const float slope_nd = (float)p.slope.nodata;  // nodata outputs, converted once
+    const int d8_nd = (int)p.d8.nodata;
+    long long ka[4], kb[4], kc[4];
+    bool ia, ib, ic;  // rows made only of +inf levels (inside a nodata region of the pipeline)
+    int ta = load_keys(s, r0 - 1, lane, ka, P, klo, khi, ia);
+    int tb = load_keys(s, r0, lane, kb, P, klo, khi, ib);
+    // the previous row's downward drops seen from this row (negated): S, SE (e1), SW (e2) of row a
+    float nS[2], e1p[3], e2p[3];
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-        shA[j] = va[j + 2] - va[j];
-        shB[j] = vb[j + 2] - vb[j];
-        vN[j] = (float)(vb[j + 1] - va[j + 1]);
-        nw[j] = (float)(vb[j + 1] - va[j]) * kinv;
-        ne[j] = (float)(vb[j + 1] - va[j + 2]) * kinv;
+    for (int j = 0; j < 2; j++) nS[j] = i64f(ka[j + 1] - kb[j + 1]);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        e1p[a] = i64f(ka[a] - kb[a + 1]) * kinv;
+        e2p[a] = i64f(ka[a + 1] - kb[a]) * kinv;
     }
+    unsigned redo = 0;
 #pragma unroll 1
     for (int i = 0; i < kRows; i++) {
-        load_row64(s, r0 + i + 1, lane, vc);
-        const bool ndc = row_maybe_nodata64(vc, P, klo, khi);
+        const int tc = load_keys(s, r0 + i + 1, lane, kc, P, klo, khi, ic);
+        const int64_t gy = gy0 + i;
+        const bool fast = interior && ta != kNoBinade && ta == tb && tb == tc;
+        const bool all_nodata = P.nodata_is_inf && ia && ib && ic;  // both windows are nodata
+        // drops of row b shared by the cells they join
         float h[3], e1[3], e2[3], vS[2];
-        double shC[2], sv[4];
 #pragma unroll
         for (int a = 0; a < 3; a++) {
-            h[a] = (float)(vb[a + 1] - vb[a]);
-            e1[a] = (float)(vb[a] - vc[a + 1]) * kinv;
-            e2[a] = (float)(vb[a + 1] - vc[a]) * kinv;
+            h[a] = i64f(kb[a + 1] - kb[a]);
+            e1[a] = i64f(kb[a] - kc[a + 1]) * kinv;
+            e2[a] = i64f(kb[a + 1] - kc[a]) * kinv;
         }
 #pragma unroll
-        for (int j = 0; j < 2; j++) {
-            shC[j] = vc[j + 2] - vc[j];
-            vS[j] = (float)(vb[j + 1] - vc[j + 1]);
-        }
+        for (int j = 0; j < 2; j++) vS[j] = i64f(kb[j + 1] - kc[j + 1]);
+        float sl[2] = {0.0f, 0.0f};
+        int cd[2] = {0, 0};
+        if (fast) {
+            const int e = ta >= 0 ? ta : -1 - ta;
+            const float unit = __int_as_float((127 + e - 1075) << 23);     // the binade's ulp
+            const float inv_unit = __int_as_float((127 + 1075 - e) << 23);
 #pragma unroll
-        for (int a = 0; a < 4; a++) sv[a] = va[a] - vc[a];
-        const bool slow_row = p.sk.method != PARGO_SLOPE_FD || nda || ndb || ndc || !interior;
-        const int64_t gy = gy0 + i;
-        float sl[2];
-        int cd[2], fl[2];
-#pragma unroll
-        for (int j = 0; j < 2; j++) {
-            int code = kD8Unsure;
-            float slope = 0.0f;
-            fl[j] = 0;
-            if (!slow_row) {
+            for (int j = 0; j < 2; j++) {
                 if (p.do_slope) {
-                    const double nx = (shA[j] + shC[j]) + 2.0 * shB[j];
-                    const double ny = (sv[j] + sv[j + 2]) + 2.0 * sv[j + 1];
-                    slope = horn_slope((float)nx, (float)ny, p.sk.k_fd);
-                    if (p.sk.degrees) slope = atanf(slope) * 57.29577951308232f;
+                    const long long nx = ((ka[j + 2] - ka[j]) + (kc[j + 2] - kc[j])) + 2 * (kb[j + 2] - kb[j]);
+                    const long long ny = ((ka[j] - kc[j]) + (ka[j + 2] - kc[j + 2])) + 2 * (ka[j + 1] - kc[j + 1]);
+                    sl[j] = horn_slope(i64f(nx) * unit, i64f(ny) * unit, p.sk.k_fd);
+                    if (p.sk.degrees) sl[j] = atanf(sl[j]) * 57.29577951308232f;
                 }
-                code = p.do_d8 ? d8_fast64(nw[j], vN[j], ne[j], h[j], -h[j + 1], e2[j], vS[j], e1[j + 1], p.dir_type)
-                               : 0;
+                if (p.do_d8) {
+                    cd[j] = d8_fast_scaled(-e1p[j], -nS[j], -e2p[j + 1], h[j], -h[j + 1], e2[j], vS[j], e1[j + 1],
+                                           inv_unit);
+                    if (cd[j] != kD8Unsure && p.dir_type != 8 && cd[j] >= 0) cd[j] = d8_bit_code(cd[j]);
+                }
             }
-            if (code == kD8Unsure) {
-                const int64_t gx = gx0 + j;
-                const bool ring = gy <= 0 || gx <= 0 || gy >= p.rows - 1 || gx >= p.cols - 1;
-                const CellOut o = cell_general64(va[j], va[j + 1], va[j + 2], vb[j], vb[j + 1], vb[j + 2], vc[j],
-                                                 vc[j + 1], vc[j + 2], &p, ring);
-                slope = o.slope;
-                code = o.code;
-                fl[j] = o.flags;
-                fell_back += (o.flags >> 2) & 1;
-            }
-            sl[j] = slope;
-            cd[j] = code;
         }
+        const bool rb = !all_nodata && (!fast || cd[0] == kD8Unsure || cd[1] == kD8Unsure);
+        redo |= (rb ? 1u : 0u) << i;
         if (gy < p.rows) {
 #pragma unroll
             for (int j = 0; j < 2; j++) {
                 const int64_t gx = gx0 + j;
                 if (gx >= p.cols) break;
-                if (p.do_slope) put_value(p.slope, gy, gx, (fl[j] & 1) ? p.slope.nodata : (double)sl[j]);
-                if (p.do_d8) put_value(p.d8, gy, gx, (fl[j] & 2) ? p.d8.nodata : (double)cd[j]);
-                if (P.do_copy) put_copy(P.copy, gy, gx, vb[j + 1]);
-                if (P.raised) {
+                if (all_nodata) {
+                    if (p.do_slope) put_float(p.slope, gy, gx, slope_nd);
+                    if (p.do_d8) put_int(p.d8, gy, gx, d8_nd);
+                } else if (!rb) {
+                    if (p.do_slope) put_float(p.slope, gy, gx, sl[j]);
+                    if (p.do_d8) put_int(p.d8, gy, gx, cd[j]);
+                }
+                const double w = s[(r0 + i + 1) * kBoxW + 2 * lane + j + 2];
+                if (P.do_copy) put_copy(P.copy, gy, gx, w);
+                if (P.raised) {  // level above the DEM, compared as order-preserving keys
                     const char* row = reinterpret_cast<const char*>(P.dem) + gy * P.dem_pitch;
-                    const double z = P.dem_f64 ? reinterpret_cast<const double*>(row)[gx]
-                                               : (double)reinterpret_cast<const float*>(row)[gx];
-                    raised += (!isinf(vb[j + 1]) && vb[j + 1] > z) ? 1 : 0;
+                    const long long kz = P.dem_f64 ? dkey64(reinterpret_cast<const double*>(row)[gx])
+                                                   : fkey64(reinterpret_cast<const float*>(row)[gx]);
+                    const long long kw = kb[j + 1];
+                    raised += (kw < 0x7FF0000000000000LL && kw > kz) ? 1 : 0;
                 }
             }
         }
 #pragma unroll
         for (int a = 0; a < 4; a++) {
-            va[a] = vb[a];
-            vb[a] = vc[a];
+            ka[a] = kb[a];
+            kb[a] = kc[a];
         }
 #pragma unroll
-        for (int j = 0; j < 2; j++) {
-            shA[j] = shB[j];
-            shB[j] = shC[j];
-            vN[j] = -vS[j];
-            nw[j] = -e1[j];
-            ne[j] = -e2[j + 1];
+        for (int j = 0; j < 2; j++) nS[j] = vS[j];
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            e1p[a] = e1[a];
+            e2p[a] = e2[a];
         }
-        nda = ndb;
-        ndb = ndc;
+        ta = tb;
+        tb = tc;
+        ia = ib;
+        ib = ic;
+    }
+    // Rows the integer path did not finish: the general FP64 path on the staged window.
+    while (redo) {
+        const int i = __ffs(redo) - 1;
+        redo &= redo - 1;
+        const int64_t gy = gy0 + i;
+        if (gy >= p.rows) break;
+#pragma unroll 1
+        for (int j = 0; j < 2; j++) {
+            const int64_t gx = gx0 + j;
+            if (gx >= p.cols) break;
+            const bool ring = gy <= 0 || gx <= 0 || gy >= p.rows - 1 || gx >= p.cols - 1;
+            const double* w = s + (r0 + i) * kBoxW + 2 * lane + j + 1;  // window's top-left
+            const CellOut o = cell_general64(w[0], w[1], w[2], w[kBoxW], w[kBoxW + 1], w[kBoxW + 2], w[2 * kBoxW],
+                                             w[2 * kBoxW + 1], w[2 * kBoxW + 2], &p, ring);
+            fell_back += (o.flags >> 2) & 1;
+            if (p.do_slope) {
+                if (o.flags & 1) put_value(p.slope, gy, gx, p.slope.nodata);
+                else put_float(p.slope, gy, gx, o.slope);
+            }
+            if (p.do_d8) {
+                if (o.flags & 2) put_value(p.d8, gy, gx, p.d8.nodata);
+                else put_int(p.d8, gy, gx, o.code);
+            }
+        }
     }
 }
 
