@@ -42,6 +42,8 @@ namespace {
 
 constexpr int kT = 32;            // tile side
 constexpr int kH = kT + 2;        // with halo
+constexpr int kLS = kH + 1;       // 35: row stride of the level tile (odd, conflict-free both ways)
+constexpr int kZS = kT + 1;       // 33: row stride of the DEM-key tile
 constexpr int kThreads = 256;     // 4 cells per thread
 constexpr int kLocalCap = 4096;   // relaxation sweeps per visit before the tile re-queues itself
 constexpr int64_t kKeyInf = 0x7FF0000000000000LL;  // key of +inf
@@ -247,7 +249,12 @@ __device__ __forceinline__ void put_tile(const FillScratch& s, int32_t* next, in
 template <bool PERSIST>
 __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p, FillScratch s, int parity,
                                                               long long patience) {
-    __shared__ int64_t lv[kH][kH];
+    // Levels with the halo and the tile's DEM keys, both with odd row strides
+    // (35 and 33 words of 8 bytes): a warp reading row runs or column runs
+    // touches every bank pair equally, so neither mapping conflicts.
+    __shared__ int64_t lv[kH * kLS];
+    __shared__ int64_t zs[kT * kZS];
+    __shared__ uint32_t dirty[kT];  // bit c of word r: cell (r, c) changed during this visit
     __shared__ int32_t claim;
     __shared__ int edges;  // bit 0 top, 1 bottom, 2 left, 3 right, 4 tl, 5 tr, 6 bl, 7 br
     __shared__ bool last_block;
@@ -258,8 +265,6 @@ __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p
     const int32_t ncur = PERSIST ? 0 : *((volatile int32_t*)cur_count);
     const int tid = threadIdx.x;
     if (!PERSIST && blockIdx.x == 0 && tid == 0 && ncur > 0) atomicAdd(s.active, 1ULL);
-    const int lr = tid >> 3;            // local row 0..31
-    const int lc0 = (tid & 7) * 4;      // local cols lc0..lc0+3
 
     for (;;) {
         if (tid == 0) {
@@ -285,73 +290,69 @@ __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p
             const int64_t r = y0 + a, c = x0 + b;
             int64_t k = kKeyInf;
             if (r >= 0 && c >= 0 && r < p.rows && c < p.cols) k = dkey(((volatile double*)p.w)[r * p.w_stride + c]);
-            lv[a][b] = k;
+            lv[a * kLS + b] = k;
         }
+        // DEM keys; kKeyInf where a level never moves (the raster's ring, beyond the raster)
+        for (int i = tid; i < kT * kT; i += kThreads) {
+            const int r = i / kT, c = i % kT;
+            const int64_t gr = y0 + 1 + r, gc = x0 + 1 + c;
+            int64_t z = kKeyInf;
+            if (gr > 0 && gc > 0 && gr < p.rows - 1 && gc < p.cols - 1) z = dkey(dem_at(p, gr, gc));
+            zs[r * kZS + c] = z;
+        }
+        if (tid < kT) dirty[tid] = 0u;
         __syncthreads();
-        // This thread's cells: row lr, cols lc0..lc0+3 of the tile interior.
-        int64_t zk[4], orig[4];
-        bool act[4];
-        const int64_t gr = y0 + 1 + lr;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int64_t gc = x0 + 1 + lc0 + j;
-            orig[j] = lv[lr + 1][lc0 + 1 + j];
-            act[j] = false;
-            zk[j] = 0;
-            if (gr < p.rows - 1 && gc < p.cols - 1 && gr > 0 && gc > 0) {
-                zk[j] = dkey(dem_at(p, gr, gc));
-                act[j] = orig[j] < kKeyInf && orig[j] > zk[j];
-            }
-        }
+        // Local relaxation until a whole pass changes nothing.  Passes alternate
+        // between row runs and column runs (a thread owns 4 consecutive cells of
+        // one row, then of one column), and every second pair of passes walks
+        // its run backwards, so a front crosses 4 cells per pass in each of the
+        // four directions; within a run the update is in place (Gauss-Seidel).
         int it = 0;
+        const int u = tid >> 3, v0 = (tid & 7) * 4;
         for (;;) {
+            const bool colrun = it & 1, rev = (it >> 1) & 1;
             int changed = 0;
 #pragma unroll
             for (int jj = 0; jj < 4; jj++) {
-                const int j = (it & 1) ? 3 - jj : jj;
-                if (!act[j]) continue;
-                const int a = lr + 1, b = lc0 + 1 + j;
-                int64_t m = lv[a - 1][b - 1];
-                m = min(m, lv[a - 1][b]);
-                m = min(m, lv[a - 1][b + 1]);
-                m = min(m, lv[a][b - 1]);
-                m = min(m, lv[a][b + 1]);
-                m = min(m, lv[a + 1][b - 1]);
-                m = min(m, lv[a + 1][b]);
-                m = min(m, lv[a + 1][b + 1]);
+                const int j = rev ? 3 - jj : jj;
+                const int r = colrun ? v0 + j : u, c = colrun ? u : v0 + j;
+                const int64_t z = zs[r * kZS + c];
+                const int64_t* w0 = lv + r * kLS + c;  // (a-1, b-1) of halo cell (a, b) = (r+1, c+1)
+                const int64_t cur_v = w0[kLS + 1];
+                if (!(cur_v > z && cur_v < kKeyInf)) continue;  // at its DEM, nodata, or never moves
+                int64_t m = min(min(w0[0], w0[1]), w0[2]);
+                m = min(m, min(w0[kLS], w0[kLS + 2]));
+                m = min(m, min(min(w0[2 * kLS], w0[2 * kLS + 1]), w0[2 * kLS + 2]));
                 const int64_t up = add_gap(m, p.gap);
-                const int64_t cur_v = lv[a][b];
-                int64_t nv = cur_v;
-                if (up <= zk[j]) {
-                    nv = zk[j];
-                    act[j] = false;
-                } else if (up < cur_v) {
-                    nv = up;
-                }
+                const int64_t nv = up <= z ? z : (up < cur_v ? up : cur_v);
                 if (nv != cur_v) {
-                    lv[a][b] = nv;
+                    lv[(r + 1) * kLS + c + 1] = nv;
                     changed = 1;
+                    atomicOr(&dirty[r], 1u << c);
                 }
             }
             it++;
             if (!__syncthreads_or(changed) || it >= kLocalCap) break;
         }
-        // Write back and note which borders moved.
+        // Write back the changed cells (row mapping) and note which borders moved.
         int e = 0;
+        {
+            const int r = u;
+            const uint32_t d = dirty[r];
+            const int64_t gr = y0 + 1 + r;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int a = lr + 1, b = lc0 + 1 + j;
-            const int64_t v = lv[a][b];
-            if (v != orig[j]) {
-                p.w[gr * p.w_stride + (x0 + b)] = dval(v);
-                if (lr == 0) e |= 1;
-                if (lr == kT - 1) e |= 2;
-                if (b == 1) e |= 4;
-                if (b == kT) e |= 8;
-                if (lr == 0 && b == 1) e |= 16;
-                if (lr == 0 && b == kT) e |= 32;
-                if (lr == kT - 1 && b == 1) e |= 64;
-                if (lr == kT - 1 && b == kT) e |= 128;
+            for (int j = 0; j < 4; j++) {
+                const int c = v0 + j;
+                if (!((d >> c) & 1u)) continue;
+                p.w[gr * p.w_stride + (x0 + 1 + c)] = dval(lv[(r + 1) * kLS + c + 1]);
+                if (r == 0) e |= 1;
+                if (r == kT - 1) e |= 2;
+                if (c == 0) e |= 4;
+                if (c == kT - 1) e |= 8;
+                if (r == 0 && c == 0) e |= 16;
+                if (r == 0 && c == kT - 1) e |= 32;
+                if (r == kT - 1 && c == 0) e |= 64;
+                if (r == kT - 1 && c == kT - 1) e |= 128;
             }
         }
         const int any = __syncthreads_or(e != 0);
