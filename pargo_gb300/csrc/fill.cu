@@ -255,6 +255,7 @@ __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p
     __shared__ int64_t lv[kH * kLS];
     __shared__ int64_t zs[kT * kZS];
     __shared__ uint32_t dirty[kT];  // bit c of word r: cell (r, c) changed during this visit
+    __shared__ uint32_t stale[kT];  // bit c of word r: a neighbour of (r, c) changed since (r, c) was last relaxed
     __shared__ int32_t claim;
     __shared__ int edges;  // bit 0 top, 1 bottom, 2 left, 3 right, 4 tl, 5 tr, 6 bl, 7 br
     __shared__ bool last_block;
@@ -300,9 +301,14 @@ __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p
             if (gr > 0 && gc > 0 && gr < p.rows - 1 && gc < p.cols - 1) z = dkey(dem_at(p, gr, gc));
             zs[r * kZS + c] = z;
         }
-        if (tid < kT) dirty[tid] = 0u;
+        if (tid < kT) {
+            dirty[tid] = 0u;
+            stale[tid] = 0xFFFFFFFFu;  // the halo is new: every cell is relaxed once
+        }
         __syncthreads();
-        // Local relaxation until a whole pass changes nothing.  Passes alternate
+        // Local relaxation until a whole pass changes nothing; a pass skips the
+        // cells none of whose neighbours moved since they were last relaxed
+        // (the `stale` marks), so only the moving front is recomputed.  Passes alternate
         // between row runs and column runs (a thread owns 4 consecutive cells of
         // one row, then of one column), and every second pair of passes walks
         // its run backwards, so a front crosses 4 cells per pass in each of the
@@ -316,6 +322,13 @@ __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p
             for (int jj = 0; jj < 4; jj++) {
                 const int j = rev ? 3 - jj : jj;
                 const int r = colrun ? v0 + j : u, c = colrun ? u : v0 + j;
+                const uint32_t bit = 1u << c;
+                if (!(stale[r] & bit)) continue;  // no neighbour moved since its last relaxation
+                // Clear the mark before reading the neighbours: a neighbour that
+                // changes after this (its write fenced before it marks this
+                // cell) leaves the cell marked for another relaxation.
+                atomicAnd(&stale[r], ~bit);
+                __threadfence_block();
                 const int64_t z = zs[r * kZS + c];
                 const int64_t* w0 = lv + r * kLS + c;  // (a-1, b-1) of halo cell (a, b) = (r+1, c+1)
                 const int64_t cur_v = w0[kLS + 1];
@@ -328,7 +341,12 @@ __global__ void __launch_bounds__(kThreads) fill_tiles_kernel(const FillParams p
                 if (nv != cur_v) {
                     lv[(r + 1) * kLS + c + 1] = nv;
                     changed = 1;
-                    atomicOr(&dirty[r], 1u << c);
+                    atomicOr(&dirty[r], bit);
+                    __threadfence_block();  // the new level before the marks
+                    const uint32_t nb = (bit | (bit << 1) | (bit >> 1)) & ~0u;  // columns c-1 .. c+1 inside the tile
+                    if (r > 0) atomicOr(&stale[r - 1], nb);
+                    atomicOr(&stale[r], nb & ~bit);
+                    if (r < kT - 1) atomicOr(&stale[r + 1], nb);
                 }
             }
             it++;
