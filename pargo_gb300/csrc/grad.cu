@@ -16,9 +16,11 @@
 //         g(c) = 2 (s - s_ref); writes dL/dz and accumulates L.
 // mode 1: g(c) = gslope(c) given (backward only).
 //
-// One CTA computes a 32 x 32 block of dL/dz: it stages z (and z_ref) with a
-// two-cell halo in shared memory, forms A and B on the 34 x 34 cells around
-// the block, then gathers.
+// One CTA computes a 32 x 64 block of dL/dz: it stages z (and z_ref) with a
+// two-cell halo in shared memory (nodata as NaN), forms A and B on the
+// 34 x 66 cells around the block, then gathers with the stencil's constant
+// coefficients.  The forward uses the slope kernels' pinned rounding
+// (horn_slope), so the fused loss sees the same slopes as pargo_slope_fwd.
 
 #include "common.cuh"
 #include "kernels.h"
@@ -27,89 +29,93 @@ namespace pargo {
 
 namespace {
 
-constexpr int kB = 32;
-constexpr int kZ = kB + 4;  // z with a two-cell halo
-constexpr int kA = kB + 2;  // A, B with a one-cell halo
-
-__constant__ float c_a[9] = {-1.f, 0.f, 1.f, -2.f, 0.f, 2.f, -1.f, 0.f, 1.f};
-__constant__ float c_b[9] = {1.f, 2.f, 1.f, 0.f, 0.f, 0.f, -1.f, -2.f, -1.f};
+constexpr int kBH = 32, kBW = 64;           // dL/dz block of one CTA
+constexpr int kZH = kBH + 4, kZW = kBW + 4;  // z with a two-cell halo
+constexpr int kAH = kBH + 2, kAW = kBW + 2;  // A, B with a one-cell halo
+constexpr int kThreads = 256;
 
 __device__ __forceinline__ float load_f32(const InView& v, int64_t r, int64_t c) {
     return reinterpret_cast<const float*>(v.base + r * v.pitch)[c];
 }
 
-__global__ void __launch_bounds__(256) slope_grad_kernel(const GradParams p, int mode, int64_t nbx) {
-    __shared__ float sz[kZ][kZ + 1];
-    __shared__ float sr[kZ][kZ + 1];
-    __shared__ float sa[kA][kA + 1];
-    __shared__ float sb[kA][kA + 1];
-    __shared__ double red[8];
+// Horn numerators of the window whose top-left is w (row stride ld), in the
+// forward's pinned rounding.  A NaN anywhere among the 8 neighbours (nodata,
+// or outside the raster) makes nx or ny NaN: NaN survives every difference,
+// even two equal markers, so validity is one test on the result.
+__device__ __forceinline__ void numerators(const float* w, int ld, float& nx, float& ny) {
+    const float z0 = w[0], z1 = w[1], z2 = w[2], z3 = w[ld], z5 = w[ld + 2];
+    const float z6 = w[2 * ld], z7 = w[2 * ld + 1], z8 = w[2 * ld + 2];
+    nx = __fmaf_rn(2.0f, __fsub_rn(z5, z3), __fadd_rn(__fsub_rn(z2, z0), __fsub_rn(z8, z6)));
+    ny = __fmaf_rn(2.0f, __fsub_rn(z1, z7), __fadd_rn(__fsub_rn(z0, z6), __fsub_rn(z2, z8)));
+}
+
+__global__ void __launch_bounds__(kThreads) slope_grad_kernel(const GradParams p, int mode, int64_t nbx) {
+    __shared__ float sz[kZH][kZW + 1];
+    __shared__ float sr[kZH][kZW + 1];
+    __shared__ float sa[kAH][kAW + 1];
+    __shared__ float sb[kAH][kAW + 1];
+    __shared__ double red[kThreads / 32];
     const int tid = threadIdx.x;
     const int64_t by = blockIdx.x / nbx, bx = blockIdx.x % nbx;
-    const int64_t y0 = by * kB, x0 = bx * kB;
-    const float NDV = 3.0e38f;  // marks nodata / outside in shared memory
+    const int64_t y0 = by * kBH, x0 = bx * kBW;
+    const float kNaN = __int_as_float(0x7FC00000);
 
-    for (int i = tid; i < kZ * kZ; i += 256) {
-        const int a = i / kZ, b = i % kZ;
-        const int64_t r = y0 - 2 + a, c = x0 - 2 + b;
-        float z = NDV, zr = NDV;
-        if (r >= 0 && c >= 0 && r < p.rows && c < p.cols) {
-            z = load_f32(p.z, r, c);
-            if (p.nd7f.has(z)) z = NDV;
-            if (mode == 0) {
-                zr = load_f32(p.zref, r, c);
-                if (p.nd7f.has(zr)) zr = NDV;
+    // z (and z_ref) with the halo; nodata (Eps 1e-7) and outside as NaN.
+    // All of a thread's loads are issued before the first is used.
+    {
+        constexpr int kPer = (kZH * kZW + kThreads - 1) / kThreads;  // 10
+        float vz[kPer], vr[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int i = tid + q * kThreads;
+            const int a = i / kZW, b = i % kZW;
+            const int64_t r = y0 - 2 + a, c = x0 - 2 + b;
+            const bool in = i < kZH * kZW && r >= 0 && c >= 0 && r < p.rows && c < p.cols;
+            vz[q] = in ? load_f32(p.z, r, c) : kNaN;
+            vr[q] = (in && mode == 0) ? load_f32(p.zref, r, c) : kNaN;
+        }
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int i = tid + q * kThreads;
+            if (i < kZH * kZW) {
+                sz[i / kZW][i % kZW] = p.nd7f.has(vz[q]) ? kNaN : vz[q];
+                sr[i / kZW][i % kZW] = p.nd7f.has(vr[q]) ? kNaN : vr[q];
             }
         }
-        sz[a][b] = z;
-        sr[a][b] = zr;
     }
     __syncthreads();
 
+    // A = g k nx / |n|, B = g k ny / |n| on the block plus a one-cell ring
     float lsum = 0.0f;
-    for (int i = tid; i < kA * kA; i += 256) {
-        const int a = i / kA, b = i % kA;  // cell (y0 - 1 + a, x0 - 1 + b); its window is sz[a..a+2][b..b+2]
+    for (int i = tid; i < kAH * kAW; i += kThreads) {
+        const int a = i / kAW, b = i % kAW;  // cell (y0 - 1 + a, x0 - 1 + b); its window is sz[a..a+2][b..b+2]
         const int64_t r = y0 - 1 + a, c = x0 - 1 + b;
         float A = 0.0f, B = 0.0f;
         const bool inner = r >= 1 && c >= 1 && r <= p.rows - 2 && c <= p.cols - 2;
-        if (inner) {
-            float w[9];
-            bool ok = true;
-#pragma unroll
-            for (int q = 0; q < 9; q++) {
-                w[q] = sz[a + q / 3][b + q % 3];
-                ok &= w[q] != NDV;
+        float nx, ny;
+        numerators(&sz[a][b], kZW + 1, nx, ny);
+        const float q = __fmaf_rn(nx, nx, __fmul_rn(ny, ny));
+        if (inner && sz[a + 1][b + 1] == sz[a + 1][b + 1] && q == q) {  // centre and neighbours valid
+            const float s = horn_slope(nx, ny, p.k_fd);
+            float g = 0.0f;
+            bool have = true;
+            if (mode == 0) {
+                float mx, my;
+                numerators(&sr[a][b], kZW + 1, mx, my);
+                const float sref = horn_slope(mx, my, p.k_fd);
+                have = sr[a + 1][b + 1] == sr[a + 1][b + 1] && sref == sref;
+                if (have) {
+                    const float d = s - sref;
+                    g = 2.0f * d;
+                    if (a >= 1 && b >= 1 && a <= kBH && b <= kBW) lsum += d * d;
+                }
+            } else {
+                g = load_f32(p.gslope, r, c);
             }
-            if (ok) {
-                const float nx = ((w[2] - w[0]) + (w[8] - w[6])) + 2.0f * (w[5] - w[3]);
-                const float ny = ((w[0] - w[6]) + (w[2] - w[8])) + 2.0f * (w[1] - w[7]);
-                const float nn = sqrtf(nx * nx + ny * ny);
-                const float s = nn * p.k_fd;
-                float g = 0.0f;
-                bool have = true;
-                if (mode == 0) {
-                    float v[9];
-#pragma unroll
-                    for (int q = 0; q < 9; q++) {
-                        v[q] = sr[a + q / 3][b + q % 3];
-                        have &= v[q] != NDV;
-                    }
-                    if (have) {
-                        const float mx = ((v[2] - v[0]) + (v[8] - v[6])) + 2.0f * (v[5] - v[3]);
-                        const float my = ((v[0] - v[6]) + (v[2] - v[8])) + 2.0f * (v[1] - v[7]);
-                        const float sref = sqrtf(mx * mx + my * my) * p.k_fd;
-                        const float d = s - sref;
-                        g = 2.0f * d;
-                        if (a >= 1 && b >= 1 && a <= kB && b <= kB) lsum += d * d;
-                    }
-                } else {
-                    g = load_f32(p.gslope, r, c);
-                }
-                if (have && nn > 0.0f) {
-                    const float f = g * p.k_fd / nn;
-                    A = f * nx;
-                    B = f * ny;
-                }
+            if (have && q > 0.0f) {  // subgradient 0 at zero slope
+                const float f = g * p.k_fd * rsqrtf(q);  // g k / |n|
+                A = f * nx;
+                B = f * ny;
             }
         }
         sa[a][b] = A;
@@ -117,18 +123,21 @@ __global__ void __launch_bounds__(256) slope_grad_kernel(const GradParams p, int
     }
     __syncthreads();
 
-    for (int i = tid; i < kB * kB; i += 256) {
-        const int a = i / kB, b = i % kB;
+    // dL/dz(q) = sum over the 3 x 3 cells c around q of A(c) a_j + B(c) b_j,
+    // j = q's position in c's window (a = d nx / d z_j, b = d ny / d z_j).
+    for (int i = tid; i < kBH * kBW; i += kThreads) {
+        const int a = i / kBW, b = i % kBW;
         const int64_t r = y0 + a, c = x0 + b;
         if (r >= p.rows || c >= p.cols) continue;
-        // q = (a+1, b+1) in the A frame; c_j = q - (j/3 - 1, j%3 - 1)
-        float acc = 0.0f;
-#pragma unroll
-        for (int j = 0; j < 9; j++) {
-            const int ca = a + 1 - (j / 3 - 1), cb = b + 1 - (j % 3 - 1);
-            acc += sa[ca][cb] * c_a[j] + sb[ca][cb] * c_b[j];
-        }
-        reinterpret_cast<float*>(reinterpret_cast<char*>(p.gz) + r * p.gz_pitch)[c] = acc;
+        // cell c_j = q - (j/3 - 1, j%3 - 1); in the A frame q sits at (a+1, b+1)
+        const float* A0 = &sa[a][b];  // A of the cell at q + (-1, -1)
+        const float* B0 = &sb[a][b];
+        constexpr int L = kAW + 1;
+        // window position j of q in c_j: c_j = q + (1 - j/3, 1 - j%3)
+        // a_j: -1 0 1 / -2 0 2 / -1 0 1 ; b_j: 1 2 1 / 0 0 0 / -1 -2 -1
+        const float ga = (-A0[2 * L + 2] + A0[2 * L]) + 2.0f * (-A0[L + 2] + A0[L]) + (-A0[2] + A0[0]);
+        const float gb = (B0[2 * L + 2] + 2.0f * B0[2 * L + 1] + B0[2 * L]) - (B0[2] + 2.0f * B0[1] + B0[0]);
+        reinterpret_cast<float*>(reinterpret_cast<char*>(p.gz) + r * p.gz_pitch)[c] = ga + gb;
     }
 
     if (mode == 0 && p.loss) {
@@ -139,7 +148,7 @@ __global__ void __launch_bounds__(256) slope_grad_kernel(const GradParams p, int
         __syncthreads();
         if (tid == 0) {
             double t = 0.0;
-            for (int w = 0; w < 8; w++) t += red[w];
+            for (int w = 0; w < kThreads / 32; w++) t += red[w];
             if (t != 0.0) atomicAdd(p.loss, t);
         }
     }
@@ -148,9 +157,9 @@ __global__ void __launch_bounds__(256) slope_grad_kernel(const GradParams p, int
 }  // namespace
 
 cudaError_t launch_slope_loss_grad(const GradParams& p, int mode, cudaStream_t st) {
-    const int64_t nby = (p.rows + kB - 1) / kB, nbx = (p.cols + kB - 1) / kB;
+    const int64_t nby = (p.rows + kBH - 1) / kBH, nbx = (p.cols + kBW - 1) / kBW;
     if (nby * nbx == 0) return cudaSuccess;
-    slope_grad_kernel<<<(unsigned)(nby * nbx), 256, 0, st>>>(p, mode, nbx);
+    slope_grad_kernel<<<(unsigned)(nby * nbx), kThreads, 0, st>>>(p, mode, nbx);
     return cudaGetLastError();
 }
 
