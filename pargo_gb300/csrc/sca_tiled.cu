@@ -31,6 +31,8 @@
 // which the reference never releases, leave cells or exits uncompleted; the
 // host compares the completion counts.
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -75,26 +77,44 @@ __device__ __forceinline__ int slot_of(int lr, int lc, int th, int tw) {
     return -1;
 }
 
+// Shared state of one tile.  In-degrees (at most 8) and flags are bytes
+// packed four to a word: a walker decrements a degree by an atomic subtract
+// on the word (a byte is at least 1 when decremented, so nothing borrows from
+// its neighbours) and sets flags by atomic OR.  Flag bits: 1 valid work cell,
+// 2 "bad" (a non-source inflow follows it in raster order), 4 completed,
+// 8 in-tile leaf, 16 some cell of its subtree is bad.  In-tile sums fit 32
+// bits in the first pass; the final pass adds inflows from other tiles.
+template <bool FINAL>
 struct TileSmem {
+    using Acc = typename std::conditional<FINAL, unsigned long long, unsigned int>::type;
     int8_t cd[kH * kH];          // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
     int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
-    int32_t ldeg[kCells];        // in-tile children not yet folded in
-    unsigned long long acc[kCells];
-    uint32_t accb[kCells];
-    uint8_t lflag[kCells];       // bit0 valid work cell, bit1 bad, bit2 completed, bit3 in-tile leaf
+    uint32_t degw[kCells / 4];   // in-tile children not yet folded in, a byte per cell
+    Acc acc[kCells];
+    uint32_t flagw[kCells / 4];  // a byte of flags per cell
     unsigned long long cnt[3];   // valid, completed, ring inflows
+    __device__ __forceinline__ unsigned flag(int i) const { return (flagw[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
+    __device__ __forceinline__ unsigned flag_sync(int i) { return (atomicOr(&flagw[i >> 2], 0u) >> (8 * (i & 3))) & 0xFFu; }
+    __device__ __forceinline__ void set_flag(int i, unsigned bits) { atomicOr(&flagw[i >> 2], bits << (8 * (i & 3))); }
+    // true when this call folded in the last child
+    __device__ __forceinline__ bool dec_degree(int i) {
+        const unsigned sh = 8 * (i & 3);
+        return ((atomicSub(&degw[i >> 2], 1u << sh) >> sh) & 0xFFu) == 1u;
+    }
 };
 
 // Whether the neighbour at (a, b) of the cell at codes position (ca, cb)
 // flows into it: its code names the cell and the cell does not name it back.
-__device__ __forceinline__ bool flows_in(const TileSmem& S, int ca, int cb, int a, int b) {
+template <class S_t>
+__device__ __forceinline__ bool flows_in(const S_t& S, int ca, int cb, int a, int b) {
     const int k = (a + 1) * 3 + (b + 1);  // window index of the neighbour seen from the cell
     const int8_t q = S.cd[(ca + a) * kH + (cb + b)];
     return q == 8 - k && S.cd[ca * kH + cb] != k;
 }
 
 // Reference in-degree of the cell at codes position (ca, cb) is zero.
-__device__ __forceinline__ bool is_source(const TileSmem& S, int ca, int cb) {
+template <class S_t>
+__device__ __forceinline__ bool is_source(const S_t& S, int ca, int cb) {
 #pragma unroll
     for (int a = -1; a <= 1; a++)
 #pragma unroll
@@ -106,7 +126,8 @@ __device__ __forceinline__ bool is_source(const TileSmem& S, int ca, int cb) {
 template <bool FINAL>
 __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
     extern __shared__ __align__(16) unsigned char sca_smem[];
-    TileSmem& S = *reinterpret_cast<TileSmem*>(sca_smem);
+    using Smem = TileSmem<FINAL>;
+    Smem& S = *reinterpret_cast<Smem*>(sca_smem);
     const int tid = threadIdx.x;
     const int64_t ntiles = T.tiles_x * T.tiles_y;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -162,8 +183,8 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                     }
             }
             S.lpar[i] = lp;
-            S.ldeg[i] = deg;
-            S.lflag[i] = (f && deg == 0) ? (uint8_t)(f | 8) : f;  // leaves fixed before any walk decrements
+            reinterpret_cast<uint8_t*>(S.degw)[i] = (uint8_t)deg;
+            reinterpret_cast<uint8_t*>(S.flagw)[i] = (f && deg == 0) ? (uint8_t)(f | 8) : f;  // leaves fixed before any walk
             unsigned long long w = 0;
             uint32_t wb = 0;
             if (FINAL && f) {
@@ -173,8 +194,8 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                     wb = T.tinb[t * kScaSlots + sl];
                 }
             }
-            S.acc[i] = w;  // external inflow (final pass) plus, later, the in-tile children
-            S.accb[i] = wb;
+            S.acc[i] = (typename Smem::Acc)w;  // external inflow (final pass) plus, later, the in-tile children
+            if (wb) reinterpret_cast<uint8_t*>(S.flagw)[i] |= 16;  // an inflow from another tile was not pulled
         }
         atomicAdd(&S.cnt[0], nvalid);
         if (nring) atomicAdd(&S.cnt[2], nring);
@@ -182,21 +203,21 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
         // Topological walk from the in-tile leaves.
         unsigned long long ndone = 0;
         for (int i = tid; i < kCells; i += kThreads) {
-            if (!(S.lflag[i] & 8)) continue;
+            if (!(S.flag(i) & 8)) continue;
             int cur = i;
             for (;;) {
-                const unsigned long long tot = 1 + atomicAdd(&S.acc[cur], 0ULL);
-                const uint32_t bad = ((S.lflag[cur] >> 1) & 1) | atomicOr(&S.accb[cur], 0u);
-                S.acc[cur] = tot;
-                S.accb[cur] = bad;
-                S.lflag[cur] |= 4;
+                const unsigned long long tot = 1 + (unsigned long long)atomicAdd(&S.acc[cur], (typename Smem::Acc)0);
+                const unsigned fl = S.flag_sync(cur);
+                const bool bad = (fl & 2) || (fl & 16);
+                S.acc[cur] = (typename Smem::Acc)tot;
+                S.set_flag(cur, 4u | (bad ? 16u : 0u));
                 ndone++;
                 const int par = S.lpar[cur];
                 if (par < 0) break;
-                atomicAdd(&S.acc[par], tot);
-                if (bad) atomicOr(&S.accb[par], 1u);
+                atomicAdd(&S.acc[par], (typename Smem::Acc)tot);
+                if (bad) S.set_flag(par, 16u);
                 __threadfence_block();
-                if (atomicSub(&S.ldeg[par], 1) != 1) break;
+                if (!S.dec_degree(par)) break;
                 __threadfence_block();
                 cur = par;
             }
@@ -213,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 if (sl < 0) continue;
                 const int64_t node = t * kScaSlots + sl;
                 int32_t ex = -1, ys = -1;
-                if (S.lflag[i] & 4) {  // completed: its path is acyclic
+                if (S.flag(i) & 4) {  // completed: its path is acyclic
                     int cur = i;
                     for (int step = 0; step < kCells && S.lpar[cur] >= 0; step++) cur = S.lpar[cur];
                     if (S.lpar[cur] == -2) {
@@ -228,7 +249,7 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                         const int ytw = (int)min((int64_t)kT, p.cols - (yc / kT) * kT);
                         ys = (int32_t)(yt * kScaSlots + slot_of((int)(yr % kT), (int)(yc % kT), yth, ytw));
                         T.tot[node] = S.acc[i];
-                        T.totb[node] = S.accb[i];
+                        T.totb[node] = (S.flag(i) >> 4) & 1u;
                     }
                 }
                 T.exit_of[node] = ex;
@@ -240,9 +261,10 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 const int lr = i / kT, lc = i % kT;
                 if (lr >= th || lc >= tw) continue;
                 const int64_t g = (r0 + lr) * p.cols + (c0 + lc);
-                const bool ok = (S.lflag[i] & 5) == 5;
-                s.conv[g] = ok ? S.acc[i] : 0ULL;
-                s.ship[g] = ok ? (unsigned long long)S.accb[i] : 0ULL;
+                const unsigned fl = S.flag(i);
+                const bool ok = (fl & 5) == 5;
+                s.conv[g] = ok ? (unsigned long long)S.acc[i] : 0ULL;
+                s.ship[g] = ok ? (unsigned long long)((fl >> 4) & 1u) : 0ULL;
             }
             if (tid == 0) {
                 atomicAdd(&s.counters[1], S.cnt[0]);
@@ -380,23 +402,27 @@ cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTile
     if (n == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(s.counters, 0, 8 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    const size_t smem = sizeof(TileSmem);
-    if ((e = cudaFuncSetAttribute(sca_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+    const size_t smem0 = sizeof(TileSmem<false>), smem1 = sizeof(TileSmem<true>);
+    if ((e = cudaFuncSetAttribute(sca_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem0)) !=
         cudaSuccess)
         return e;
-    if ((e = cudaFuncSetAttribute(sca_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+    if ((e = cudaFuncSetAttribute(sca_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1)) !=
         cudaSuccess)
         return e;
-    int dev = 0, sms = 0, per_sm = 0;
+    int dev = 0, sms = 0, per0 = 0, per1 = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sca_tile_kernel<false>, kThreads, smem)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sca_tile_kernel<false>, kThreads, smem0)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, sca_tile_kernel<true>, kThreads, smem1)) !=
         cudaSuccess)
         return e;
     const int64_t ntiles = T.tiles_x * T.tiles_y;
-    int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
-    if (grid > ntiles) grid = ntiles;
-    sca_tile_kernel<false><<<(unsigned)grid, kThreads, smem, st>>>(p, s, T);
+    int64_t grid0 = (int64_t)sms * (per0 > 0 ? per0 : 1), grid1 = (int64_t)sms * (per1 > 0 ? per1 : 1);
+    if (grid0 > ntiles) grid0 = ntiles;
+    if (grid1 > ntiles) grid1 = ntiles;
+    sca_tile_kernel<false><<<(unsigned)grid0, kThreads, smem0, st>>>(p, s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int64_t nodes = ntiles * kScaSlots;
     int64_t nb = (nodes + 255) / 256;
@@ -407,7 +433,7 @@ cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTile
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sca_exit_walk_kernel<<<(unsigned)nb, 256, 0, st>>>(s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    sca_tile_kernel<true><<<(unsigned)grid, kThreads, smem, st>>>(p, s, T);
+    sca_tile_kernel<true><<<(unsigned)grid1, kThreads, smem1, st>>>(p, s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     int64_t blocks = (n + 255) / 256;
     if (blocks > 8192) blocks = 8192;
