@@ -667,7 +667,8 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     // two worklists (or one ring) of ntiles ids, 8 round counters, 8 queue words (u64)
     int32_t* lists = (int32_t*)slot(ctx, kSlotFillLists, (size_t)(2 * ntiles + 8) * sizeof(int32_t) + 8 * 8 + 8, &e);
     if (!lists) return cuda_fail(ctx, e, "fill worklists");
-    int32_t* queued = (int32_t*)slot(ctx, kSlotFillQueued, (size_t)ntiles * sizeof(int32_t), &e);
+    // per tile: its state word, then 5 words of changed halo cells
+    int32_t* queued = (int32_t*)slot(ctx, kSlotFillQueued, (size_t)ntiles * 6 * sizeof(int32_t), &e);
     if (!queued) return cuda_fail(ctx, e, "fill queue flags");
     FillScratch sc{};
     sc.list_a = lists;
@@ -680,6 +681,7 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     sc.iters = &ctx->d_counters[5];
     sc.ring = lists;
     sc.ring_cap = 2 * ntiles;
+    sc.halo_chg = (uint32_t*)(queued + ntiles);
     sc.q = (unsigned long long*)(((uintptr_t)(lists + 2 * ntiles + 8) + 7) & ~(uintptr_t)7);
     const char* force_rounds = getenv("PARGO_FILL_ROUNDS");
     const bool persistent = o.max_rounds <= 0 && !(force_rounds && force_rounds[0] == '1');

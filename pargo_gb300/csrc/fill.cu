@@ -44,12 +44,15 @@ constexpr int kT = 32;            // tile side
 constexpr int kH = kT + 2;        // with halo
 constexpr int kLS = kH + 1;       // 35: row stride of the level tile (odd, conflict-free both ways)
 constexpr int kZS = kT + 1;       // 33: row stride of the DEM-key tile
-constexpr int kThreads = 256;     // 4 cells per thread
+constexpr int kThreads = 256;     // threads per tile
+constexpr int kRun = kT * kT / kThreads;  // 4: cells of a thread's run (a row run, then a column run)
+constexpr int kRunsPerLine = kT / kRun;   // 8
 constexpr int kLocalCap = 4096;   // relaxation sweeps per visit before the tile re-queues itself
 constexpr int64_t kKeyInf = 0x7FF0000000000000LL;  // key of +inf
 // FillScratch::q slots of the persistent form
 constexpr int kQHead = 0, kQTail = 1, kQPending = 2, kQProgress = 3, kQError = 4;
 constexpr int kQErrPop = 1, kQErrPush = 2, kQErrState = 3;
+constexpr uint32_t kHaloAll = 0x80000000u;  // halo_chg corner-word flag: relax every cell of the tile
 
 // Per biased exponent e: fl64(x + gap) - x in ulps of x's binade when that
 // is the same for every x of the binade, else -1 (subnormals, inf/nan, a sum
@@ -114,6 +117,9 @@ __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
         s.list_a[t] = (int32_t)t;  // also ring positions 0 .. ntiles-1
         s.list_b[t] = -1;          // the ring's empty second half
         s.queued[t] = 1;
+#pragma unroll
+        for (int k = 0; k < 4; k++) s.halo_chg[t * 5 + k] = 0u;
+        s.halo_chg[t * 5 + 4] = kHaloAll;  // first visit: relax every cell
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         s.counts[0] = (int32_t)ntiles;
@@ -230,6 +236,14 @@ __device__ void finish_tile(const FillScratch& s, int32_t t, bool again, long lo
     }
 }
 
+// Record, in tile (ty, tx)'s halo-change words, cells of its halo that this
+// visit changed (word k, bits); ignored outside the raster's tiles.
+__device__ __forceinline__ void mark_halo(const FillScratch& s, const FillParams& p, int64_t ty, int64_t tx, int k,
+                                          uint32_t bits) {
+    if (ty < 0 || tx < 0 || ty >= p.tiles_y || tx >= p.tiles_x || !bits) return;
+    atomicOr(&s.halo_chg[(ty * p.tiles_x + tx) * 5 + k], bits);
+}
+
 template <bool PERSIST>
 __device__ __forceinline__ void put_tile(const FillScratch& s, int32_t* next, int32_t* next_count, int64_t ty, int64_t tx,
                                          const FillParams& p, long long patience) {
@@ -248,7 +262,9 @@ __device__ __forceinline__ void put_tile(const FillScratch& s, int32_t* next, in
 // in one launch over the ring.
 // 8 CTAs of 256 threads per SM (full warp occupancy, 32 registers): the
 // visits are latency bound, and occupancy measured worth more than the few
-// registers spilled at this bound (8192^2: 25.0 -> 22.8 ms).
+// registers spilled at this bound (8192^2: 25.0 -> 22.8 ms).  Runs of 8 cells
+// (128 threads, 12 CTAs per SM) took fewer passes but more visits and more
+// time (25.6 ms against 21.5).
 template <bool PERSIST>
 __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParams p, FillScratch s, int parity,
                                                               long long patience) {
@@ -259,6 +275,8 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
     __shared__ int64_t zs[kT * kZS];
     __shared__ uint32_t dirty[kT];  // bit c of word r: cell (r, c) changed during this visit
     __shared__ uint32_t stale[kT];  // bit c of word r: a neighbour of (r, c) changed since (r, c) was last relaxed
+    __shared__ uint32_t hmask[5];   // this visit's halo-change words
+    __shared__ uint32_t colmask[2]; // changed cells of tile column 0 and 31 (bit = row)
     __shared__ int32_t claim;
     __shared__ int edges;  // bit 0 top, 1 bottom, 2 left, 3 right, 4 tl, 5 tr, 6 bl, 7 br
     __shared__ bool last_block;
@@ -269,6 +287,7 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
     const int32_t ncur = PERSIST ? 0 : *((volatile int32_t*)cur_count);
     const int tid = threadIdx.x;
     if (!PERSIST && blockIdx.x == 0 && tid == 0 && ncur > 0) atomicAdd(s.active, 1ULL);
+    unsigned long long st_visits = 0, st_iters = 0, st_changed = 0;  // thread 0's tallies
 
     for (;;) {
         if (tid == 0) {
@@ -279,14 +298,18 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
                 claim = k < ncur ? cur[k] : -1;
             }
             edges = 0;
-            if (claim >= 0) {
-                atomicExch(&s.queued[claim], PERSIST ? kRunning : 0);
-                __threadfence();
-            }
+            if (claim >= 0) atomicExch(&s.queued[claim], PERSIST ? kRunning : 0);
         }
         __syncthreads();
         const int32_t t = claim;
         if (t < 0) break;
+        // Take the halo changes (one word per thread of five) before the halo
+        // is read: a change recorded after this is followed by another request.
+        if (tid < 5) {
+            hmask[tid] = atomicExch(&s.halo_chg[(int64_t)t * 5 + tid], 0u);
+            __threadfence();
+        }
+        __syncthreads();
         const int64_t ty = t / p.tiles_x, tx = t % p.tiles_x;
         const int64_t y0 = ty * kT - 1, x0 = tx * kT - 1;  // global coords of lv[0][0]
         for (int i = tid; i < kH * kH; i += kThreads) {
@@ -305,9 +328,24 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
             zs[r * kZS + c] = z;
         }
         if (tid < kT) {
+            // Cells next to a halo cell that changed since the last visit (or
+            // every cell on a first visit): between visits only the halo moves,
+            // and the last visit left the tile stable against the halo it read.
             dirty[tid] = 0u;
-            stale[tid] = 0xFFFFFFFFu;  // the halo is new: every cell is relaxed once
+            uint32_t st;
+            if (hmask[4] & kHaloAll) {
+                st = 0xFFFFFFFFu;
+            } else {
+                const uint32_t L = hmask[2] | (hmask[2] << 1) | (hmask[2] >> 1);
+                const uint32_t Rr = hmask[3] | (hmask[3] << 1) | (hmask[3] >> 1);
+                st = ((L >> tid) & 1u) | (((Rr >> tid) & 1u) << 31);
+                if (tid == 0) st |= hmask[0] | (hmask[0] << 1) | (hmask[0] >> 1) | (hmask[4] & 1u) | (((hmask[4] >> 1) & 1u) << 31);
+                if (tid == kT - 1)
+                    st |= hmask[1] | (hmask[1] << 1) | (hmask[1] >> 1) | ((hmask[4] >> 2) & 1u) | (((hmask[4] >> 3) & 1u) << 31);
+            }
+            stale[tid] = st;
         }
+        if (tid < 2) colmask[tid] = 0u;
         __syncthreads();
         // Local relaxation until a whole pass changes nothing; a pass skips the
         // cells none of whose neighbours moved since they were last relaxed
@@ -317,13 +355,13 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
         // its run backwards, so a front crosses 4 cells per pass in each of the
         // four directions; within a run the update is in place (Gauss-Seidel).
         int it = 0;
-        const int u = tid >> 3, v0 = (tid & 7) * 4;
+        const int u = tid / kRunsPerLine, v0 = (tid % kRunsPerLine) * kRun;
         for (;;) {
             const bool colrun = it & 1, rev = (it >> 1) & 1;
             int changed = 0;
 #pragma unroll
-            for (int jj = 0; jj < 4; jj++) {
-                const int j = rev ? 3 - jj : jj;
+            for (int jj = 0; jj < kRun; jj++) {
+                const int j = rev ? kRun - 1 - jj : jj;
                 const int r = colrun ? v0 + j : u, c = colrun ? u : v0 + j;
                 const uint32_t bit = 1u << c;
                 if (!(stale[r] & bit)) continue;  // no neighbour moved since its last relaxation
@@ -362,7 +400,7 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
             const uint32_t d = dirty[r];
             const int64_t gr = y0 + 1 + r;
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
+            for (int j = 0; j < kRun; j++) {
                 const int c = v0 + j;
                 if (!((d >> c) & 1u)) continue;
                 p.w[gr * p.w_stride + (x0 + 1 + c)] = dval(lv[(r + 1) * kLS + c + 1]);
@@ -374,36 +412,50 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
                 if (r == 0 && c == kT - 1) e |= 32;
                 if (r == kT - 1 && c == 0) e |= 64;
                 if (r == kT - 1 && c == kT - 1) e |= 128;
+                if (c == 0) atomicOr(&colmask[0], 1u << r);
+                if (c == kT - 1) atomicOr(&colmask[1], 1u << r);
             }
         }
         const int any = __syncthreads_or(e != 0);
         if (e) atomicOr(&edges, e);
         __syncthreads();
-        if (tid == 0) {
-            if (any || it >= kLocalCap) __threadfence();  // the writes above before any queueing
-            if (!PERSIST && it >= kLocalCap) put_tile<PERSIST>(s, next, next_count, ty, tx, p, patience);
-            if (any) {
-                const int ed = edges;
-                if (ed & 1) put_tile<PERSIST>(s, next, next_count, ty - 1, tx, p, patience);
-                if (ed & 2) put_tile<PERSIST>(s, next, next_count, ty + 1, tx, p, patience);
-                if (ed & 4) put_tile<PERSIST>(s, next, next_count, ty, tx - 1, p, patience);
-                if (ed & 8) put_tile<PERSIST>(s, next, next_count, ty, tx + 1, p, patience);
-                if (ed & 16) put_tile<PERSIST>(s, next, next_count, ty - 1, tx - 1, p, patience);
-                if (ed & 32) put_tile<PERSIST>(s, next, next_count, ty - 1, tx + 1, p, patience);
-                if (ed & 64) put_tile<PERSIST>(s, next, next_count, ty + 1, tx - 1, p, patience);
-                if (ed & 128) put_tile<PERSIST>(s, next, next_count, ty + 1, tx + 1, p, patience);
-                atomicAdd(s.changed, 1ULL);
+        // Neighbour d (one lane of warp 0 each, in parallel): record which of
+        // its halo cells moved, then queue it.  Every lane fences first, which
+        // orders the whole CTA's writes (seen through the barrier) before its marks.
+        if (tid < 32) {
+            const int ed = edges;
+            if (any || it >= kLocalCap) __threadfence();
+            if (tid < 8 && ((ed >> tid) & 1)) {
+                const int64_t ny = ty + (tid == 0 || tid == 4 || tid == 5 ? -1 : (tid == 1 || tid == 6 || tid == 7 ? 1 : 0));
+                const int64_t nx = tx + (tid == 2 || tid == 4 || tid == 6 ? -1 : (tid == 3 || tid == 5 || tid == 7 ? 1 : 0));
+                const int word = tid == 0 ? 1 : tid == 1 ? 0 : tid == 2 ? 3 : tid == 3 ? 2 : 4;
+                const uint32_t bits = tid == 0 ? dirty[0] : tid == 1 ? dirty[kT - 1] : tid == 2 ? colmask[0]
+                                    : tid == 3 ? colmask[1] : (8u >> (tid - 4));  // corners: BR, BL, TR, TL of the neighbour
+                mark_halo(s, p, ny, nx, word, bits);
+                __threadfence();  // the mark before the request
+                put_tile<PERSIST>(s, next, next_count, ny, nx, p, patience);
             }
-            atomicAdd(s.visits, 1ULL);
-            atomicAdd(s.iters, (unsigned long long)it);
-            if (PERSIST) {
-                finish_tile(s, t, it >= kLocalCap, patience);
-                __threadfence();
-                atomicAdd(&s.q[kQProgress], 1ULL);
-                atomicAdd(&s.q[kQPending], ~0ULL);  // minus one, after the pushes above
+            __syncwarp();
+            if (tid == 0) {
+                if (it >= kLocalCap) mark_halo(s, p, ty, tx, 4, kHaloAll);  // stopped early: relax every cell next time
+                if (!PERSIST && it >= kLocalCap) put_tile<PERSIST>(s, next, next_count, ty, tx, p, patience);
+                st_visits++;
+                st_iters += (unsigned long long)it;
+                st_changed += any ? 1ull : 0ull;
+                if (PERSIST) {
+                    finish_tile(s, t, it >= kLocalCap, patience);
+                    __threadfence();
+                    atomicAdd(&s.q[kQProgress], 1ULL);
+                    atomicAdd(&s.q[kQPending], ~0ULL);  // minus one, after the pushes above (the warp synced)
+                }
             }
         }
         __syncthreads();
+    }
+    if (tid == 0) {  // this CTA's statistics, once
+        if (st_visits) atomicAdd(s.visits, st_visits);
+        if (st_iters) atomicAdd(s.iters, st_iters);
+        if (st_changed) atomicAdd(s.changed, st_changed);
     }
     if (PERSIST) return;
     // The last CTA to finish resets the consumed list and the claim cursor.

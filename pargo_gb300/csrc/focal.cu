@@ -36,7 +36,7 @@ struct Shape {
     static constexpr int kTH = kWarps * ROWS;
     static constexpr int kBoxH = kTH + 2;
     static constexpr int kStageBytes = kBoxW * kBoxH * 4;
-    static constexpr int kStageStride = (kStageBytes + 1023) / 1024 * 1024;
+    static constexpr int kStageStride = (kStageBytes + 127) / 128 * 128;  // TMA needs 128-byte aligned stages
 };
 constexpr long long kWaitBudget = 4000000000LL;  // ~2 s of SM clocks
 
@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(kThreads, MINB) focal_tma_kernel(const __grid_
                                                                 int64_t ntiles) {
     using S = Shape<ROWS>;
     constexpr int kTH = S::kTH, kStageBytes = S::kStageBytes, kStageStride = S::kStageStride;
-    extern __shared__ __align__(1024) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[2];
     const int tid = threadIdx.x;
 
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(kThreads, 5) batch_tma_kernel(const CUtensorMa
                                                              const int64_t* tile_start, const int64_t* ntx_of,
                                                              int count, int64_t total, unsigned long long* claim,
                                                              unsigned long long* fallbacks, int* error_flag) {
-    extern __shared__ __align__(1024) unsigned char smem[];
+    extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int64_t slot_tile[2];
     __shared__ int slot_item[2];
@@ -541,7 +541,7 @@ __global__ void __launch_bounds__(256) batch_generic_kernel(const FocalParams* p
 struct Variant {
     int rows, unroll, minb;
 };
-static const Variant kVariants[] = {{8, 1, 5}, {9, 3, 4}, {6, 3, 5}, {6, 6, 5}, {12, 1, 4}};
+static const Variant kVariants[] = {{8, 1, 5}, {6, 1, 6}, {6, 1, 7}, {4, 1, 8}, {8, 1, 6}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
 int focal_num_variants() { return kNumVariants; }
@@ -576,10 +576,10 @@ template <bool SLOPE, bool D8>
 static cudaError_t launch_variants(const CUtensorMap* map, const FocalParams& p, int variant, int num_sms,
                                    cudaStream_t s) {
     switch (variant) {
-        case 1: return launch_variant<9, 3, 4, SLOPE, D8>(map, p, num_sms, s);
-        case 2: return launch_variant<6, 3, 5, SLOPE, D8>(map, p, num_sms, s);
-        case 3: return launch_variant<6, 6, 5, SLOPE, D8>(map, p, num_sms, s);
-        case 4: return launch_variant<12, 1, 4, SLOPE, D8>(map, p, num_sms, s);
+        case 1: return launch_variant<6, 1, 6, SLOPE, D8>(map, p, num_sms, s);
+        case 2: return launch_variant<6, 1, 7, SLOPE, D8>(map, p, num_sms, s);
+        case 3: return launch_variant<4, 1, 8, SLOPE, D8>(map, p, num_sms, s);
+        case 4: return launch_variant<8, 1, 6, SLOPE, D8>(map, p, num_sms, s);
         default: return launch_variant<8, 1, 5, SLOPE, D8>(map, p, num_sms, s);
     }
 }

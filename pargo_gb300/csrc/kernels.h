@@ -96,6 +96,11 @@ struct FillScratch {
     int32_t* ring;
     int64_t ring_cap;
     unsigned long long* q;
+    // per tile, 5 words: the halo cells that changed since its last visit --
+    // [0] top row, [1] bottom row, [2] left column, [3] right column (bit =
+    // tile column or row), [4] corners (bit 0 TL, 1 TR, 2 BL, 3 BR; bit 31:
+    // relax every cell, set for first visits)
+    uint32_t* halo_chg;
 };
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st);
 cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st);
