@@ -186,6 +186,15 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
 pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr,
                        int contract, void* stream);
 
+/* Topographic wetness index ln(sca / slope), replacing TWIOperator::Run()
+ * (apps/hydrology/twi/TWIOperator.cpp:42-69): a work cell is nodata (the SCA
+ * raster's nodata) when any value of its 3x3 window, in either input, equals
+ * the SCA raster's nodata; slope below 1e-7 counts as 1e-7; ring cells get the
+ * output's nodata.  slope, sca, twi: F32 or F64; computed in FP32 (about 1e-6
+ * relative to the reference's FP64). */
+pargo_status pargo_twi(pargo_ctx* ctx, const pargo_raster* slope, const pargo_raster* sca, pargo_raster* twi,
+                       const pargo_nbr* nbr, void* stream);
+
 /* Batched fused slope + D8 over `count` independent rasters in one persistent
  * launch; slopes / d8s may be NULL (no such output) and all rasters must be on
  * the device. */

@@ -49,6 +49,7 @@ class Oracle:
         lib.orc_fill_pf.argtypes = [_c_f32p, i, i, d, d, d, _c_f64p]
         lib.orc_sca_sweeps.argtypes = [_c_f64p, i, i, d, i, _c_f64p, ctypes.POINTER(ctypes.c_int)]
         lib.orc_sca_topo.argtypes = [_c_f64p, i, i, d, _c_f64p, _c_f64p]
+        lib.orc_twi.argtypes = [_c_f64p, _c_f64p, i, i, d, d, _c_f64p]
         self.lib = lib
 
     @staticmethod
@@ -115,6 +116,18 @@ class Oracle:
         return ship if shipped else conv
 
 
+
+    def twi(self, slope, sca, nodata, out_nodata=None):
+        """Topographic wetness index ln(sca / max(slope, 1e-7)) with the
+        reference's nodata rule (TWIOperator.cpp:42-69), in FP64."""
+        s1 = _c(slope, np.float64)
+        s2 = _c(sca, np.float64)
+        out = np.empty(s1.shape, np.float64)
+        rc = self.lib.orc_twi(_p(s1, _c_f64p), _p(s2, _c_f64p), s1.shape[0], s1.shape[1], nodata,
+                              nodata if out_nodata is None else out_nodata, _p(out, _c_f64p))
+        if rc:
+            raise OracleError("orc_twi rc=%d" % rc)
+        return out
 class Reference:
     """The unmodified reference operators (available where the reference tree is)."""
 
@@ -130,6 +143,7 @@ class Reference:
         lib.ref_d8.argtypes = [cp, vp, i, i, i, d, d, i, i, _c_f64p]
         lib.ref_fill.argtypes = [cp, _c_f32p, i, i, d, d, _c_f64p, ctypes.POINTER(ctypes.c_int)]
         lib.ref_sca.argtypes = [cp, _c_f64p, i, i, d, d, i, _c_f64p, ctypes.POINTER(ctypes.c_int)]
+        lib.ref_twi.argtypes = [cp, _c_f64p, _c_f64p, i, i, d, d, _c_f64p]
         self.lib = lib
         self._nbr = os.path.join(_build.REF_OUT, "moore.nbr")
         with open(self._nbr, "w") as fh:
@@ -177,3 +191,13 @@ class Reference:
         if rc:
             raise OracleError("ref_sca rc=%d" % rc)
         return out, sw.value
+
+    def twi(self, slope, sca, nodata, cellsize=1.0):
+        s1 = _c(slope, np.float64)
+        s2 = _c(sca, np.float64)
+        out = np.empty(s1.shape, np.float64)
+        rc = self.lib.ref_twi(self._nbr.encode(), _p(s1, _c_f64p), _p(s2, _c_f64p), s1.shape[0], s1.shape[1], nodata,
+                              cellsize, _p(out, _c_f64p))
+        if rc:
+            raise OracleError("ref_twi rc=%d" % rc)
+        return out

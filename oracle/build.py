@@ -7,7 +7,7 @@ Two libraries:
   baseline use).
 * ``oracle/_ref/libpargo_ref.so`` -- the UNMODIFIED reference operators,
   compiled from the reference sources where they lie (``gpro/application.cpp``,
-  ``gpro/utility.cpp``, the four ``apps/.../*Operator.cpp``) against the
+  ``gpro/utility.cpp``, the ``apps/.../*Operator.cpp`` of the path) against the
   single-rank ``mpi.h`` and in-memory ``gdal_priv.h`` in ``oracle/ref_shim/``,
   plus ``oracle/ref_driver.cpp``.  Built only where the reference tree exists.
   Nothing is copied out of the reference; only the objects land in
@@ -34,6 +34,7 @@ REF_SOURCES = [
     "apps/hydrology/flowdird8/d8Operator.cpp",
     "apps/hydrology/pitremove/pitRemoveOperator.cpp",
     "apps/hydrology/scad8/scaOperator.cpp",
+    "apps/hydrology/twi/TWIOperator.cpp",
 ]
 REF_INCLUDES = [
     "gpro",
@@ -41,6 +42,7 @@ REF_INCLUDES = [
     "apps/hydrology/flowdird8",
     "apps/hydrology/pitremove",
     "apps/hydrology/scad8",
+    "apps/hydrology/twi",
 ]
 
 

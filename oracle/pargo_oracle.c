@@ -469,3 +469,40 @@ int orc_sca_topo(const double* d8, int rows, int cols, double nodata, double* co
     free(deg); free(q); free(cv); free(sh); free(src); free(notdone);
     return rc;
 }
+
+/* Topographic wetness index, restating TWIOperator::Operator
+ * (apps/hydrology/twi/TWIOperator.cpp:42-69): on work cells (the 3x3 window
+ * inside the raster) the result is nodata when any value of the window, in
+ * the SCA or the slope layer, equals the SCA layer's nodata exactly (:51-55);
+ * otherwise ln(sca / slope) with slope raised to Eps = 1e-7 when below it
+ * (:61-65).  Ring cells keep the output layer's initial value, which
+ * copyLayerInfo(slopeLayer) sets to nodata (pTWI.cpp:66); here out_nodata. */
+int orc_twi(const double* slope, const double* sca, int rows, int cols, double sca_nodata, double out_nodata,
+            double* twi) {
+    if (rows < 0 || cols < 0) return 1;
+    for (int r = 0; r < rows; r++)
+        for (int c = 0; c < cols; c++) {
+            const size_t i = (size_t)r * cols + c;
+            if (r < 1 || c < 1 || r > rows - 2 || c > cols - 2) {
+                twi[i] = out_nodata;
+                continue;
+            }
+            int nd = 0;
+            for (int a = -1; a <= 1 && !nd; a++)
+                for (int b = -1; b <= 1; b++) {
+                    const size_t j = (size_t)(r + a) * cols + (c + b);
+                    if (sca[j] == sca_nodata || slope[j] == sca_nodata) {
+                        nd = 1;
+                        break;
+                    }
+                }
+            if (nd) {
+                twi[i] = sca_nodata;
+                continue;
+            }
+            double s = slope[i];
+            if (s < 0.0000001) s = 0.0000001;
+            twi[i] = log(sca[i] / s);
+        }
+    return 0;
+}

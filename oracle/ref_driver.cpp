@@ -36,6 +36,8 @@
 #undef Eps
 #include "scaOperator.h"
 #undef Eps
+#include "TWIOperator.h"
+#undef Eps
 
 using namespace GPRO;
 
@@ -177,6 +179,30 @@ int ref_sca(const char* nbr, const double* d8, int rows, int cols, double nodata
         if (sweeps) *sweeps = 3;
     }
     copy_out(scaLayer, out, rows, cols);
+    return 0;
+}
+
+/* TWI by the reference TWIOperator from a slope and an SCA raster (both
+ * double, one nodata value), as pTWI.cpp:57-81 runs it. */
+int ref_twi(const char* nbr, const double* slope, const double* sca, int rows, int cols, double nodata,
+            double cellsize, double* out) {
+    start(MPI_Type);
+    pargo_shim_register("ref://slope", slope, GDT_Float64, rows, cols, nodata, cellsize);
+    pargo_shim_register("ref://sca", sca, GDT_Float64, rows, cols, nodata, cellsize);
+    RasterLayer<double> slopeLayer("slopeLayer");
+    slopeLayer.readNeighborhood(nbr);
+    if (!slopeLayer.readFile("ref://slope", ROWWISE_DCMP)) return 1;
+    RasterLayer<double> scaLayer("scaLayer");
+    scaLayer.readNeighborhood(nbr);
+    if (!scaLayer.readFile("ref://sca", ROWWISE_DCMP)) return 1;
+    RasterLayer<double> twiLayer("twiLayer");
+    twiLayer.copyLayerInfo(slopeLayer);
+    TWIOperator op;
+    op.SCALayer(scaLayer);
+    op.slopeLayer(slopeLayer);
+    op.twiLayer(twiLayer);
+    if (!op.Run()) return 2;
+    copy_out(twiLayer, out, rows, cols);
     return 0;
 }
 

@@ -77,6 +77,7 @@ def lib():
         L.pargo_slope_d8.argtypes = [vp, R, R, R, N, i, i, i, vp]
         L.pargo_fill.argtypes = [vp, R, R, N, P(FillOpts), P(FillStats), vp]
         L.pargo_sca.argtypes = [vp, R, R, N, i, vp]
+        L.pargo_twi.argtypes = [vp, R, R, R, N, vp]
         L.pargo_hydro_pipeline.argtypes = [vp, R, R, R, R, R, N, P(FillOpts), i, i, i, P(FillStats), vp]
         L.pargo_batch_slope_d8.argtypes = [vp, i, R, R, R, N, i, i, i, vp]
         L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
@@ -89,7 +90,7 @@ def lib():
         L.pargo_last_d8_fallbacks.argtypes = [vp]
         L.pargo_last_d8_fallbacks.restype = ctypes.c_int64
         for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
-                     "pargo_fill", "pargo_sca", "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
+                     "pargo_fill", "pargo_sca", "pargo_twi", "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
                      "pargo_slope_loss_grad"):
             getattr(L, name).restype = st
         _lib = L
@@ -215,6 +216,11 @@ class Context:
     def sca(self, d8, sca, contract=SCA_CONVERGED, nbr=None, stream=None):
         self._check(lib().pargo_sca(self._p, ctypes.byref(d8), ctypes.byref(sca), self._nbr(nbr), contract,
                                     _stream_ptr(stream)))
+
+    def twi(self, slope, sca, twi, nbr=None, stream=None):
+        """Topographic wetness index ln(sca / max(slope, 1e-7)) (TWIOperator)."""
+        self._check(lib().pargo_twi(self._p, ctypes.byref(slope), ctypes.byref(sca), ctypes.byref(twi),
+                                    self._nbr(nbr), _stream_ptr(stream)))
 
     def batch_slope_d8(self, dems, slopes=None, d8s=None, method=SLOPE_FD, units=RATIO, dir_type=8, nbr=None,
                        stream=None):

@@ -1013,6 +1013,48 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
     return PARGO_OK;
 }
 
+// ------------------------------------------------------------------- TWI --
+pargo_status pargo_twi(pargo_ctx* ctx, const pargo_raster* slope, const pargo_raster* sca, pargo_raster* twi,
+                       const pargo_nbr* nbr, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if ((st = check_raster(ctx, slope, "slope")) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, sca, "sca")) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, twi, "twi")) != PARGO_OK) return st;
+    if ((st = check_dims(ctx, slope)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if ((st = check_same(ctx, slope, sca, "sca")) != PARGO_OK) return st;
+    if ((st = check_same(ctx, slope, twi, "twi")) != PARGO_OK) return st;
+    for (const pargo_raster* r : {slope, sca, (const pargo_raster*)twi})
+        if (r->dtype != PARGO_F32 && r->dtype != PARGO_F64)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "twi: slope, sca and twi must be F32 or F64");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged ss, sa, so;
+    if ((st = stage_in(ctx, slope, kSlotIn0, s, &ss)) != PARGO_OK) return st;
+    if ((st = stage_in(ctx, sca, kSlotIn1, s, &sa)) != PARGO_OK) return st;
+    if ((st = stage_out(ctx, twi, kSlotOut0, &so)) != PARGO_OK) return st;
+    TwiParams p{};
+    p.rows = slope->rows;
+    p.cols = slope->cols;
+    p.slope = ss.in;
+    p.sca = sa.in;
+    p.out = so.out;
+    p.sca_nodata = sca->nodata;
+    memcpy(&p.nd_bits, &sca->nodata, 8);
+    p.nd_f = (float)sca->nodata;
+    p.nd_is_float = (double)p.nd_f == sca->nodata;
+    p.sca_nd_f = (float)sca->nodata;
+    p.out_nd_f = (float)twi->nodata;
+    float eps = 1.0e-7f;
+    if ((double)eps < 1.0e-7) eps = nextafterf(eps, INFINITY);
+    p.eps_cut = eps;
+    CU(ctx, launch_twi(p, ctx->num_sms, s));
+    if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
+    return finish_call(ctx, s, so.host);
+}
+
 // ------------------------------------------------------------------- SCA --
 pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr, int contract,
                        void* stream) {

@@ -149,6 +149,21 @@ ScaTiles sca_tiles_layout(void* base, int64_t rows, int64_t cols);
 // last-cell ship, [4] exits, [5] exits completed, [6] inflows from the ring.
 cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTiles& t, cudaStream_t st);
 
+// twi.cu
+struct TwiParams {
+    int64_t rows, cols;
+    InView slope, sca;
+    OutView out;
+    double sca_nodata;     // the value both inputs are tested against (the SCA raster's nodata)
+    long long nd_bits;     // its bit pattern, for double inputs
+    int nd_is_float;       // it is exactly a float (else no float input can equal it)
+    float nd_f;            // and that float
+    float sca_nd_f;        // the nodata written on nodata windows, as float
+    float out_nd_f;        // the output's nodata (ring), as float
+    float eps_cut;         // the least float >= 1e-7
+};
+cudaError_t launch_twi(const TwiParams& p, int num_sms, cudaStream_t st);
+
 // grad.cu
 struct GradParams {
     int64_t rows, cols;

@@ -76,6 +76,29 @@ protected:
     RasterLayer<double>* _pwDEMLayer = nullptr;
 };
 
+// Topographic wetness index ln(sca / slope) (apps/hydrology/twi/TWIOperator.h:10-31).
+class TWIOperator : public RasterOperator<double> {
+public:
+    void SCALayer(RasterLayer<double>& layerD) {
+        _pSCALayer = &layerD;
+        Configure(_pSCALayer, false);
+    }
+    void slopeLayer(RasterLayer<double>& layerD) {
+        _pSlopeLayer = &layerD;
+        Configure(_pSlopeLayer, false);
+    }
+    void twiLayer(RasterLayer<double>& layerD) {
+        _pTWILayer = &layerD;
+        Configure(_pTWILayer, false);
+    }
+    bool Run() override;
+
+protected:
+    RasterLayer<double>* _pSCALayer = nullptr;
+    RasterLayer<double>* _pSlopeLayer = nullptr;
+    RasterLayer<double>* _pTWILayer = nullptr;
+};
+
 class SCAOperator : public RasterOperator<double> {
 public:
     void d8Layer(RasterLayer<double>& layerD) {

@@ -113,6 +113,17 @@ bool SCAOperator::Run() {
     return report_status(pargo_sca(ctx, &d8, &out, &_pD8Layer->nbrhood()->abi(), c, nullptr), "SCAOperator::Run");
 }
 
+bool TWIOperator::Run() {
+    if (!_pSCALayer || !_pSlopeLayer || !_pTWILayer) {
+        cerr << "TWIOperator::Run: SCALayer, slopeLayer and twiLayer must be set" << endl;
+        return false;
+    }
+    pargo_ctx* ctx = Application::context();
+    if (!ctx) return false;
+    pargo_raster sl = _pSlopeLayer->abi_raster(), sa = _pSCALayer->abi_raster(), out = _pTWILayer->abi_raster();
+    return report_status(pargo_twi(ctx, &sl, &sa, &out, &_pSCALayer->nbrhood()->abi(), nullptr), "TWIOperator::Run");
+}
+
 }  // namespace GPRO
 
 bool StringMatch(const char* a, const char* b) { return strcasecmp(a, b) == 0; }

@@ -56,6 +56,27 @@ def test_app_chain_matches_reference(case, tmp_path):
     assert bits_equal(d8r, g["d8_256"])
 
 
+@pytest.mark.parametrize("case", ["demtif", "fbm_hydro"])
+def test_app_twi_after_the_chain(case, tmp_path, oracle_lib):
+    """pTWI's step on the chain's files: slope of the filled DEM and the
+    shipped SCA in, TWI out, against the oracle (pinned to TWIOperator) within
+    the FP32 tolerance 1e-6 relative + 1e-6."""
+    g = load_golden(case)
+    nd, cs = float(g["nodata"]), float(g["cellsize"])
+    nbr = tmp_path / "moore.nbr"
+    nbr.write_text(MOORE)
+    write_tiff(str(tmp_path / "fill.tif"), g["fill"], nd, cs)
+    write_tiff(str(tmp_path / "sca.tif"), g["sca_ship"], nd, cs)
+    run("pargo_slope", "-elev", tmp_path / "fill.tif", "-nbr", nbr, "-slp", tmp_path / "slope.tif")
+    sl, _, _ = read_tiff(str(tmp_path / "slope.tif"))
+    run("pargo_twi", tmp_path / "slope.tif", tmp_path / "sca.tif", nbr, tmp_path / "twi.tif")
+    t, tnd, _ = read_tiff(str(tmp_path / "twi.tif"))
+    ref = oracle_lib.twi(sl, g["sca_ship"], nd)
+    assert tnd == nd and np.array_equal(t == nd, ref == nd)
+    ok = ref != nd
+    assert (np.abs(t[ok] - ref[ok]) <= 1e-6 * np.abs(ref[ok]) + 1e-6).all()
+
+
 def test_app_rejects_bad_neighbourhood(tmp_path):
     g = load_golden("fbm_slope")
     dem = tmp_path / "dem.tif"

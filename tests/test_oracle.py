@@ -117,3 +117,20 @@ def test_oracle_fill_near_zero_matches_reference_binary(oracle_lib):
     w_gs, sw = oracle_lib.fill_gs(dem, -9999.0)
     assert bits_equal(w_gs, w_ref) and sw == sw_ref
     assert bits_equal(oracle_lib.fill(dem, -9999.0), w_ref)
+
+
+@pytest.mark.parametrize("seed,shape", [(31, (90, 120)), (32, (47, 203))])
+def test_oracle_twi_matches_reference_binary(seed, shape, oracle_lib):
+    """The TWI restatement against the reference TWIOperator, on a filled,
+    routed DEM (nodata windows, flat cells where slope is raised to 1e-7)."""
+    from pargo_gb300 import synth
+    R = _ref()
+    O = oracle_lib
+    dem = synth.hydro_dem(shape[0], shape[1], seed=seed)
+    w = O.fill(dem, -9999.0)
+    sl = O.slope(w, -9999.0, 30.0)
+    sca = O.sca(O.d8(w, -9999.0), -9999.0, shipped=True)
+    sl[5, 5] = 0.0   # a zero slope: raised to Eps
+    ref = R.twi(sl, sca, -9999.0, 30.0)
+    assert bits_equal(O.twi(sl, sca, -9999.0), ref)
+    assert (ref == -9999.0).any() and np.isfinite(ref).all()
