@@ -169,6 +169,8 @@ def test_full_size_d8_bit_exact_and_fallback_rate(ctx, oracle_lib):
     sref = oracle_lib.slope(dem, -9999.0, 30.0, threads=16)
     ok, mx, mean = slope_close(host(s), sref)
     assert ok, mx
+    # the FP32 slope's error against the FP64 oracle, stated (pytest -s shows it)
+    print("slope error vs FP64 oracle, 8192^2 hydro DEM, float32 kernel: max rel %.3e, mean rel %.3e" % (mx, mean))
     # host-buffer call to read the fallback count
     sh = np.empty((512, 512), np.float32)
     ch = np.empty((512, 512), np.int8)

@@ -6,7 +6,7 @@ import pytest
 import torch
 
 from conftest import GOLDEN_CASES, bits_equal, load_golden, near_zero_dem
-from gpu_helpers import d8_as_f64, dev, empty_dev, host
+from gpu_helpers import d8_as_f64, dev, empty_dev, host, ref_noise_floor, slope_close
 from pargo_gb300 import abi, synth
 
 pytestmark = pytest.mark.gpu
@@ -56,6 +56,13 @@ def test_pipeline_against_oracle(seed, shape, ctx, oracle_lib):
         out = empty_dev(shape, np.float64)
         ctx.sca(abi.raster(c, -128), abi.raster(out, nd), contract=contract)
         assert bits_equal(host(out), oracle_lib.sca(d8ref, nd, shipped=shipped))
+    # slope on the float64 levels (integer-key path) against the FP64 oracle, stated
+    s = empty_dev(shape, np.float32)
+    ctx.slope(abi.raster(w, nd, 30.0), abi.raster(s, nd))
+    ok, mx, mean = slope_close(host(s), oracle_lib.slope(wref, nd, 30.0), atol=ref_noise_floor(wref, 30.0))
+    assert ok, mx
+    print("slope error vs FP64 oracle, filled %dx%d levels, float64-input kernel: max rel %.3e, mean rel %.3e"
+          % (shape[0], shape[1], mx, mean))
 
 
 def test_fill_options_and_round_cap(ctx, oracle_lib):
