@@ -195,6 +195,28 @@ pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca
 pargo_status pargo_twi(pargo_ctx* ctx, const pargo_raster* slope, const pargo_raster* sca, pargo_raster* twi,
                        const pargo_nbr* nbr, void* stream);
 
+/* MFD-md flow partition weights, replacing MFDOperator::Operator()
+ * (apps/hydrology/flowdirmfdmd/mfdOperator.cpp:39-125) run over the raster: `weights` points to
+ * 8 rasters, layer i holding the share of the cell's flow sent to window
+ * position i (positions in row-major order, the centre skipped).  A cell's
+ * weights are drop_i^pe * l_i / sum over its strictly lower valid neighbours,
+ * pe = (1 - e) * min(max drop, 1) + e with e = slp_exp; a nodata cell (|z -
+ * nodata| <= 1e-6) and the ring get the DEM's nodata in every layer.  dem: F32
+ * or F64; weights: F32 or F64, computed in FP32 (about 1e-6 relative). */
+pargo_status pargo_mfd(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* weights, const pargo_nbr* nbr,
+                       double slp_exp, void* stream);
+
+/* MFD specific catchment area, replacing the scamfdmd SCAOperator
+ * (apps/hydrology/scamfdmd/scaOperator.cpp:43-113) as its single raster-order
+ * sweep leaves it: a valid cell takes 1 + the sum, in window order, of
+ * sca(q) * w(q -> cell) over the neighbours q that have finished before it in
+ * that sweep.  Sums are FP64 with the reference's operation order, so the
+ * output is bit-identical given the same weights.  weights: 8 rasters (F32 or
+ * F64), nodata = |w0 - nodata| < 1e-6; sca: F32 or F64 with weight layer 0's
+ * nodata.  PARGO_ERR_CYCLE when the weights hold a cycle. */
+pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_raster* sca, const pargo_nbr* nbr,
+                           void* stream);
+
 /* Batched fused slope + D8 over `count` independent rasters in one persistent
  * launch; slopes / d8s may be NULL (no such output) and all rasters must be on
  * the device. */

@@ -50,6 +50,8 @@ class Oracle:
         lib.orc_sca_sweeps.argtypes = [_c_f64p, i, i, d, i, _c_f64p, ctypes.POINTER(ctypes.c_int)]
         lib.orc_sca_topo.argtypes = [_c_f64p, i, i, d, _c_f64p, _c_f64p]
         lib.orc_twi.argtypes = [_c_f64p, _c_f64p, i, i, d, d, _c_f64p]
+        lib.orc_mfd.argtypes = [vp, i, i, i, d, f, d, _c_f64p]
+        lib.orc_sca_mfd.argtypes = [_c_f64p, i, i, d, _c_f64p]
         self.lib = lib
 
     @staticmethod
@@ -117,6 +119,26 @@ class Oracle:
 
 
 
+    def mfd(self, dem, nodata, cellsize, slp_exp):
+        """MFD-md weights (MFDOperator) as an (8, rows, cols) array: layer i is
+        window position i (i < 4) or i + 1 (i >= 4)."""
+        a, f64 = self._surface(dem)
+        out = np.empty((8,) + a.shape, np.float64)
+        rc = self.lib.orc_mfd(a.ctypes.data, f64, a.shape[0], a.shape[1], nodata, float(np.float32(cellsize)),
+                              float(slp_exp), _p(out, _c_f64p))
+        if rc:
+            raise OracleError("orc_mfd rc=%d" % rc)
+        return out
+
+    def sca_mfd(self, weights, nodata):
+        """MFD SCA as the reference's single accumulation sweep leaves it."""
+        w = _c(weights, np.float64)
+        out = np.empty(w.shape[1:], np.float64)
+        rc = self.lib.orc_sca_mfd(_p(w, _c_f64p), w.shape[1], w.shape[2], nodata, _p(out, _c_f64p))
+        if rc:
+            raise OracleError("orc_sca_mfd rc=%d" % rc)
+        return out
+
     def twi(self, slope, sca, nodata, out_nodata=None):
         """Topographic wetness index ln(sca / max(slope, 1e-7)) with the
         reference's nodata rule (TWIOperator.cpp:42-69), in FP64."""
@@ -145,6 +167,12 @@ class Reference:
         lib.ref_sca.argtypes = [cp, _c_f64p, i, i, d, d, i, _c_f64p, ctypes.POINTER(ctypes.c_int)]
         lib.ref_twi.argtypes = [cp, _c_f64p, _c_f64p, i, i, d, d, _c_f64p]
         self.lib = lib
+        self.mfd_lib = None
+        if os.path.exists(_build.REF_MFD_SO):
+            m = ctypes.CDLL(_build.REF_MFD_SO)
+            m.ref_mfd.argtypes = [cp, _c_f32p, i, i, d, d, d, _c_f64p]
+            m.ref_sca_mfd.argtypes = [cp, _c_f64p, i, i, d, d, _c_f64p]
+            self.mfd_lib = m
         self._nbr = os.path.join(_build.REF_OUT, "moore.nbr")
         with open(self._nbr, "w") as fh:
             fh.write(MOORE_NBR)
@@ -191,6 +219,24 @@ class Reference:
         if rc:
             raise OracleError("ref_sca rc=%d" % rc)
         return out, sw.value
+
+    def mfd(self, dem, nodata, cellsize, slp_exp):
+        a = _c(dem, np.float32)
+        out = np.empty((8,) + a.shape, np.float64)
+        rc = self.mfd_lib.ref_mfd(self._nbr.encode(), _p(a, _c_f32p), a.shape[0], a.shape[1], nodata, cellsize,
+                                  float(slp_exp), _p(out, _c_f64p))
+        if rc:
+            raise OracleError("ref_mfd rc=%d" % rc)
+        return out
+
+    def sca_mfd(self, weights, nodata, cellsize=1.0):
+        w = _c(weights, np.float64)
+        out = np.empty(w.shape[1:], np.float64)
+        rc = self.mfd_lib.ref_sca_mfd(self._nbr.encode(), _p(w, _c_f64p), w.shape[1], w.shape[2], nodata, cellsize,
+                                      _p(out, _c_f64p))
+        if rc:
+            raise OracleError("ref_sca_mfd rc=%d" % rc)
+        return out
 
     def twi(self, slope, sca, nodata, cellsize=1.0):
         s1 = _c(slope, np.float64)

@@ -25,6 +25,7 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD, "liboracle.so")
 REF_SO = os.path.join(REF_OUT, "libpargo_ref.so")
+REF_MFD_SO = os.path.join(REF_OUT, "libpargo_ref_mfd.so")
 REFERENCE_ROOT = os.environ.get("PARGO_REFERENCE_ROOT", "/root/reference")
 
 REF_SOURCES = [
@@ -52,6 +53,17 @@ def oracle_cmd():
             os.path.join(HERE, "pargo_oracle.c"), "-o", ORACLE_SO, "-lm"]
 
 
+# The MFD-md pair lives in a library of its own: its SCA operator has the
+# same class name as the D8 one.
+REF_MFD_SOURCES = [
+    "gpro/application.cpp",
+    "gpro/utility.cpp",
+    "apps/hydrology/flowdirmfdmd/mfdOperator.cpp",
+    "apps/hydrology/scamfdmd/scaOperator.cpp",
+]
+REF_MFD_INCLUDES = ["gpro", "apps/hydrology/flowdirmfdmd", "apps/hydrology/scamfdmd"]
+
+
 def reference_available():
     return all(os.path.exists(os.path.join(REFERENCE_ROOT, s)) for s in REF_SOURCES)
 
@@ -66,11 +78,23 @@ def ref_cmd():
     return cmd
 
 
+def ref_mfd_cmd():
+    os.makedirs(REF_OUT, exist_ok=True)
+    cmd = ["g++", "-std=gnu++14", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+           "-DLINUX", "-DNDEBUG", "-w", "-I" + os.path.join(HERE, "ref_shim")]
+    cmd += ["-I" + os.path.join(REFERENCE_ROOT, d) for d in REF_MFD_INCLUDES]
+    cmd += [os.path.join(REFERENCE_ROOT, s) for s in REF_MFD_SOURCES]
+    cmd += [os.path.join(HERE, "ref_driver_mfd.cpp"), "-o", REF_MFD_SO]
+    return cmd
+
+
 def commands():
     """(name, argv) pairs for everything buildable on this machine."""
     out = [("oracle", oracle_cmd())]
     if reference_available():
         out.append(("reference", ref_cmd()))
+        if all(os.path.exists(os.path.join(REFERENCE_ROOT, s)) for s in REF_MFD_SOURCES):
+            out.append(("reference MFD-md", ref_mfd_cmd()))
     return out
 
 

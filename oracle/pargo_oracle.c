@@ -506,3 +506,119 @@ int orc_twi(const double* slope, const double* sca, int rows, int cols, double s
         }
     return 0;
 }
+
+/* MFD-md flow partition weights, restating MFDOperator::Operator
+ * (apps/hydrology/flowdirmfdmd/mfdOperator.cpp:36-123).  w holds 8 layers of
+ * rows*cols doubles; layer i is the window position i (i < 4) or i + 1
+ * (i >= 4) seen from the cell, as pMFDmd.cpp:132-137 names the files.  Work
+ * cells: all 8 weights nodata when the cell is nodata (|z - nd| <= 1e-6, :60);
+ * else drops to strictly lower, valid neighbours -- (z - zn) / (1.414 cs) on
+ * diagonals with contour length 0.354 cs, (z - zn) / cs with 0.5 cs on
+ * cardinals (:83-92) -- the exponent pe = (1 - e) min(max drop, 1) + e
+ * (:100-103) and w_i = drop_i^pe l_i / sum over the window (:104-116).
+ * Ring cells keep the layers' initial nodata (copyLayerInfo, pMFDmd.cpp:138). */
+int orc_mfd(const void* dem, int dem_f64, int rows, int cols, double nodata, float cellsize_f, double slp_exp,
+            double* w) {
+    if (rows < 0 || cols < 0) return 1;
+    const double cs = (double)cellsize_f;
+    const size_t n = (size_t)rows * cols;
+    for (size_t i = 0; i < 8 * n; i++) w[i] = nodata;
+    for (int r = 1; r < rows - 1; r++)
+        for (int c = 1; c < cols - 1; c++) {
+            const size_t i = (size_t)r * cols + c;
+            const double z = dem_f64 ? ((const double*)dem)[i] : (double)((const float*)dem)[i];
+            if (fabs(z - nodata) <= 0.000001) continue;  /* all 8 stay nodata */
+            double diff[9], l[9], maxd = 0.0;
+            int dir = 0;
+            for (int a = -1; a <= 1; a++)
+                for (int b = -1; b <= 1; b++, dir++) {
+                    const size_t j = (size_t)(r + a) * cols + (c + b);
+                    const double zn = dem_f64 ? ((const double*)dem)[j] : (double)((const float*)dem)[j];
+                    if (fabs(zn - nodata) <= 0.000001 || z <= zn) {
+                        diff[dir] = 0.0;
+                        l[dir] = 0.0;
+                    } else {
+                        if (dir == 0 || dir == 2 || dir == 6 || dir == 8) {
+                            diff[dir] = (z - zn) / (1.414 * cs);
+                            l[dir] = 0.354 * cs;
+                        } else {
+                            diff[dir] = (z - zn) / cs;
+                            l[dir] = 0.5 * cs;
+                        }
+                        if (diff[dir] > maxd) maxd = diff[dir];
+                    }
+                }
+            if (maxd > 1) maxd = 1;
+            const double pe = (1 - slp_exp) * maxd + slp_exp;
+            double sum = 0.0;
+            for (int k = 0; k < 9; k++) sum += pow(diff[k], pe) * l[k];
+            for (int k = 0; k < 8; k++) w[(size_t)k * n + i] = 0.0;
+            if (sum > 0)
+                for (int k = 0; k < 9; k++) {
+                    if (k == 4) continue;
+                    w[(size_t)(k < 4 ? k : k - 1) * n + i] = (pow(diff[k], pe) * l[k]) / sum;
+                }
+        }
+    return 0;
+}
+
+/* MFD specific catchment area, restating the scamfdmd SCAOperator
+ * (apps/hydrology/scamfdmd/scaOperator.cpp:42-113) as the reference runs it:
+ * one raster sweep to initialise (sca = 1, degree 0; nodata when weight layer
+ * 0 is within 1e-6 of nodata: degree -1), one to count in-degrees (neighbours
+ * whose weight towards the cell is > 0), then ONE accumulation sweep in raster
+ * order: a cell with degree > 0 adds sca(n) w(n -> cell) for each neighbour n
+ * whose degree is 0 at that moment, in window order, and decrements its own
+ * degree.  Ring cells stay nodata; the degree layer's ring holds nodata. */
+int orc_sca_mfd(const double* w, int rows, int cols, double nodata, double* sca) {
+    if (rows < 0 || cols < 0) return 1;
+    const size_t n = (size_t)rows * cols;
+    double* deg = (double*)malloc(n * sizeof(double));
+    if (!deg) return 2;
+    for (size_t i = 0; i < n; i++) {
+        sca[i] = nodata;
+        deg[i] = nodata;
+    }
+    for (int r = 1; r < rows - 1; r++)
+        for (int c = 1; c < cols - 1; c++) {
+            const size_t i = (size_t)r * cols + c;
+            if (fabs(w[i] - nodata) < 0.000001) {
+                deg[i] = -1;
+                sca[i] = nodata;
+            } else {
+                deg[i] = 0;
+                sca[i] = 1;
+            }
+        }
+    for (int r = 1; r < rows - 1; r++)
+        for (int c = 1; c < cols - 1; c++) {
+            const size_t i = (size_t)r * cols + c;
+            int dir = 8;
+            for (int a = -1; a <= 1; a++)
+                for (int b = -1; b <= 1; b++, dir--) {
+                    const size_t j = (size_t)(r + a) * cols + (c + b);
+                    if (dir > 4 && w[(size_t)(dir - 1) * n + j] > 0) deg[i]++;
+                    if (dir < 4 && w[(size_t)dir * n + j] > 0) deg[i]++;
+                }
+        }
+    for (int r = 1; r < rows - 1; r++)
+        for (int c = 1; c < cols - 1; c++) {
+            const size_t i = (size_t)r * cols + c;
+            if (deg[i] <= 0) continue;
+            int dir = 8;
+            for (int a = -1; a <= 1; a++)
+                for (int b = -1; b <= 1; b++, dir--) {
+                    const size_t j = (size_t)(r + a) * cols + (c + b);
+                    if (dir > 4 && deg[j] == 0 && w[(size_t)(dir - 1) * n + j] > 0) {
+                        sca[i] += sca[j] * w[(size_t)(dir - 1) * n + j];
+                        deg[i]--;
+                    }
+                    if (dir < 4 && deg[j] == 0 && w[(size_t)dir * n + j] > 0) {
+                        sca[i] += sca[j] * w[(size_t)dir * n + j];
+                        deg[i]--;
+                    }
+                }
+        }
+    free(deg);
+    return 0;
+}

@@ -78,6 +78,8 @@ def lib():
         L.pargo_fill.argtypes = [vp, R, R, N, P(FillOpts), P(FillStats), vp]
         L.pargo_sca.argtypes = [vp, R, R, N, i, vp]
         L.pargo_twi.argtypes = [vp, R, R, R, N, vp]
+        L.pargo_mfd.argtypes = [vp, R, R, N, ctypes.c_double, vp]
+        L.pargo_sca_mfd.argtypes = [vp, R, R, N, vp]
         L.pargo_hydro_pipeline.argtypes = [vp, R, R, R, R, R, N, P(FillOpts), i, i, i, P(FillStats), vp]
         L.pargo_batch_slope_d8.argtypes = [vp, i, R, R, R, N, i, i, i, vp]
         L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
@@ -90,7 +92,8 @@ def lib():
         L.pargo_last_d8_fallbacks.argtypes = [vp]
         L.pargo_last_d8_fallbacks.restype = ctypes.c_int64
         for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
-                     "pargo_fill", "pargo_sca", "pargo_twi", "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
+                     "pargo_fill", "pargo_sca", "pargo_twi", "pargo_mfd", "pargo_sca_mfd",
+                     "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
                      "pargo_slope_loss_grad"):
             getattr(L, name).restype = st
         _lib = L
@@ -221,6 +224,21 @@ class Context:
         """Topographic wetness index ln(sca / max(slope, 1e-7)) (TWIOperator)."""
         self._check(lib().pargo_twi(self._p, ctypes.byref(slope), ctypes.byref(sca), ctypes.byref(twi),
                                     self._nbr(nbr), _stream_ptr(stream)))
+
+    def mfd(self, dem, weights, slp_exp=1.1, nbr=None, stream=None):
+        """MFD-md flow partition weights (MFDOperator) into 8 rasters."""
+        if len(weights) != 8:
+            raise ValueError("mfd: 8 weight rasters")
+        W = (Raster * 8)(*weights)
+        self._check(lib().pargo_mfd(self._p, ctypes.byref(dem), W, self._nbr(nbr), float(slp_exp),
+                                    _stream_ptr(stream)))
+
+    def sca_mfd(self, weights, sca, nbr=None, stream=None):
+        """MFD specific catchment area from 8 weight rasters (scamfdmd SCAOperator)."""
+        if len(weights) != 8:
+            raise ValueError("sca_mfd: 8 weight rasters")
+        W = (Raster * 8)(*weights)
+        self._check(lib().pargo_sca_mfd(self._p, W, ctypes.byref(sca), self._nbr(nbr), _stream_ptr(stream)))
 
     def batch_slope_d8(self, dems, slopes=None, d8s=None, method=SLOPE_FD, units=RATIO, dir_type=8, nbr=None,
                        stream=None):

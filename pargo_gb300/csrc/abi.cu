@@ -7,6 +7,8 @@
 
 #include <cudaTypedefs.h>
 #include <math.h>
+
+#include <cmath>
 #include <string.h>
 
 #include <algorithm>
@@ -33,7 +35,7 @@ struct pargo_ctx {
         void* p = nullptr;
         size_t n = 0;
     };
-    Slot slots[32];
+    Slot slots[48];
     // pinned host scratch (counter read-back, table staging)
     void* pinned = nullptr;
     size_t pinned_n = 0;
@@ -56,9 +58,10 @@ enum SlotId {
     kSlotIn0 = 0, kSlotIn1, kSlotOut0, kSlotOut1, kSlotFillW, kSlotFillLists, kSlotFillQueued,
     kSlotScaIndeg, kSlotScaConv, kSlotScaShip, kSlotScaFlags, kSlotScaCounters, kSlotBatchMaps,
     kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut,
-    kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotCount
+    kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotMfdLayer0,
+    kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotCount
 };
-static_assert(kSlotCount <= 32, "context slot table");
+static_assert(kSlotCount <= 48, "context slot table");
 
 namespace {
 
@@ -199,23 +202,26 @@ double dval_h(uint64_t k) {
 }
 
 template <typename K, typename T, typename ToV>
-void band_search(K kmin, K kmax, double nodata, double eps, ToV val, T* lo, T* hi) {
-    // f(k) = fl64((double)val(k) - nodata) is non-decreasing in k.
+void band_search(K kmin, K kmax, double nodata, double eps, ToV val, T* lo, T* hi, bool inclusive = false) {
+    // f(k) = fl64((double)val(k) - nodata) is non-decreasing in k.  The band is
+    // |f| < eps, or |f| <= eps when inclusive.
     auto f = [&](K k) { return (double)val(k) - nodata; };
-    // smallest k with f(k) > -eps
+    auto above = [&](K k) { return inclusive ? f(k) >= -eps : f(k) > -eps; };
+    auto below = [&](K k) { return inclusive ? f(k) <= eps : f(k) < eps; };
+    // smallest k above -eps
     K a = kmin, b = kmax;
-    if (!(f(b) > -eps)) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
+    if (!above(b)) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
     while (a < b) {
         K m = a + (b - a) / 2;
-        if (f(m) > -eps) b = m; else a = m + 1;
+        if (above(m)) b = m; else a = m + 1;
     }
     K l = a;
-    // largest k with f(k) < eps
+    // largest k below eps
     a = kmin; b = kmax;
-    if (!(f(a) < eps)) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
+    if (!below(a)) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
     while (a < b) {
         K m = a + (b - a + 1) / 2;
-        if (f(m) < eps) a = m; else b = m - 1;
+        if (below(m)) a = m; else b = m - 1;
     }
     K h = a;
     if (l > h) { *lo = (T)INFINITY; *hi = (T)-INFINITY; return; }
@@ -233,6 +239,32 @@ Band<double> double_band(double nodata, double eps) {
     Band<double> b;
     band_search<uint64_t, double>(dkey_h(-INFINITY), dkey_h(INFINITY), nodata, eps, dval_h, &b.lo, &b.hi);
     return b;
+}
+Band<float> float_band_incl(double nodata, double eps) {
+    Band<float> b;
+    band_search<uint32_t, float>(fkey(-INFINITY), fkey(INFINITY), nodata, eps, fval, &b.lo, &b.hi, true);
+    return b;
+}
+Band<double> double_band_incl(double nodata, double eps) {
+    Band<double> b;
+    band_search<uint64_t, double>(dkey_h(-INFINITY), dkey_h(INFINITY), nodata, eps, dval_h, &b.lo, &b.hi, true);
+    return b;
+}
+// A band of doubles as signed order-preserving keys (the device's dkey64);
+// an empty band gives lo > hi.
+void band_keys(const Band<double>& b, long long* lo, long long* hi) {
+    if (!(b.lo <= b.hi)) {
+        *lo = 1;
+        *hi = 0;
+        return;
+    }
+    auto k = [](double x) {
+        long long v;
+        memcpy(&v, &x, 8);
+        return v ^ ((v >> 63) & 0x7FFFFFFFFFFFFFFFLL);
+    };
+    *lo = k(b.lo);
+    *hi = k(b.hi);
 }
 
 SlopeConsts slope_consts(double cellsize, int method, int units) {
@@ -1010,6 +1042,155 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
     local.raised_cells = wdem ? (int64_t)hp[0] : -1;
     if (stats) *stats = local;
     if (sca) return sca_check(ctx, hp + 1, "pipeline sca");
+    return PARGO_OK;
+}
+
+// ---------------------------------------------------------------- MFD-md --
+pargo_status pargo_mfd(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* weights, const pargo_nbr* nbr,
+                       double slp_exp, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if (!weights) return fail(ctx, PARGO_ERR_INVALID_ARG, "mfd: weights must point to 8 rasters");
+    if ((st = check_raster(ctx, dem, "dem")) != PARGO_OK) return st;
+    if (dem->dtype != PARGO_F32 && dem->dtype != PARGO_F64)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "mfd: dem must be F32 or F64");
+    if ((st = check_dims(ctx, dem)) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    for (int q = 0; q < 8; q++) {
+        if ((st = check_raster(ctx, &weights[q], "weight")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, dem, &weights[q], "weight")) != PARGO_OK) return st;
+        if (weights[q].dtype != PARGO_F32 && weights[q].dtype != PARGO_F64)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "mfd: weights must be F32 or F64");
+    }
+    if (!std::isfinite(slp_exp)) return fail(ctx, PARGO_ERR_INVALID_ARG, "mfd: slope exponent must be finite");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sd, sw[8];
+    if ((st = stage_in(ctx, dem, kSlotIn0, s, &sd)) != PARGO_OK) return st;
+    for (int q = 0; q < 8; q++)
+        if ((st = stage_out(ctx, &weights[q], kSlotMfdLayer0 + q, &sw[q])) != PARGO_OK) return st;
+    MfdParams p{};
+    p.rows = dem->rows;
+    p.cols = dem->cols;
+    p.dem = sd.in;
+    p.ndf = float_band_incl(dem->nodata, kEpsHydro);  // flowdirmfdmd/mfdOperator.cpp:55,77 test <= 1e-6
+    long long klo, khi;
+    band_keys(double_band_incl(dem->nodata, kEpsHydro), &klo, &khi);
+    p.ndd_lo = klo;
+    p.ndd_hi = khi;
+    const double cs = (double)(float)dem->cellsize;  // MetaData::cellSize is a float
+    p.den_card = (float)cs;
+    p.den_diag = (float)(1.414 * cs);
+    p.len_card = (float)(0.5 * cs);
+    p.len_diag = (float)(0.354 * cs);
+    p.slp_exp = (float)slp_exp;
+    bool any_host = false;
+    for (int q = 0; q < 8; q++) {
+        p.w[q] = sw[q].out;
+        any_host = any_host || sw[q].host;
+    }
+    CU(ctx, launch_mfd_weights(p, ctx->num_sms, s));
+    for (int q = 0; q < 8; q++)
+        if ((st = unstage_out(ctx, sw[q], s)) != PARGO_OK) return st;
+    return finish_call(ctx, s, any_host);
+}
+
+pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_raster* sca, const pargo_nbr* nbr,
+                           void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if (!weights) return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: weights must point to 8 rasters");
+    for (int q = 0; q < 8; q++) {
+        if ((st = check_raster(ctx, &weights[q], "weight")) != PARGO_OK) return st;
+        if (q && (st = check_same(ctx, &weights[0], &weights[q], "weight")) != PARGO_OK) return st;
+        if (weights[q].dtype != PARGO_F32 && weights[q].dtype != PARGO_F64)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: weights must be F32 or F64");
+    }
+    if ((st = check_dims(ctx, &weights[0])) != PARGO_OK) return st;
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if ((st = check_raster(ctx, sca, "sca")) != PARGO_OK) return st;
+    if ((st = check_same(ctx, &weights[0], sca, "sca")) != PARGO_OK) return st;
+    if (sca->dtype != PARGO_F32 && sca->dtype != PARGO_F64)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: sca must be F32 or F64");
+    const int64_t n = weights[0].rows * weights[0].cols;
+    if (n >= INT32_MAX) return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: raster too large");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sw[8], so;
+    for (int q = 0; q < 8; q++)
+        if ((st = stage_in(ctx, &weights[q], kSlotMfdLayer0 + q, s, &sw[q])) != PARGO_OK) return st;
+    if ((st = stage_out(ctx, sca, kSlotOut0, &so)) != PARGO_OK) return st;
+    cudaError_t e;
+    ScaMfdParams p{};
+    p.rows = weights[0].rows;
+    p.cols = weights[0].cols;
+    for (int q = 0; q < 8; q++) p.w[q] = sw[q].in;
+    long long klo, khi;
+    band_keys(double_band(weights[0].nodata, kEpsHydro), &klo, &khi);  // scamfdmd/scaOperator.cpp:50 tests < 1e-6
+    p.nd_lo = klo;
+    p.nd_hi = khi;
+    p.nodata = weights[0].nodata;  // the reference's SCA layer copies weight layer 0's nodata
+    p.out = so.out;
+    p.cnt = (int32_t*)slot(ctx, kSlotMfdCnt, (size_t)n * 4, &e);
+    p.flags = (uint8_t*)slot(ctx, kSlotMfdFlags, (size_t)n, &e);
+    p.sca = (double*)slot(ctx, kSlotMfdSca, (size_t)n * 8, &e);
+    int32_t* lists = (int32_t*)slot(ctx, kSlotMfdLists, (size_t)(2 * n + 8) * 4 + 64, &e);
+    if (!p.cnt || !p.flags || !p.sca || !lists) return cuda_fail(ctx, e, "sca_mfd scratch");
+    p.list_a = lists;
+    p.list_b = lists + n;
+    p.counts = lists + 2 * n;
+    p.totals = (unsigned long long*)(((uintptr_t)(lists + 2 * n + 8) + 7) & ~(uintptr_t)7);
+    CU(ctx, launch_sca_mfd_init(p, ctx->num_sms, s));
+    // Frontier rounds, 32 per CUDA graph (an even number: list A is current
+    // again after each graph), until both lists are empty.
+    constexpr int kRounds = 32;
+    CU(ctx, cudaEventRecord(ctx->ev_a, s));
+    CU(ctx, cudaStreamWaitEvent(ctx->own, ctx->ev_a, 0));
+    cudaGraph_t g;
+    cudaGraphExec_t ge = nullptr;
+    CU(ctx, cudaStreamBeginCapture(ctx->own, cudaStreamCaptureModeThreadLocal));
+    cudaError_t ce = cudaSuccess;
+    for (int r = 0; r < kRounds && ce == cudaSuccess; r++) ce = launch_sca_mfd_round(p, r & 1, ctx->num_sms, ctx->own);
+    cudaError_t ee = cudaStreamEndCapture(ctx->own, &g);
+    if (ce != cudaSuccess) return cuda_fail(ctx, ce, "sca_mfd round capture");
+    if (ee != cudaSuccess) return cuda_fail(ctx, ee, "sca_mfd graph capture");
+    ee = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ee != cudaSuccess) return cuda_fail(ctx, ee, "sca_mfd graph instantiate");
+    int32_t* hc = (int32_t*)pinned(ctx, 128, &e);
+    if (!hc) {
+        cudaGraphExecDestroy(ge);
+        return cuda_fail(ctx, e, "pinned counters");
+    }
+    pargo_status rs = PARGO_OK;
+    for (int64_t launched = 0;; launched += kRounds) {
+        if ((e = cudaGraphLaunch(ge, ctx->own)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(hc, p.counts, 2 * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->own)) != cudaSuccess ||
+            (e = cudaStreamSynchronize(ctx->own)) != cudaSuccess) {
+            rs = cuda_fail(ctx, e, "sca_mfd rounds");
+            break;
+        }
+        if (hc[0] == 0 && hc[1] == 0) break;
+        if (launched > n + kRounds) {  // more rounds than cells: cannot happen on a DAG
+            rs = fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: frontier did not drain");
+            break;
+        }
+    }
+    cudaGraphExecDestroy(ge);
+    if (rs != PARGO_OK) return rs;
+    CU(ctx, cudaEventRecord(ctx->ev_b, ctx->own));
+    CU(ctx, cudaStreamWaitEvent(s, ctx->ev_b, 0));
+    CU(ctx, launch_sca_mfd_output(p, ctx->num_sms, s));
+    if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
+    unsigned long long* ht = (unsigned long long*)(hc + 8);
+    CU(ctx, cudaMemcpyAsync(ht, p.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+    if (ht[2] != 0)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: %llu nodata cells carry positive weights", ht[2]);
+    if (ht[0] != ht[1])
+        return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: %llu of %llu valid cells processed (cycle)", ht[1], ht[0]);
     return PARGO_OK;
 }
 

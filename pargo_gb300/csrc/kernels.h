@@ -164,6 +164,37 @@ struct TwiParams {
 };
 cudaError_t launch_twi(const TwiParams& p, int num_sms, cudaStream_t st);
 
+// mfd.cu
+struct MfdParams {
+    int64_t rows, cols;
+    InView dem;                    // F32 or F64
+    Band<float> ndf;               // DEM nodata, |z - nd| <= 1e-6, float input
+    long long ndd_lo, ndd_hi;      // the same band as order-preserving keys, double input
+    float den_card, den_diag;      // cs, 1.414 cs
+    float len_card, len_diag;      // 0.5 cs, 0.354 cs
+    float slp_exp;
+    OutView w[8];                  // layer i: window position i (i < 4) or i + 1
+};
+cudaError_t launch_mfd_weights(const MfdParams& p, int num_sms, cudaStream_t st);
+
+struct ScaMfdParams {
+    int64_t rows, cols;
+    InView w[8];
+    long long nd_lo, nd_hi;        // weight layer 0 nodata band (|w - nd| < 1e-6) as keys
+    double nodata;                 // written on nodata cells and the ring
+    OutView out;
+    int32_t* cnt;                  // inflows from valid work cells not yet processed
+    uint8_t* flags;                // valid, source, never done, done
+    double* sca;
+    int32_t* list_a;
+    int32_t* list_b;
+    int32_t* counts;               // [0] length of list_a, [1] of list_b, [2] finished blocks
+    unsigned long long* totals;    // [0] valid cells, [1] processed cells, [2] nodata cells with weights
+};
+cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t st);
+cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms, cudaStream_t st);
+cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st);
+
 // grad.cu
 struct GradParams {
     int64_t rows, cols;

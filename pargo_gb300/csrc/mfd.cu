@@ -1,0 +1,257 @@
+// mfd.cu -- MFD-md flow partition weights and the MFD specific catchment area.
+//
+// Weights (MFDOperator::Operator, apps/hydrology/flowdirmfdmd/mfdOperator.cpp:36-123):
+// per work cell, drops to strictly lower valid neighbours -- (z - zn) / (1.414 cs)
+// on diagonals with contour length 0.354 cs, (z - zn) / cs with 0.5 cs on
+// cardinals -- the exponent pe = (1 - e) min(max drop, 1) + e, and
+// w_i = drop_i^pe l_i / sum.  All 8 weights are nodata on a nodata cell
+// (|z - nd| <= 1e-6, the operator's test) and on the ring.  Computed in FP32
+// (powf; about 1e-6 relative to the reference's FP64 pow): drops of float DEMs
+// are exact float differences; for float64 DEMs (pit-removed levels, whose
+// differences are of order the gap) the drop is taken in FP64 and rounded once.
+// Layer i is the window position i (i < 4) or i + 1 (i >= 4).
+//
+// MFD SCA (the scamfdmd SCAOperator, apps/hydrology/scamfdmd/scaOperator.cpp:42-113):
+// the reference makes ONE raster-order accumulation sweep, in which a cell
+// adds sca(n) w(n -> cell) for each inflow n whose degree is 0 at that moment
+// -- a source, or an earlier cell that pulled all its own inflows ("done").
+// Here the same sums are evaluated in topological order: a cell is processed
+// once every inflow from a valid work cell is processed (frontier rounds with
+// in-degree counters); it then adds, in the reference's window order and in
+// FP64 with separately rounded products and sums, the inflows the sweep pulls
+// (source, or earlier in raster order and done), so with the same weights the
+// result equals the reference's bit for bit.  Inflows from cells that are
+// never processed (the ring, nodata) are never pulled.
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace pargo {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr uint8_t kValid = 1, kSource = 2, kNeverDone = 4, kDone = 8;
+
+// window position of c seen from its neighbour at position k, and that
+// neighbour's layer for it
+__device__ __forceinline__ int layer_towards_centre(int k) {
+    const int dir = 8 - k;
+    return dir < 4 ? dir : dir - 1;
+}
+__device__ __forceinline__ int pos_of_layer(int i) { return i < 4 ? i : i + 1; }
+
+__device__ __forceinline__ double load_d(const InView& v, int64_t r, int64_t c) {
+    const char* row = v.base + r * v.pitch;
+    return v.dtype == PARGO_F64 ? reinterpret_cast<const double*>(row)[c]
+                                : (double)reinterpret_cast<const float*>(row)[c];
+}
+// weight > 0 without an FP64 compare
+__device__ __forceinline__ bool positive(const InView& v, int64_t r, int64_t c) {
+    const char* row = v.base + r * v.pitch;
+    if (v.dtype == PARGO_F64) {
+        const long long b = reinterpret_cast<const long long*>(row)[c];
+        return b > 0 && b <= 0x7FF0000000000000LL;  // positive, not NaN (+inf counts, as in the reference)
+    }
+    return reinterpret_cast<const float*>(row)[c] > 0.0f;
+}
+
+// ------------------------------------------------------------- weights --
+__global__ void __launch_bounds__(kThreads) mfd_weights_kernel(const MfdParams p) {
+    const int64_t n = p.rows * p.cols;
+    const bool f64 = p.dem.dtype == PARGO_F64;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / p.cols, c = i % p.cols;
+        bool nd_out = r < 1 || c < 1 || r > p.rows - 2 || c > p.cols - 2;
+        float drop[9], len[9];
+        float maxd = 0.0f;
+        if (!nd_out) {
+            const char* rowc = p.dem.base + r * p.dem.pitch;
+            const float zf = f64 ? 0.0f : reinterpret_cast<const float*>(rowc)[c];
+            const double zd = f64 ? reinterpret_cast<const double*>(rowc)[c] : 0.0;
+            const long long kz = f64 ? dkey64(zd) : 0;
+            nd_out = f64 ? (kz >= p.ndd_lo && kz <= p.ndd_hi) : p.ndf.has(zf);
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                drop[k] = 0.0f;
+                len[k] = 0.0f;
+                if (k == 4 || nd_out) continue;
+                const char* row = p.dem.base + (r + k / 3 - 1) * p.dem.pitch;
+                const int64_t cc = c + k % 3 - 1;
+                const bool diag = k == 0 || k == 2 || k == 6 || k == 8;
+                float d;
+                if (f64) {
+                    const double zn = reinterpret_cast<const double*>(row)[cc];
+                    const long long kn = dkey64(zn);
+                    if ((kn >= p.ndd_lo && kn <= p.ndd_hi) || kz <= kn) continue;  // nodata or not lower
+                    d = (float)__dsub_rn(zd, zn);
+                } else {
+                    const float zn = reinterpret_cast<const float*>(row)[cc];
+                    if (p.ndf.has(zn) || zf <= zn) continue;
+                    d = __fsub_rn(zf, zn);
+                }
+                drop[k] = __fdiv_rn(d, diag ? p.den_diag : p.den_card);
+                len[k] = diag ? p.len_diag : p.len_card;
+                maxd = fmaxf(maxd, drop[k]);
+            }
+        }
+        if (nd_out) {
+#pragma unroll
+            for (int q = 0; q < 8; q++) put_value(p.w[q], r, c, p.w[q].nodata);
+            continue;
+        }
+        if (maxd > 1.0f) maxd = 1.0f;
+        const float pe = (1.0f - p.slp_exp) * maxd + p.slp_exp;
+        float t[9], sum = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            t[k] = powf(drop[k], pe) * len[k];  // 0^pe * 0: 0, or NaN when pe < 0 (as the reference's pow)
+            sum += t[k];
+        }
+        const bool any = sum > 0.0f;
+#pragma unroll
+        for (int q = 0; q < 8; q++) put_float(p.w[q], r, c, any ? __fdiv_rn(t[pos_of_layer(q)], sum) : 0.0f);
+    }
+}
+
+// ------------------------------------------------------------------ SCA --
+__device__ __forceinline__ bool w0_nodata(const ScaMfdParams& p, int64_t r, int64_t c) {
+    // |w - nd| < 1e-6 (scaOperator.cpp:47), as a band of order-preserving keys
+    const char* row = p.w[0].base + r * p.w[0].pitch;
+    const long long k = p.w[0].dtype == PARGO_F64 ? dkey64(reinterpret_cast<const double*>(row)[c])
+                                                  : fkey64(reinterpret_cast<const float*>(row)[c]);
+    return k >= p.nd_lo && k <= p.nd_hi;
+}
+
+__global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdParams p) {
+    const int64_t n = p.rows * p.cols;
+    unsigned long long nvalid = 0, bad = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / p.cols, c = i % p.cols;
+        const bool work = r >= 1 && c >= 1 && r <= p.rows - 2 && c <= p.cols - 2;
+        uint8_t f = 0;
+        int cnt = 0;
+        if (work) {
+            const bool valid = !w0_nodata(p, r, c);
+            int indeg = 0;
+            for (int k = 0; k < 9; k++) {
+                if (k == 4) continue;
+                const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
+                if (!positive(p.w[layer_towards_centre(k)], qr, qc)) continue;
+                indeg++;
+                const bool qwork = qr >= 1 && qc >= 1 && qr <= p.rows - 2 && qc <= p.cols - 2;
+                if (qwork && !w0_nodata(p, qr, qc)) cnt++;
+            }
+            if (valid) {
+                f = kValid | (indeg == 0 ? kSource : 0) | (indeg > cnt ? kNeverDone : 0);
+                nvalid++;
+                if (cnt == 0) p.list_a[atomicAdd(&p.counts[0], 1)] = (int32_t)i;
+            } else {
+                bool out = false;
+                for (int q = 0; q < 8; q++) out = out || positive(p.w[q], r, c);
+                if (indeg > 0 || out) bad++;  // weights into or out of a nodata cell
+            }
+        }
+        p.flags[i] = f;
+        p.cnt[i] = cnt;
+    }
+    if (nvalid) atomicAdd(&p.totals[0], nvalid);
+    if (bad) atomicAdd(&p.totals[2], bad);
+}
+
+// One round: process the current frontier, queue the cells whose last inflow it was.
+__global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdParams p, int parity) {
+    int32_t* cur = parity ? p.list_b : p.list_a;
+    int32_t* next = parity ? p.list_a : p.list_b;
+    int32_t* cur_count = &p.counts[parity];
+    int32_t* next_count = &p.counts[parity ^ 1];
+    const int32_t ncur = *((volatile int32_t*)cur_count);
+    unsigned long long done_cells = 0;
+    for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < ncur;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = cur[idx];
+        const int64_t r = i / p.cols, c = i % p.cols;
+        double sum = 1.0;
+        bool done = !(p.flags[i] & kNeverDone);
+        for (int k = 0; k < 9; k++) {  // window order, as the reference sweeps it
+            if (k == 4) continue;
+            const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
+            const InView& wv = p.w[layer_towards_centre(k)];
+            if (!positive(wv, qr, qc)) continue;
+            const int64_t q = qr * p.cols + qc;
+            const uint8_t fq = p.flags[q];
+            const bool pulled = (fq & kValid) && ((fq & kSource) || (q < i && (fq & kDone)));
+            if (pulled) sum = __dadd_rn(sum, __dmul_rn(p.sca[q], load_d(wv, qr, qc)));
+            else done = false;
+        }
+        p.sca[i] = sum;
+        p.flags[i] = p.flags[i] | (done ? kDone : 0);
+        done_cells++;
+        for (int q = 0; q < 8; q++) {
+            if (!positive(p.w[q], r, c)) continue;
+            const int pos = pos_of_layer(q);
+            const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
+            if (dr < 1 || dc < 1 || dr > p.rows - 2 || dc > p.cols - 2) continue;
+            const int64_t d = dr * p.cols + dc;
+            if (!(p.flags[d] & kValid)) continue;
+            if (atomicSub(&p.cnt[d], 1) == 1) next[atomicAdd(next_count, 1)] = (int32_t)d;
+        }
+    }
+    if (done_cells) atomicAdd(&p.totals[1], done_cells);
+    // the last block to finish empties the consumed list
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&p.counts[2], 1) == (int32_t)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        *cur_count = 0;
+        p.counts[2] = 0;
+        __threadfence();
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) sca_mfd_output_kernel(const ScaMfdParams p) {
+    const int64_t n = p.rows * p.cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / p.cols, c = i % p.cols;
+        put_value(p.out, r, c, (p.flags[i] & kValid) ? p.sca[i] : p.nodata);
+    }
+}
+
+int64_t blocks_for(int64_t n, int num_sms) {
+    int64_t b = (n + kThreads - 1) / kThreads;
+    if (b > (int64_t)num_sms * 16) b = (int64_t)num_sms * 16;
+    return b < 1 ? 1 : b;
+}
+
+}  // namespace
+
+cudaError_t launch_mfd_weights(const MfdParams& p, int num_sms, cudaStream_t st) {
+    if (p.rows * p.cols == 0) return cudaSuccess;
+    mfd_weights_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(p.counts, 0, 4 * sizeof(int32_t), st);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(p.totals, 0, 4 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
+    sca_mfd_init_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms, cudaStream_t st) {
+    // a grid sized for the frontier the image can hold at once; the kernel strides
+    sca_mfd_round_kernel<<<(unsigned)num_sms * 4, kThreads, 0, st>>>(p, parity);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
+    sca_mfd_output_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace pargo

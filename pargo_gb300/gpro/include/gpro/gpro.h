@@ -92,6 +92,9 @@ private:
     CellCoord _nw, _se;
 };
 
+// The MPI rank (gpro/utility.h:227): always 0 in the one-process GPU build.
+int GetRank();
+
 // Process-wide GPU context (gpro/application.h).
 class Application {
 public:

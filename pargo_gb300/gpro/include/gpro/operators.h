@@ -1,6 +1,8 @@
 // operators.h -- the four focal operators of PaRGO with the reference's setter
 // API (apps/morphology/slope/slopeOperator.h, apps/hydrology/flowdird8/d8Operator.h,
-// apps/hydrology/pitremove/pitRemoveOperator.h, apps/hydrology/scad8/scaOperator.h);
+// apps/hydrology/pitremove/pitRemoveOperator.h, apps/hydrology/scad8/scaOperator.h),
+// TWI (apps/hydrology/twi/TWIOperator.h) and MFD-md (apps/hydrology/flowdirmfdmd/mfdOperator.h,
+// apps/hydrology/scamfdmd/scaOperator.h);
 // Run() is one call of the GPU C ABI on the layers' host buffers.
 #ifndef PARGO_GPRO_OPERATORS_H
 #define PARGO_GPRO_OPERATORS_H
@@ -113,12 +115,41 @@ public:
     // accumulation sweep) or PARGO_SCA_CONVERGED (the full upslope count);
     // the environment variable PARGO_SCA_CONTRACT=converged selects the latter.
     void contract(int c) { _contract = c; }
+    // The scamfdmd operator's input (apps/hydrology/scamfdmd/scaOperator.h:24):
+    // 8 MFD weight layers instead of a D8 layer; Run() then computes the MFD SCA.
+    void mfdLayer(vector<RasterLayer<double>*>& layerV) {
+        _weightLayers.assign(layerV.begin(), layerV.end());
+        for (RasterLayer<double>* l : _weightLayers) Configure(l, false);
+    }
     bool Run() override;
 
 protected:
     int _contract = -1;
     RasterLayer<double>* _pD8Layer = nullptr;
     RasterLayer<double>* _pSCALayer = nullptr;
+    vector<RasterLayer<double>*> _weightLayers;
+};
+
+// MFD-md flow partition (apps/hydrology/flowdirmfdmd/mfdOperator.h:13-40): 8
+// weight layers, layer i for window position i (i < 4) or i + 1.
+class MFDOperator : public RasterOperator<double> {
+public:
+    MFDOperator() : slpExp(0.0) {}
+    explicit MFDOperator(double pExp) : slpExp(pExp) {}
+    void demLayer(RasterLayer<double>& layerD) {
+        _pDEMLayer = &layerD;
+        Configure(_pDEMLayer, false);
+    }
+    void weightLayers(vector<RasterLayer<double>*>& layers) {
+        _weightLayers.assign(layers.begin(), layers.end());
+        for (RasterLayer<double>* l : _weightLayers) Configure(l, false);
+    }
+    bool Run() override;
+
+protected:
+    double slpExp;
+    RasterLayer<double>* _pDEMLayer = nullptr;
+    vector<RasterLayer<double>*> _weightLayers;
 };
 
 }  // namespace GPRO

@@ -12,6 +12,8 @@ typedef struct { int MPI_SOURCE, MPI_TAG, MPI_ERROR; } MPI_Status;
 #define MPI_INT 3
 #define MPI_DOUBLE 6
 #define MPI_LAND 1
+#define MPI_MAX 2
+#define MPI_SUM 3
 #define MPI_MAX_PROCESSOR_NAME 256
 #ifdef __cplusplus
 extern "C" {
@@ -23,6 +25,7 @@ int MPI_Comm_size(MPI_Comm comm, int* size);
 int MPI_Barrier(MPI_Comm comm);
 double MPI_Wtime(void);
 int MPI_Allreduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op op, MPI_Comm comm);
+int MPI_Reduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op op, int root, MPI_Comm comm);
 #ifdef __cplusplus
 }
 #endif

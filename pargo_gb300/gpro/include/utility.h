@@ -1,5 +1,5 @@
 // utility.h -- the helpers of the reference's gpro/utility.h that application
-// mains use (StringMatch, FileExists).
+// mains use (StringMatch, FileExists, SplitString).
 #ifndef PARGO_GPRO_UTILITY_H
 #define PARGO_GPRO_UTILITY_H
 #include "gpro/gpro.h"
@@ -16,4 +16,5 @@
 bool StringMatch(const char* a, const char* b);
 bool StringMatch(const string& a, const string& b);
 bool FileExists(string const& filename);
+vector<string> SplitString(const string& item, char delimiter);
 #endif

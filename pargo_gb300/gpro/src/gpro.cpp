@@ -98,6 +98,18 @@ bool PitRemoveOperator::Run() {
 }
 
 bool SCAOperator::Run() {
+    if (!_weightLayers.empty()) {  // the scamfdmd operator
+        if (_weightLayers.size() != 8 || !_pSCALayer) {
+            cerr << "SCAOperator::Run: 8 mfdLayer weight layers and scaLayer must be set" << endl;
+            return false;
+        }
+        pargo_ctx* ctx = Application::context();
+        if (!ctx) return false;
+        pargo_raster w[8], out = _pSCALayer->abi_raster();
+        for (int i = 0; i < 8; i++) w[i] = _weightLayers[i]->abi_raster();
+        return report_status(pargo_sca_mfd(ctx, w, &out, &_weightLayers[0]->nbrhood()->abi(), nullptr),
+                             "SCAOperator::Run");
+    }
     if (!_pD8Layer || !_pSCALayer) {
         cerr << "SCAOperator::Run: d8Layer and scaLayer must be set" << endl;
         return false;
@@ -113,6 +125,18 @@ bool SCAOperator::Run() {
     return report_status(pargo_sca(ctx, &d8, &out, &_pD8Layer->nbrhood()->abi(), c, nullptr), "SCAOperator::Run");
 }
 
+bool MFDOperator::Run() {
+    if (!_pDEMLayer || _weightLayers.size() != 8) {
+        cerr << "MFDOperator::Run: demLayer and 8 weightLayers must be set" << endl;
+        return false;
+    }
+    pargo_ctx* ctx = Application::context();
+    if (!ctx) return false;
+    pargo_raster dem = _pDEMLayer->abi_raster(), w[8];
+    for (int i = 0; i < 8; i++) w[i] = _weightLayers[i]->abi_raster();
+    return report_status(pargo_mfd(ctx, &dem, w, &_pDEMLayer->nbrhood()->abi(), slpExp, nullptr), "MFDOperator::Run");
+}
+
 bool TWIOperator::Run() {
     if (!_pSCALayer || !_pSlopeLayer || !_pTWILayer) {
         cerr << "TWIOperator::Run: SCALayer, slopeLayer and twiLayer must be set" << endl;
@@ -124,10 +148,23 @@ bool TWIOperator::Run() {
     return report_status(pargo_twi(ctx, &sl, &sa, &out, &_pSCALayer->nbrhood()->abi(), nullptr), "TWIOperator::Run");
 }
 
+int GetRank() { return 0; }
+
 }  // namespace GPRO
 
 bool StringMatch(const char* a, const char* b) { return strcasecmp(a, b) == 0; }
 bool StringMatch(const string& a, const string& b) { return strcasecmp(a.c_str(), b.c_str()) == 0; }
+vector<string> SplitString(const string& item, char delimiter) {
+    vector<string> out;
+    size_t start = 0;
+    while (start < item.size()) {  // fields as getline() yields them: no trailing empty field
+        size_t end = item.find(delimiter, start);
+        if (end == string::npos) end = item.size();
+        out.push_back(item.substr(start, end - start));
+        start = end + 1;
+    }
+    return out;
+}
 bool FileExists(string const& filename) {
     struct stat st;
     return stat(filename.c_str(), &st) == 0 && S_ISREG(st.st_mode);
@@ -154,5 +191,8 @@ int MPI_Allreduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op, MPI_Com
     const size_t sz = t == MPI_DOUBLE ? 8 : 4;
     if (s != r) memcpy(r, s, sz * (size_t)n);
     return MPI_SUCCESS;
+}
+int MPI_Reduce(const void* s, void* r, int n, MPI_Datatype t, MPI_Op op, int, MPI_Comm c) {
+    return MPI_Allreduce(s, r, n, t, op, c);
 }
 }

@@ -20,7 +20,7 @@ def _link_args():
 
 
 def test_apps_are_built():
-    for app in ("pargo_slope", "pargo_d8", "pargo_pitremove", "pargo_sca", "pargo_twi"):
+    for app in ("pargo_slope", "pargo_d8", "pargo_pitremove", "pargo_sca", "pargo_twi", "pargo_mfd", "pargo_sca_mfd"):
         assert os.access(os.path.join(_paths.BIN_DIR, app), os.X_OK), app
     assert os.path.exists(_paths.GPRO_SO)
 
@@ -45,7 +45,8 @@ def test_tiff_written_by_python_reads_in_cpp_and_back(tmp_path):
 
 @pytest.mark.parametrize("main", ["apps/morphology/slope/pSlope.cpp", "apps/hydrology/flowdird8/pD8.cpp",
                                   "apps/hydrology/pitremove/pPitRemove.cpp", "apps/hydrology/scad8/pSCA.cpp",
-                                  "apps/hydrology/twi/pTWI.cpp"])
+                                  "apps/hydrology/twi/pTWI.cpp", "apps/hydrology/flowdirmfdmd/pMFDmd.cpp",
+                                  "apps/hydrology/scamfdmd/pSCA.cpp"])
 def test_reference_main_compiles_against_gpu_gpro(main, tmp_path):
     """The reference's application main, byte for byte, built against the GPU
     gpro headers (copied to a scratch directory so that its quoted includes of

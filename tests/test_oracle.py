@@ -134,3 +134,23 @@ def test_oracle_twi_matches_reference_binary(seed, shape, oracle_lib):
     ref = R.twi(sl, sca, -9999.0, 30.0)
     assert bits_equal(O.twi(sl, sca, -9999.0), ref)
     assert (ref == -9999.0).any() and np.isfinite(ref).all()
+
+
+@pytest.mark.parametrize("slp_exp", [-1.0, 0.0, 0.5, 1.0])
+def test_oracle_mfd_matches_reference_binary(slp_exp, oracle_lib):
+    """MFD-md weights (MFDOperator) and the MFD SCA (the scamfdmd operator's
+    single accumulation sweep) against the reference built from its sources,
+    bit for bit, on a filled DEM with nodata and flats; -1 is pMFDmd's default
+    exponent."""
+    from pargo_gb300 import synth
+    R = _ref()
+    if R.mfd_lib is None:
+        pytest.skip("MFD-md reference build absent")
+    O = oracle_lib
+    dem = synth.hydro_dem(83, 117, seed=71, blob_fraction=0.05)
+    w = O.fill(dem, -9999.0).astype(np.float32)
+    w[40:44, 50:60] = w[40, 50]   # an exact flat
+    a = O.mfd(w, -9999.0, 30.0, slp_exp)
+    b = R.mfd(w, -9999.0, 30.0, slp_exp)
+    assert bits_equal(a.reshape(8, -1), b.reshape(8, -1))
+    assert bits_equal(O.sca_mfd(b, -9999.0), R.sca_mfd(b, -9999.0))
