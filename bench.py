@@ -573,6 +573,95 @@ def run_grad(args, ws, rank, local, side=8192):
     }
 
 
+def run_mfd(args, ws, rank, local, side=8192):
+    """MFD-md: flow partition weights (exponent 1.1) of the pit-removed side^2
+    hydro DEM (seed 1, 30 m cells; levels float64, filled untimed on the GPU)
+    into 8 float32 layers, then the MFD SCA of those layers (float64).  A step
+    is one pargo_mfd call and one pargo_sca_mfd call."""
+    import torch
+    from pargo_gb300 import abi
+    torch.cuda.set_device(local)
+    ctx = abi.Context(local)
+    dem = make_hydro(side, side)
+    cells = side * side
+    stream = torch.cuda.current_stream()
+    R = abi.raster
+    d = torch.from_numpy(dem).cuda()
+    del dem
+    lv = torch.empty((side, side), dtype=torch.float64, device="cuda")
+    ctx.hydro_pipeline(R(d, ND, 30.0), wdem=R(lv, ND), gap=1e-3, stream=stream)
+    del d
+    ws_dev = [torch.empty((side, side), dtype=torch.float32, device="cuda") for _ in range(8)]
+    out = torch.empty((side, side), dtype=torch.float64, device="cuda")
+    rl, rw, ro = R(lv, ND, 30.0), [R(w, ND) for w in ws_dev], R(out, ND)
+
+    def weights():
+        ctx.mfd(rl, rw, slp_exp=1.1, stream=stream)
+
+    def sca():
+        ctx.sca_mfd(rw, ro, stream=stream)
+
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed_steps(lambda: (weights(), sca()), args, stream)
+    clk = clocks.stop()
+    ms_w = timed_steps(weights, argparse.Namespace(steps=args.steps, warmup=1), stream)
+    ms_s = timed_steps(sca, argparse.Namespace(steps=args.steps, warmup=1), stream)
+    ms = max_over_ranks(ms, ws, torch.device("cuda", local))
+    # end to end with host buffers: float64 levels in, 8 float32 layers and float64 SCA out
+    hl = lv.cpu().pin_memory()
+    hw = [torch.empty((side, side), dtype=torch.float32).pin_memory() for _ in range(8)]
+    ho = torch.empty((side, side), dtype=torch.float64).pin_memory()
+    rhl, rhw, rho = R(hl, ND, 30.0), [R(w, ND) for w in hw], R(ho, ND)
+
+    def e2e():
+        ctx.mfd(rhl, rhw, slp_exp=1.1, stream=stream)
+        ctx.sca_mfd(rhw, rho, stream=stream)
+
+    e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, ws, torch.device("cuda", local))
+    cpu = None
+    if rank == 0 and ws == 1:
+        import oracle
+        O = oracle.Oracle()
+        a = hl.numpy()
+        n = 1024
+        r0, c0 = (side - n) // 2, (side - n) // 2
+        crop = np.ascontiguousarray(a[r0:r0 + n, c0:c0 + n])
+        t0 = time.perf_counter()
+        O.sca_mfd(O.mfd(crop, ND, 30.0, 1.1), ND)
+        dt = time.perf_counter() - t0
+        cpu = {"value": round(crop.size / dt / 1e6, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
+               "sample": "1024x1024 crop of the same levels: the oracle's MFD-md weights + one-sweep MFD SCA "
+                         "(serial, as the reference), %.2f s" % dt}
+    peak, kind = hbm_peak()
+    achieved = cells * 40.0 / (ms_w * 1e-3) / 1e9
+    return {
+        "metric": "Mcells/s MFD-md weights + MFD SCA", "value": round(ws * cells / (ms * 1e-3) / 1e6, 1),
+        "unit": "Mcells/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 weights, f64 SCA sums", "data": "synthetic",
+        "config": {"workload": "mfd%d: MFD-md weights (exponent 1.1) + MFD SCA on the pit-removed %dx%d hydro "
+                               "DEM (seed 1, 30 m cells, float64 levels), 8 float32 layers, float64 SCA"
+                               % (side, side, side), "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "kernel": "mfd_weights_kernel", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
+                     "traffic": None, "algorithmic_bytes_per_cell": 40, "weights_ms": round(ms_w, 3),
+                     "sca_ms": round(ms_s, 3)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells * 8,
+                "d2h_bytes_per_step": cells * (32 + 8)},
+        "gpu_launches": None, "clocks": clk,
+    }
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
@@ -606,7 +695,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hydro8192",
                     choices=["hydro8192", "hydro2048", "slope32768", "slope8192", "slope1024", "batch512",
-                             "sca16384", "sca4096", "grad8192"])
+                             "sca16384", "sca4096", "grad8192", "mfd8192", "mfd2048"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()
@@ -616,6 +705,8 @@ def main():
         out = run_hydro(args, ws, rank, local, int(args.workload[5:]))
     elif args.workload.startswith("sca"):
         out = run_sca(args, ws, rank, local, int(args.workload[3:]))
+    elif args.workload.startswith("mfd"):
+        out = run_mfd(args, ws, rank, local, int(args.workload[3:]))
     elif args.workload == "grad8192":
         out = run_grad(args, ws, rank, local)
     elif args.workload == "batch512":

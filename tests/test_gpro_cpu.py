@@ -41,6 +41,10 @@ def test_tiff_written_by_python_reads_in_cpp_and_back(tmp_path):
     write_tiff(str(tmp_path / "p.tif"), a, -9999.0, 25.0)
     b, nd, cs = read_tiff(str(tmp_path / "p.tif"))
     assert np.array_equal(a, b) and nd == -9999.0 and cs == 25.0
+    d = a.astype(np.float64) + 1e-9          # float64 stays float64
+    write_tiff(str(tmp_path / "d.tif"), d, -9999.0, 25.0)
+    e, _, _ = read_tiff(str(tmp_path / "d.tif"))
+    assert e.dtype == np.float64 and np.array_equal(d, e)
 
 
 @pytest.mark.parametrize("main", ["apps/morphology/slope/pSlope.cpp", "apps/hydrology/flowdird8/pD8.cpp",

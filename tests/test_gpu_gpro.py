@@ -77,6 +77,29 @@ def test_app_twi_after_the_chain(case, tmp_path, oracle_lib):
     assert (np.abs(t[ok] - ref[ok]) <= 1e-6 * np.abs(ref[ok]) + 1e-6).all()
 
 
+@pytest.mark.parametrize("case", ["demtif", "fbm_hydro"])
+def test_app_mfd_then_sca_mfd(case, tmp_path, oracle_lib):
+    """pMFDmd's and scamfdmd's steps on the filled DEM: the 8 weight files
+    against the oracle (pinned to MFDOperator) within 1e-5 relative + 1e-6,
+    then the MFD SCA of those files bit for bit against the oracle's sweep."""
+    g = load_golden(case)
+    nd, cs = float(g["nodata"]), float(g["cellsize"])
+    nbr = tmp_path / "moore.nbr"
+    nbr.write_text(MOORE)
+    write_tiff(str(tmp_path / "fill.tif"), g["fill"], nd, cs)
+    prefix = str(tmp_path / "mfd_")
+    run("pargo_mfd", "-elev", tmp_path / "fill.tif", "-nbr", nbr, "-out", prefix, "-exp", 1.1)
+    files = [prefix + "weightLayer%d.tif" % (i if i < 4 else i + 1) for i in range(8)]
+    w = np.stack([read_tiff(f)[0] for f in files]).astype(np.float64)
+    ref = oracle_lib.mfd(g["fill"], nd, cs, 1.1)
+    assert np.array_equal(w == nd, ref == nd) and np.array_equal(w == 0, ref == 0)
+    ok = ref != nd
+    assert (np.abs(w[ok] - ref[ok]) <= 1e-5 * np.abs(ref[ok]) + 1e-6).all()
+    run("pargo_sca_mfd", ",".join(files), nbr, tmp_path / "sca.tif")
+    sca, snd, _ = read_tiff(str(tmp_path / "sca.tif"))
+    assert snd == nd and bits_equal(sca, oracle_lib.sca_mfd(w, nd))
+
+
 def test_app_rejects_bad_neighbourhood(tmp_path):
     g = load_golden("fbm_slope")
     dem = tmp_path / "dem.tif"

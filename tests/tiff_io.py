@@ -33,8 +33,10 @@ def read_tiff(path):
 
 
 def write_tiff(path, arr, nodata, cellsize, origin=(0.0, 0.0)):
-    """float32 single-strip GeoTIFF with pixel scale, tiepoint and GDAL_NODATA."""
-    a = np.ascontiguousarray(arr, np.float32)
+    """Single-strip GeoTIFF with pixel scale, tiepoint and GDAL_NODATA: float64
+    for a float64 array, float32 otherwise."""
+    f64 = np.asarray(arr).dtype == np.float64
+    a = np.ascontiguousarray(arr, np.float64 if f64 else np.float32)
     rows, cols = a.shape
     nd = ("%.17g" % nodata).encode() + b"\0"
     entries = []  # (tag, type, count, payload bytes)
@@ -43,7 +45,7 @@ def write_tiff(path, arr, nodata, cellsize, origin=(0.0, 0.0)):
         entries.append((tag, typ, count, payload))
     add(256, 4, 1, struct.pack("<I", cols))
     add(257, 4, 1, struct.pack("<I", rows))
-    add(258, 3, 1, struct.pack("<H", 32))
+    add(258, 3, 1, struct.pack("<H", 64 if f64 else 32))
     add(259, 3, 1, struct.pack("<H", 1))
     add(262, 3, 1, struct.pack("<H", 1))
     add(273, 4, 1, b"\0\0\0\0")
@@ -71,6 +73,6 @@ def write_tiff(path, arr, nodata, cellsize, origin=(0.0, 0.0)):
             payload = struct.pack("<I", data_off)
         out += struct.pack("<HHI", tag, typ, count)
         out += struct.pack("<I", o) if o is not None else payload.ljust(4, b"\0")
-    out += struct.pack("<I", 0) + extra + a.astype("<f4").tobytes()
+    out += struct.pack("<I", 0) + extra + a.astype("<f8" if f64 else "<f4").tobytes()
     with open(path, "wb") as fh:
         fh.write(out)
