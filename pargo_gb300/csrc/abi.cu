@@ -39,7 +39,7 @@ struct pargo_ctx {
     // pinned host scratch (counter read-back, table staging)
     void* pinned = nullptr;
     size_t pinned_n = 0;
-    unsigned long long* d_counters = nullptr;  // [0] fallbacks [1] visits [2] changed [3] raised
+    unsigned long long* d_counters = nullptr;  // [0] fallbacks [1] visits [2] changed [3] raised [4,5] strip walk
     int* d_error = nullptr;
     int64_t last_fallbacks = 0;
     // fill graph cache
@@ -59,7 +59,7 @@ enum SlotId {
     kSlotScaIndeg, kSlotScaConv, kSlotScaShip, kSlotScaFlags, kSlotScaCounters, kSlotBatchMaps,
     kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut,
     kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotMfdLayer0,
-    kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotCount
+    kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotStripSlow, kSlotCount
 };
 static_assert(kSlotCount <= 48, "context slot table");
 
@@ -420,6 +420,31 @@ int pick_variant(pargo_ctx* ctx, int64_t cells) {
     return v >= 0 ? v : 0;
 }
 
+// Slope + D8 over a float32 DEM with TMA-compatible rows by kernel variant v
+// (a tiled variant, or the strip walk with its fix-up pass).
+pargo_status launch_focal_variant(pargo_ctx* ctx, const InView& dem, const FocalParams& p, int fast_out, int v,
+                                  cudaStream_t s) {
+    pargo_status st;
+    const bool strip = focal_variant_is_strip(v) && fast_out && p.rows * ((p.cols + 3) / 4) < (1LL << 32);
+    if (strip) {
+        CUtensorMap ms, mp;
+        if ((st = make_tma_map(ctx, &ms, dem.base, p.rows, p.cols, dem.pitch, focal_strip_stage_rows())) != PARGO_OK)
+            return st;
+        if ((st = make_tma_map(ctx, &mp, dem.base, p.rows, p.cols, dem.pitch, 2)) != PARGO_OK) return st;
+        cudaError_t e;
+        uint32_t* slow = (uint32_t*)slot(ctx, kSlotStripSlow, focal_strip_slow_bytes(p.rows, p.cols), &e);
+        if (!slow) return cuda_fail(ctx, e, "strip walk scratch");
+        CU(ctx, launch_focal_strip(&ms, &mp, dem, p, fast_out, &ctx->d_counters[4], slow, ctx->num_sms, s));
+        return PARGO_OK;
+    }
+    if (focal_variant_is_strip(v)) v = 0;
+    CUtensorMap map;
+    if ((st = make_tma_map(ctx, &map, dem.base, p.rows, p.cols, dem.pitch, focal_variant_rows(v) + 2)) != PARGO_OK)
+        return st;
+    CU(ctx, launch_focal_tma(&map, p, fast_out, v, ctx->num_sms, s));
+    return PARGO_OK;
+}
+
 pargo_status focal_impl(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
                         const pargo_nbr* nbr, int method, int units, int dir_type, void* stream) {
     if (!ctx) return PARGO_ERR_INVALID_ARG;
@@ -482,11 +507,7 @@ pargo_status focal_impl(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* s
         CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s));
     } else if (tma_ok(sdem.in)) {
         const int v = pick_variant(ctx, p.rows * p.cols);
-        CUtensorMap map;
-        if ((st = make_tma_map(ctx, &map, sdem.in.base, p.rows, p.cols, sdem.in.pitch, focal_variant_rows(v) + 2)) !=
-            PARGO_OK)
-            return st;
-        CU(ctx, launch_focal_tma(&map, p, fast_out_ok(p) ? 1 : 0, v, ctx->num_sms, s));
+        if ((st = launch_focal_variant(ctx, sdem.in, p, fast_out_ok(p) ? 1 : 0, v, s)) != PARGO_OK) return st;
     } else {
         CU(ctx, launch_focal_generic(sdem.in, p, s));
     }
@@ -644,13 +665,12 @@ pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps,
     p.error_flag = ctx->d_error;
     float best_ms = 1e30f;
     int best_v = 0;
+    const InView din{(const char*)dem->data, pitch_of(dem), PARGO_F32};
     for (int v = 0; v < focal_num_variants(); v++) {
-        CUtensorMap map;
-        if ((st = make_tma_map(ctx, &map, dem->data, rows, cols, pitch_of(dem), focal_variant_rows(v) + 2)) != PARGO_OK)
-            return st;
-        CU(ctx, launch_focal_tma(&map, p, 1, v, ctx->num_sms, ctx->own));  // warm
+        if ((st = launch_focal_variant(ctx, din, p, 1, v, ctx->own)) != PARGO_OK) return st;  // warm
         CU(ctx, cudaEventRecord(ctx->ev_t0, ctx->own));
-        for (int r = 0; r < reps; r++) CU(ctx, launch_focal_tma(&map, p, 1, v, ctx->num_sms, ctx->own));
+        for (int r = 0; r < reps; r++)
+            if ((st = launch_focal_variant(ctx, din, p, 1, v, ctx->own)) != PARGO_OK) return st;
         CU(ctx, cudaEventRecord(ctx->ev_t1, ctx->own));
         CU(ctx, cudaEventSynchronize(ctx->ev_t1));
         float ms = 0.0f;

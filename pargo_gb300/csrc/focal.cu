@@ -535,6 +535,310 @@ __global__ void __launch_bounds__(256) batch_generic_kernel(const FocalParams* p
     count_fallbacks(fell_back, fallbacks);
 }
 
+// ------------------------------------------------------------ strip walk --
+// Warp-independent form of the same computation.  Each warp walks a 128-cell
+// wide column strip down a segment of kSegRows rows, keeping the three-row
+// window and the per-row / per-row-pair differences in registers from one
+// row to the next (no tile prologue, no re-read halo rows), with a private
+// pipeline of TMA stages: a 2-row priming box per segment, then kSegStages
+// boxes of kSR rows, double-buffered and waited on by mbarrier.  Segments
+// are claimed from a device counter, so strips whose lanes fall back to the
+// general path often (the raster's left and right edges) do not stretch the
+// launch.  The row loop is unrolled by three with the registers' roles
+// rotated (above / centre / below), so no register is copied from row to row.
+constexpr int kSR = 6;                                      // rows per stage (a multiple of 3)
+constexpr int kSegStages = 8;                               // stages per segment
+constexpr int kSegRows = kSR * kSegStages;                  // output rows per segment
+constexpr int kSStageBytes = kBoxW * kSR * 4;               // 3264
+constexpr int kSStageStride = (kSStageBytes + 127) / 128 * 128;
+constexpr int kSPrimeBytes = kBoxW * 2 * 4;                 // 1088
+constexpr int kSPrimeStride = (kSPrimeBytes + 127) / 128 * 128;
+constexpr int kSWarpBytes = 2 * kSStageStride + 2 * kSPrimeStride;
+constexpr int kSWarps = 4;
+
+__device__ __forceinline__ float fmax3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float fmin3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// d8_fast with the maximum taken by three-input max (the same value).
+__device__ __forceinline__ int d8_fast3(float x0, float x1, float x2, float x3, float x5, float x6, float x7,
+                                        float x8) {
+    const float m = fmax3f(fmax3f(x0, x1, x2), fmax3f(x3, x5, x6), fmaxf(x7, x8));
+    const float t = __fadd_rn(__fmaf_rn(m, -k2m19, m), -kTHi);
+    const uint32_t ua = prmt(prmt(__float_as_uint(__fsub_rn(t, x0)), __float_as_uint(__fsub_rn(t, x1)), 0x00FB),
+                             prmt(__float_as_uint(__fsub_rn(t, x2)), __float_as_uint(__fsub_rn(t, x3)), 0x00FB), 0x5410);
+    const uint32_t ub = prmt(prmt(__float_as_uint(__fsub_rn(t, x5)), __float_as_uint(__fsub_rn(t, x6)), 0x00FB),
+                             prmt(__float_as_uint(__fsub_rn(t, x7)), __float_as_uint(__fsub_rn(t, x8)), 0x00FB), 0x5410);
+    const uint32_t w = (ua & 0x55555555u) | (ub & 0xAAAAAAAAu);
+    const int hb = 31 - __clz(w);
+    const int k = (hb >> 3) + (hb & 1) * 5;
+    return m < kLowCut ? -1 : (m > kHighCut && __popc(w) == 4) ? k : kD8Unsure;
+}
+
+__device__ __forceinline__ bool row6_maybe_nodata(const float v[6], const Band<float>& b) {
+    const float mn = fminf(fmin3f(v[0], v[1], v[2]), fmin3f(v[3], v[4], v[5]));
+    if (b.hi < 0.0f) return mn <= b.hi;
+    const float mx = fmaxf(fmax3f(v[0], v[1], v[2]), fmax3f(v[3], v[4], v[5]));
+    return mn <= b.hi && mx >= b.lo;
+}
+
+// One window row: this lane's six values (columns 4l-1 .. 4l+4 of the strip),
+// its two-apart differences (Horn x numerator) and whether it may hold nodata.
+struct SRow {
+    float v[6];
+    float sh[4];
+    bool nd;
+};
+// Differences between a row (U) and the row below it (L), each serving the
+// two cells it joins: vd[j] = U - L in column j (S of U, -N of L);
+// e1[a] = (U[a] - L[a+1]) / sqrt 2 (SE of U[a], -NW of L[a+1]);
+// e2[a] = (U[a+1] - L[a]) / sqrt 2 (SW of U[a+1], -NE of L[a]).
+struct SPair {
+    float vd[4];
+    float e1[5];
+    float e2[5];
+};
+
+__device__ __forceinline__ void s_load_row(const float* row, int lane, SRow& r, const Band<float>& nd6) {
+    const float* q = row + 4 * lane + 3;
+    const float4 c = *reinterpret_cast<const float4*>(q + 1);
+    r.v[0] = q[0]; r.v[1] = c.x; r.v[2] = c.y; r.v[3] = c.z; r.v[4] = c.w; r.v[5] = q[5];
+#pragma unroll
+    for (int j = 0; j < 4; j++) r.sh[j] = __fsub_rn(r.v[j + 2], r.v[j]);
+    r.nd = row6_maybe_nodata(r.v, nd6);
+}
+
+__device__ __forceinline__ void s_pair(const SRow& u, const SRow& l, SPair& p) {
+    const float kinv = 0.70710677f;
+#pragma unroll
+    for (int j = 0; j < 4; j++) p.vd[j] = __fsub_rn(u.v[j + 1], l.v[j + 1]);
+#pragma unroll
+    for (int a = 0; a < 5; a++) {
+        p.e1[a] = __fmul_rn(__fsub_rn(u.v[a], l.v[a + 1]), kinv);
+        p.e2[a] = __fmul_rn(__fsub_rn(u.v[a + 1], l.v[a]), kinv);
+    }
+}
+
+// Where the fast path cannot finish a lane's four cells of a row (the ring,
+// windows that may touch nodata, uncertain D8, lanes at the raster's edge),
+// the (row, lane) goes to a device list -- index y * lanes_per_row + gx0 / 4,
+// appended once per warp by a single atomic -- and strip_fixup_kernel
+// recomputes those cells afterwards through the general path.
+struct SlowList {
+    uint32_t* items;
+    unsigned long long* count;
+    int64_t lanes_per_row;  // ceil(cols / 4)
+};
+
+// Output row y from the window rows A (y-1), B (y), C (y+1); C is loaded
+// here from stage row `crow`, and the pair B/C is formed for the next row.
+template <bool SLOPE, bool D8>
+__device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, SRow& C, const SPair& PAB, SPair& PBC,
+                                           int64_t y, int64_t gx0, bool lane_int, const FocalParams& p, int lane,
+                                           const SlowList& slow) {
+    s_load_row(crow, lane, C, p.nd6f);
+    s_pair(B, C, PBC);
+    float sl[4];
+    int cd[4];
+    if (SLOPE) {
+        float sv[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) sv[a] = __fsub_rn(A.v[a], C.v[a]);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float nx = __fmaf_rn(2.0f, B.sh[j], __fadd_rn(A.sh[j], C.sh[j]));
+            const float ny = __fmaf_rn(2.0f, sv[j + 1], __fadd_rn(sv[j], sv[j + 2]));
+            sl[j] = horn_slope(nx, ny, p.sk.k_fd);
+            if (p.sk.degrees) sl[j] = atanf(sl[j]) * 57.29577951308232f;
+        }
+    }
+    bool unsure = false;
+    if (D8) {
+        float hd[5];
+#pragma unroll
+        for (int a = 0; a < 5; a++) hd[a] = __fsub_rn(B.v[a + 1], B.v[a]);
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            cd[j] = d8_fast3(-PAB.e1[j], -PAB.vd[j], -PAB.e2[j + 1], hd[j], -hd[j + 1], PBC.e2[j], PBC.vd[j],
+                             PBC.e1[j + 1]);
+            unsure |= cd[j] == kD8Unsure;
+        }
+        if (p.dir_type != 8) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) cd[j] = d8_weight(cd[j]);
+        }
+    }
+    if (y >= p.rows) return;
+    const bool rb = !lane_int || (uint64_t)(y - 1) >= (uint64_t)(p.rows - 2) || A.nd || B.nd || C.nd || unsure;
+    if (!rb) {
+        if (SLOPE)
+            *reinterpret_cast<float4*>(p.slope.base + y * p.slope.pitch + 4 * gx0) = make_float4(sl[0], sl[1], sl[2], sl[3]);
+        if (D8)
+            *reinterpret_cast<uint32_t*>(p.d8.base + y * p.d8.pitch + gx0) =
+                __byte_perm(__byte_perm((uint32_t)cd[0], (uint32_t)cd[1], 0x0040),
+                            __byte_perm((uint32_t)cd[2], (uint32_t)cd[3], 0x0040), 0x5410);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, rb && gx0 < p.cols);
+    if (m) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(slow.count, (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (rb && gx0 < p.cols)
+            slow.items[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)(y * slow.lanes_per_row + (gx0 >> 2));
+    }
+}
+
+// Warp-uniform bounded wait on an mbarrier phase.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
+    const bool ok = mbar_wait_bounded(bar, parity, kWaitBudget);
+    return __all_sync(0xffffffffu, ok);
+}
+
+template <bool SLOPE, bool D8>
+__global__ void __launch_bounds__(kSWarps * 32, 5) focal_strip_kernel(const __grid_constant__ CUtensorMap map_stage,
+                                                                       const __grid_constant__ CUtensorMap map_prime,
+                                                                       const __grid_constant__ FocalParams p,
+                                                                       int64_t nstrips, int64_t nsegs,
+                                                                       unsigned long long* claim, SlowList slow) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[kSWarps][4];  // stage 0, stage 1, prime 0, prime 1
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wbase = smem + warp * kSWarpBytes;
+    auto stage = [&](int b) { return reinterpret_cast<float*>(wbase + b * kSStageStride); };
+    auto prime = [&](int b) { return reinterpret_cast<float*>(wbase + 2 * kSStageStride + b * kSPrimeStride); };
+    uint64_t* bar = bars[warp];
+    if (lane == 0) {
+        tma_prefetch_desc(&map_stage);
+        tma_prefetch_desc(&map_prime);
+        for (int i = 0; i < 4; i++) mbar_init(&bar[i], 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    const int64_t box_y_max = p.rows - 1;  // a box always starts inside the raster
+    auto claim_seg = [&]() -> int64_t {
+        unsigned long long v = 0;
+        if (lane == 0) v = atomicAdd(claim, 1ULL);
+        return (int64_t)__shfl_sync(0xffffffffu, v, 0);
+    };
+    auto issue_prime = [&](int64_t seg, int buf) {
+        if (lane == 0) {
+            const int64_t x0 = (seg % nstrips) * kTW, y0 = (seg / nstrips) * kSegRows;
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[2 + buf], kSPrimeBytes);
+            tma_load_2d(prime(buf), &map_prime, (int32_t)(x0 - 4), (int32_t)(y0 - 1), &bar[2 + buf]);
+        }
+    };
+    auto issue_stage = [&](int64_t seg, int k, int buf) {
+        if (lane == 0) {
+            const int64_t x0 = (seg % nstrips) * kTW, y0 = (seg / nstrips) * kSegRows;
+            int64_t yb = y0 + 1 + (int64_t)k * kSR;
+            if (yb > box_y_max) yb = box_y_max;  // rows past the raster: never stored
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[buf], kSStageBytes);
+            tma_load_2d(stage(buf), &map_stage, (int32_t)(x0 - 4), (int32_t)yb, &bar[buf]);
+        }
+    };
+
+    int64_t cur = claim_seg();
+    if (cur >= nsegs) return;
+    issue_prime(cur, 0);
+    issue_stage(cur, 0, 0);
+    issue_stage(cur, 1, 1);
+    uint32_t sphase = 0, pphase = 0;
+    int pb = 0;
+    SRow A, B, C;
+    SPair PAB, PBC, PCA;
+    while (true) {
+        const int64_t x0 = (cur % nstrips) * kTW, y0 = (cur / nstrips) * kSegRows;
+        const int64_t gx0 = x0 + 4 * lane;
+        const bool lane_int = p.fd && p.fast_out && gx0 >= 1 && gx0 + 4 <= p.cols - 1;
+        int64_t nxt = nsegs;
+        if (!warp_wait(&bar[2 + pb], (pphase >> pb) & 1u)) {
+            if (lane == 0 && p.error_flag) atomicExch(p.error_flag, 1);
+            return;
+        }
+        pphase ^= 1u << pb;
+        s_load_row(prime(pb), lane, A, p.nd6f);
+        s_load_row(prime(pb) + kBoxW, lane, B, p.nd6f);
+        s_pair(A, B, PAB);
+#pragma unroll 1
+        for (int k = 0; k < kSegStages; k++) {
+            const int buf = k & 1;
+            if (!warp_wait(&bar[buf], (sphase >> buf) & 1u)) {
+                if (lane == 0 && p.error_flag) atomicExch(p.error_flag, 1);
+                return;
+            }
+            sphase ^= 1u << buf;
+#pragma unroll 1
+            for (int t = 0; t < kSR; t += 3) {
+                const float* st = stage(buf) + t * kBoxW;
+                const int64_t y = y0 + (int64_t)k * kSR + t;
+                strip_step<SLOPE, D8>(st, A, B, C, PAB, PBC, y, gx0, lane_int, p, lane, slow);
+                strip_step<SLOPE, D8>(st + kBoxW, B, C, A, PBC, PCA, y + 1, gx0, lane_int, p, lane, slow);
+                strip_step<SLOPE, D8>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, gx0, lane_int, p, lane, slow);
+            }
+            __syncwarp();
+            // refill this buffer with the item two ahead
+            if (k + 2 < kSegStages) {
+                issue_stage(cur, k + 2, buf);
+            } else {
+                if (k + 2 == kSegStages) {
+                    nxt = claim_seg();
+                    if (nxt < nsegs) issue_prime(nxt, pb ^ 1);
+                }
+                if (nxt < nsegs) issue_stage(nxt, k + 2 - kSegStages, buf);
+            }
+        }
+        if (nxt >= nsegs) break;
+        cur = nxt;
+        pb ^= 1;
+    }
+}
+
+// The (row, lane) items the strip walk left: each lane's four cells through
+// cell_general on the window read from the DEM.
+__global__ void __launch_bounds__(128) strip_fixup_kernel(const InView dem, const __grid_constant__ FocalParams p,
+                                                          const SlowList slow) {
+    const unsigned long long n = *((volatile unsigned long long*)slow.count);
+    int fell_back = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint32_t e = slow.items[i];
+        const int64_t y = (int64_t)(e / (uint64_t)slow.lanes_per_row);
+        const int64_t gx0 = (int64_t)(e % (uint64_t)slow.lanes_per_row) * 4;
+#pragma unroll 1
+        for (int j = 0; j < 4; j++) {
+            const int64_t gx = gx0 + j;
+            if (gx >= p.cols) break;
+            const bool ring = y <= 0 || gx <= 0 || y >= p.rows - 1 || gx >= p.cols - 1;
+            float z[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (!ring) {
+#pragma unroll
+                for (int q = 0; q < 9; q++)
+                    z[q] = reinterpret_cast<const float*>(dem.base + (y + q / 3 - 1) * dem.pitch)[gx + q % 3 - 1];
+            }
+            const CellOut o = cell_general<float>(z[0], z[1], z[2], z[3], z[4], z[5], z[6], z[7], z[8], &p, ring);
+            fell_back += (o.flags >> 2) & 1;
+            if (p.do_slope) {
+                if (o.flags & 1) put_value(p.slope, y, gx, p.slope.nodata);
+                else put_float(p.slope, y, gx, o.slope);
+            }
+            if (p.do_d8) {
+                if (o.flags & 2) put_value(p.d8, y, gx, p.d8.nodata);
+                else put_int(p.d8, y, gx, o.code);
+            }
+        }
+    }
+    count_fallbacks(fell_back, p.fallbacks);
+}
+
 }  // namespace
 
 // Kernel variants the autotuner chooses among (tile rows = 4 x ROWS).
@@ -544,7 +848,9 @@ struct Variant {
 static const Variant kVariants[] = {{8, 1, 5}, {6, 1, 6}, {6, 1, 7}, {4, 1, 8}, {8, 1, 6}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-int focal_num_variants() { return kNumVariants; }
+// Variant kNumVariants is the strip walk (launch_focal_strip).
+int focal_num_variants() { return kNumVariants + 1; }
+bool focal_variant_is_strip(int v) { return v == kNumVariants; }
 int focal_variant_rows(int v) { return kWarps * kVariants[(v >= 0 && v < kNumVariants) ? v : 0].rows; }
 size_t focal_tma_smem_bytes() { return 2 * Shape<kBatchRows>::kStageStride; }
 int focal_tma_tile_rows() { return Shape<kBatchRows>::kTH; }
@@ -582,6 +888,53 @@ static cudaError_t launch_variants(const CUtensorMap* map, const FocalParams& p,
         case 4: return launch_variant<8, 1, 6, SLOPE, D8>(map, p, num_sms, s);
         default: return launch_variant<8, 1, 5, SLOPE, D8>(map, p, num_sms, s);
     }
+}
+
+int focal_strip_stage_rows() { return kSR; }
+
+template <bool SLOPE, bool D8>
+static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
+                                const FocalParams& p, unsigned long long* counters, uint32_t* slow_items, int num_sms,
+                                cudaStream_t s) {
+    const int64_t nstrips = (p.cols + kTW - 1) / kTW, nbands = (p.rows + kSegRows - 1) / kSegRows;
+    const int64_t nsegs = nstrips * nbands;
+    if (nsegs == 0) return cudaSuccess;
+    const size_t smem = (size_t)kSWarps * kSWarpBytes;
+    auto kern = focal_strip_kernel<SLOPE, D8>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSWarps * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int64_t grid = (int64_t)num_sms * per_sm;
+    const int64_t need = (nsegs + kSWarps - 1) / kSWarps;
+    if (grid > need) grid = need;
+    if ((e = cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    const SlowList slow{slow_items, counters + 1, (p.cols + 3) / 4};
+    kern<<<(unsigned)grid, kSWarps * 32, smem, s>>>(*map_stage, *map_prime, p, nstrips, nsegs, counters, slow);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    strip_fixup_kernel<<<(unsigned)num_sms * 4, 128, 0, s>>>(dem, p, slow);
+    return cudaGetLastError();
+}
+
+size_t focal_strip_slow_bytes(int64_t rows, int64_t cols) { return (size_t)(rows * ((cols + 3) / 4)) * 4; }
+
+// Strip-walk form: `map_stage` has a (kBoxW, focal_strip_stage_rows()) box and
+// `map_prime` a (kBoxW, 2) box over the same float32 DEM `dem`; `counters`
+// points to two device counters (segment claims, slow items) and
+// `slow_items` to focal_strip_slow_bytes() of scratch.
+cudaError_t launch_focal_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
+                               const FocalParams& p, int fast_out, unsigned long long* counters, uint32_t* slow_items,
+                               int num_sms, cudaStream_t s) {
+    FocalParams q = p;
+    q.fast_out = fast_out;
+    q.fd = p.sk.method == PARGO_SLOPE_FD || !p.do_slope;
+    if (q.do_slope && q.do_d8)
+        return launch_strip<true, true>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    if (q.do_slope) return launch_strip<true, false>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    if (q.do_d8) return launch_strip<false, true>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    return cudaSuccess;
 }
 
 // The tensor map's box must be (kBoxW, focal_variant_rows(variant) + 2).

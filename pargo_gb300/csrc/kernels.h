@@ -37,12 +37,20 @@ cudaError_t launch_focal_tma(const CUtensorMap* map, const FocalParams& p, int f
                              cudaStream_t s);
 int focal_num_variants();
 int focal_variant_rows(int v);  // tile rows of variant v (its TMA box is that + 2)
+bool focal_variant_is_strip(int v);
 cudaError_t launch_focal_generic(const InView& dem, const FocalParams& p, cudaStream_t s);
 size_t focal_tma_smem_bytes();
 int focal_tma_tile_rows();
 int focal_tma_tile_cols();
 int focal_tma_box_cols();
 int focal_tma_box_rows();
+// Strip-walk form of the same kernel (warp-private TMA pipelines down 128-cell
+// column strips, segments claimed from `claim`).
+cudaError_t launch_focal_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
+                               const FocalParams& p, int fast_out, unsigned long long* counters, uint32_t* slow_items,
+                               int num_sms, cudaStream_t s);
+int focal_strip_stage_rows();
+size_t focal_strip_slow_bytes(int64_t rows, int64_t cols);
 
 // Batched slope+D8 (focal.cu): device tables of per-raster descriptors/params.
 cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params, const int64_t* tile_start,
