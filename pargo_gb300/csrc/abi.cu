@@ -425,7 +425,9 @@ int pick_variant(pargo_ctx* ctx, int64_t cells) {
 pargo_status launch_focal_variant(pargo_ctx* ctx, const InView& dem, const FocalParams& p, int fast_out, int v,
                                   cudaStream_t s) {
     pargo_status st;
-    const bool strip = focal_variant_is_strip(v) && fast_out && p.rows * ((p.cols + 3) / 4) < (1LL << 32);
+    // the strip walk's fast path covers Horn rise/run slope and dirType 8
+    const bool plain = (p.sk.method == PARGO_SLOPE_FD || !p.do_slope) && !p.sk.degrees && (!p.do_d8 || p.dir_type == 8);
+    const bool strip = focal_variant_is_strip(v) && plain && fast_out && p.rows * ((p.cols + 3) / 4) < (1LL << 32);
     if (strip) {
         CUtensorMap ms, mp;
         if ((st = make_tma_map(ctx, &ms, dem.base, p.rows, p.cols, dem.pitch, focal_strip_stage_rows())) != PARGO_OK)
@@ -434,7 +436,7 @@ pargo_status launch_focal_variant(pargo_ctx* ctx, const InView& dem, const Focal
         cudaError_t e;
         uint32_t* slow = (uint32_t*)slot(ctx, kSlotStripSlow, focal_strip_slow_bytes(p.rows, p.cols), &e);
         if (!slow) return cuda_fail(ctx, e, "strip walk scratch");
-        CU(ctx, launch_focal_strip(&ms, &mp, dem, p, fast_out, &ctx->d_counters[4], slow, ctx->num_sms, s));
+        CU(ctx, launch_focal_strip(&ms, &mp, dem, p, fast_out, v, &ctx->d_counters[4], slow, ctx->num_sms, s));
         return PARGO_OK;
     }
     if (focal_variant_is_strip(v)) v = 0;

@@ -567,26 +567,31 @@ __device__ __forceinline__ float fmin3f(float a, float b, float c) {
     return d;
 }
 
-// d8_fast with the maximum taken by three-input max (the same value).
-__device__ __forceinline__ int d8_fast3(float x0, float x1, float x2, float x3, float x5, float x6, float x7,
-                                        float x8) {
-    const float m = fmax3f(fmax3f(x0, x1, x2), fmax3f(x3, x5, x6), fmaxf(x7, x8));
+// d8_fast with the maximum taken by three-input max (the same value); the
+// certification is returned as a flag (false: the general path decides).
+// The four drops toward the row above and the east neighbour arrive negated
+// (n0 = -x0, n1 = -x1, n2 = -x2, n5 = -x5): their maximum is minus a minimum.
+__device__ __forceinline__ int d8_fast3(float n0, float n1, float n2, float x3, float n5, float x6, float x7, float x8,
+                                        bool& sure) {
+    const float m = fmax3f(fmax3f(x3, x6, x7), x8, -fmin3f(n0, n1, fminf(n2, n5)));
+    const float x0 = -n0, x1 = -n1, x2 = -n2, x5 = -n5;
     const float t = __fadd_rn(__fmaf_rn(m, -k2m19, m), -kTHi);
     const uint32_t ua = prmt(prmt(__float_as_uint(__fsub_rn(t, x0)), __float_as_uint(__fsub_rn(t, x1)), 0x00FB),
                              prmt(__float_as_uint(__fsub_rn(t, x2)), __float_as_uint(__fsub_rn(t, x3)), 0x00FB), 0x5410);
     const uint32_t ub = prmt(prmt(__float_as_uint(__fsub_rn(t, x5)), __float_as_uint(__fsub_rn(t, x6)), 0x00FB),
                              prmt(__float_as_uint(__fsub_rn(t, x7)), __float_as_uint(__fsub_rn(t, x8)), 0x00FB), 0x5410);
     const uint32_t w = (ua & 0x55555555u) | (ub & 0xAAAAAAAAu);
-    const int hb = 31 - __clz(w);
-    const int k = (hb >> 3) + (hb & 1) * 5;
-    return m < kLowCut ? -1 : (m > kHighCut && __popc(w) == 4) ? k : kD8Unsure;
+    uint32_t hb;
+    asm("bfind.u32 %0, %1;" : "=r"(hb) : "r"(w));  // position of the highest set bit
+    const bool low = m < kLowCut;
+    sure = low | ((m > kHighCut) & (__popc(w) == 4));  // no short-circuit branches
+    return low ? -1 : (int)((hb >> 3) + (hb & 1) * 5);
 }
 
 __device__ __forceinline__ bool row6_maybe_nodata(const float v[6], const Band<float>& b) {
     const float mn = fminf(fmin3f(v[0], v[1], v[2]), fmin3f(v[3], v[4], v[5]));
-    if (b.hi < 0.0f) return mn <= b.hi;
     const float mx = fmaxf(fmax3f(v[0], v[1], v[2]), fmax3f(v[3], v[4], v[5]));
-    return mn <= b.hi && mx >= b.lo;
+    return (mn <= b.hi) & (mx >= b.lo);
 }
 
 // One window row: this lane's six values (columns 4l-1 .. 4l+4 of the strip),
@@ -635,15 +640,18 @@ struct SlowList {
     uint32_t* items;
     unsigned long long* count;
     int64_t lanes_per_row;  // ceil(cols / 4)
+    int64_t cols;
 };
 
 // Output row y from the window rows A (y-1), B (y), C (y+1); C is loaded
 // here from stage row `crow`, and the pair B/C is formed for the next row.
+// `sp` / `dp` point to this lane's four slope / code cells of row y.  Only the
+// plain configuration runs here (Horn, rise/run, dirType 8).
 template <bool SLOPE, bool D8>
 __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, SRow& C, const SPair& PAB, SPair& PBC,
-                                           int64_t y, int64_t gx0, bool lane_int, const FocalParams& p, int lane,
-                                           const SlowList& slow) {
-    s_load_row(crow, lane, C, p.nd6f);
+                                           int y, int rows, int64_t gx0, bool lane_int, float k_fd, const Band<float>& nd6,
+                                           char* sp, char* dp, int lane, const SlowList& slow) {
+    s_load_row(crow, lane, C, nd6);
     s_pair(B, C, PBC);
     float sl[4];
     int cd[4];
@@ -655,43 +663,38 @@ __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, 
         for (int j = 0; j < 4; j++) {
             const float nx = __fmaf_rn(2.0f, B.sh[j], __fadd_rn(A.sh[j], C.sh[j]));
             const float ny = __fmaf_rn(2.0f, sv[j + 1], __fadd_rn(sv[j], sv[j + 2]));
-            sl[j] = horn_slope(nx, ny, p.sk.k_fd);
-            if (p.sk.degrees) sl[j] = atanf(sl[j]) * 57.29577951308232f;
+            sl[j] = horn_slope(nx, ny, k_fd);
         }
     }
-    bool unsure = false;
+    bool sure = true;
     if (D8) {
         float hd[5];
 #pragma unroll
         for (int a = 0; a < 5; a++) hd[a] = __fsub_rn(B.v[a + 1], B.v[a]);
 #pragma unroll
         for (int j = 0; j < 4; j++) {
-            cd[j] = d8_fast3(-PAB.e1[j], -PAB.vd[j], -PAB.e2[j + 1], hd[j], -hd[j + 1], PBC.e2[j], PBC.vd[j],
-                             PBC.e1[j + 1]);
-            unsure |= cd[j] == kD8Unsure;
-        }
-        if (p.dir_type != 8) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) cd[j] = d8_weight(cd[j]);
+            bool ok;
+            cd[j] = d8_fast3(PAB.e1[j], PAB.vd[j], PAB.e2[j + 1], hd[j], hd[j + 1], PBC.e2[j], PBC.vd[j],
+                             PBC.e1[j + 1], ok);
+            sure &= ok;
         }
     }
-    if (y >= p.rows) return;
-    const bool rb = !lane_int || (uint64_t)(y - 1) >= (uint64_t)(p.rows - 2) || A.nd || B.nd || C.nd || unsure;
-    if (!rb) {
-        if (SLOPE)
-            *reinterpret_cast<float4*>(p.slope.base + y * p.slope.pitch + 4 * gx0) = make_float4(sl[0], sl[1], sl[2], sl[3]);
+    const bool live = y < rows;
+    const bool fast = lane_int & ((unsigned)(y - 1) < (unsigned)(rows - 2)) & !(A.nd | B.nd | C.nd) & sure;
+    if (live & fast) {
+        if (SLOPE) *reinterpret_cast<float4*>(sp) = make_float4(sl[0], sl[1], sl[2], sl[3]);
         if (D8)
-            *reinterpret_cast<uint32_t*>(p.d8.base + y * p.d8.pitch + gx0) =
-                __byte_perm(__byte_perm((uint32_t)cd[0], (uint32_t)cd[1], 0x0040),
-                            __byte_perm((uint32_t)cd[2], (uint32_t)cd[3], 0x0040), 0x5410);
+            *reinterpret_cast<uint32_t*>(dp) = __byte_perm(__byte_perm((uint32_t)cd[0], (uint32_t)cd[1], 0x0040),
+                                                          __byte_perm((uint32_t)cd[2], (uint32_t)cd[3], 0x0040), 0x5410);
     }
-    const unsigned m = __ballot_sync(0xffffffffu, rb && gx0 < p.cols);
+    const bool slow_here = live & !fast & (gx0 < slow.cols);
+    const unsigned m = __ballot_sync(0xffffffffu, slow_here);
     if (m) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(slow.count, (unsigned long long)__popc(m));
         base = __shfl_sync(0xffffffffu, base, 0);
-        if (rb && gx0 < p.cols)
-            slow.items[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)(y * slow.lanes_per_row + (gx0 >> 2));
+        if (slow_here)
+            slow.items[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)((int64_t)y * slow.lanes_per_row + (gx0 >> 2));
     }
 }
 
@@ -701,8 +704,8 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
     return __all_sync(0xffffffffu, ok);
 }
 
-template <bool SLOPE, bool D8>
-__global__ void __launch_bounds__(kSWarps * 32, 5) focal_strip_kernel(const __grid_constant__ CUtensorMap map_stage,
+template <bool SLOPE, bool D8, int MINB>
+__global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const __grid_constant__ CUtensorMap map_stage,
                                                                        const __grid_constant__ CUtensorMap map_prime,
                                                                        const __grid_constant__ FocalParams p,
                                                                        int64_t nstrips, int64_t nsegs,
@@ -755,10 +758,16 @@ __global__ void __launch_bounds__(kSWarps * 32, 5) focal_strip_kernel(const __gr
     int pb = 0;
     SRow A, B, C;
     SPair PAB, PBC, PCA;
+    const int rows = (int)p.rows;
+    const float k_fd = p.sk.k_fd;
+    // the fast path's configuration: Horn rise/run slope, dirType 8, vector stores
+    const bool plain = p.fd && p.fast_out && !p.sk.degrees && (!D8 || p.dir_type == 8);
     while (true) {
         const int64_t x0 = (cur % nstrips) * kTW, y0 = (cur / nstrips) * kSegRows;
         const int64_t gx0 = x0 + 4 * lane;
-        const bool lane_int = p.fd && p.fast_out && gx0 >= 1 && gx0 + 4 <= p.cols - 1;
+        const bool lane_int = plain && gx0 >= 1 && gx0 + 4 <= p.cols - 1;
+        char* sp = SLOPE ? p.slope.base + y0 * p.slope.pitch + 4 * gx0 : nullptr;
+        char* dp = D8 ? p.d8.base + y0 * p.d8.pitch + gx0 : nullptr;
         int64_t nxt = nsegs;
         if (!warp_wait(&bar[2 + pb], (pphase >> pb) & 1u)) {
             if (lane == 0 && p.error_flag) atomicExch(p.error_flag, 1);
@@ -779,10 +788,16 @@ __global__ void __launch_bounds__(kSWarps * 32, 5) focal_strip_kernel(const __gr
 #pragma unroll 1
             for (int t = 0; t < kSR; t += 3) {
                 const float* st = stage(buf) + t * kBoxW;
-                const int64_t y = y0 + (int64_t)k * kSR + t;
-                strip_step<SLOPE, D8>(st, A, B, C, PAB, PBC, y, gx0, lane_int, p, lane, slow);
-                strip_step<SLOPE, D8>(st + kBoxW, B, C, A, PBC, PCA, y + 1, gx0, lane_int, p, lane, slow);
-                strip_step<SLOPE, D8>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, gx0, lane_int, p, lane, slow);
+                const int y = (int)y0 + k * kSR + t;
+                const int64_t spp = SLOPE ? p.slope.pitch : 0, dpp = D8 ? p.d8.pitch : 0;
+                strip_step<SLOPE, D8>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp, lane,
+                                      slow);
+                strip_step<SLOPE, D8>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd, p.nd6f,
+                                      sp + spp, dp + dpp, lane, slow);
+                strip_step<SLOPE, D8>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd, p.nd6f,
+                                      sp + 2 * spp, dp + 2 * dpp, lane, slow);
+                sp += 3 * spp;
+                dp += 3 * dpp;
             }
             __syncwarp();
             // refill this buffer with the item two ahead
@@ -848,9 +863,10 @@ struct Variant {
 static const Variant kVariants[] = {{8, 1, 5}, {6, 1, 6}, {6, 1, 7}, {4, 1, 8}, {8, 1, 6}};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
 
-// Variant kNumVariants is the strip walk (launch_focal_strip).
-int focal_num_variants() { return kNumVariants + 1; }
-bool focal_variant_is_strip(int v) { return v == kNumVariants; }
+// Variants kNumVariants and kNumVariants + 1 are the strip walk
+// (launch_focal_strip) at 5 and 6 CTAs per SM.
+int focal_num_variants() { return kNumVariants + 2; }
+bool focal_variant_is_strip(int v) { return v == kNumVariants || v == kNumVariants + 1; }
 int focal_variant_rows(int v) { return kWarps * kVariants[(v >= 0 && v < kNumVariants) ? v : 0].rows; }
 size_t focal_tma_smem_bytes() { return 2 * Shape<kBatchRows>::kStageStride; }
 int focal_tma_tile_rows() { return Shape<kBatchRows>::kTH; }
@@ -892,7 +908,7 @@ static cudaError_t launch_variants(const CUtensorMap* map, const FocalParams& p,
 
 int focal_strip_stage_rows() { return kSR; }
 
-template <bool SLOPE, bool D8>
+template <bool SLOPE, bool D8, int MINB>
 static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
                                 const FocalParams& p, unsigned long long* counters, uint32_t* slow_items, int num_sms,
                                 cudaStream_t s) {
@@ -900,7 +916,7 @@ static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap*
     const int64_t nsegs = nstrips * nbands;
     if (nsegs == 0) return cudaSuccess;
     const size_t smem = (size_t)kSWarps * kSWarpBytes;
-    auto kern = focal_strip_kernel<SLOPE, D8>;
+    auto kern = focal_strip_kernel<SLOPE, D8, MINB>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -911,7 +927,7 @@ static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap*
     const int64_t need = (nsegs + kSWarps - 1) / kSWarps;
     if (grid > need) grid = need;
     if ((e = cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
-    const SlowList slow{slow_items, counters + 1, (p.cols + 3) / 4};
+    const SlowList slow{slow_items, counters + 1, (p.cols + 3) / 4, p.cols};
     kern<<<(unsigned)grid, kSWarps * 32, smem, s>>>(*map_stage, *map_prime, p, nstrips, nsegs, counters, slow);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     strip_fixup_kernel<<<(unsigned)num_sms * 4, 128, 0, s>>>(dem, p, slow);
@@ -924,17 +940,28 @@ size_t focal_strip_slow_bytes(int64_t rows, int64_t cols) { return (size_t)(rows
 // `map_prime` a (kBoxW, 2) box over the same float32 DEM `dem`; `counters`
 // points to two device counters (segment claims, slow items) and
 // `slow_items` to focal_strip_slow_bytes() of scratch.
+template <int MINB>
+static cudaError_t launch_strip_minb(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
+                                     const FocalParams& q, unsigned long long* counters, uint32_t* slow_items,
+                                     int num_sms, cudaStream_t s) {
+    if (q.do_slope && q.do_d8)
+        return launch_strip<true, true, MINB>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    if (q.do_slope)
+        return launch_strip<true, false, MINB>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    if (q.do_d8)
+        return launch_strip<false, true, MINB>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    return cudaSuccess;
+}
+
 cudaError_t launch_focal_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
-                               const FocalParams& p, int fast_out, unsigned long long* counters, uint32_t* slow_items,
-                               int num_sms, cudaStream_t s) {
+                               const FocalParams& p, int fast_out, int variant, unsigned long long* counters,
+                               uint32_t* slow_items, int num_sms, cudaStream_t s) {
     FocalParams q = p;
     q.fast_out = fast_out;
     q.fd = p.sk.method == PARGO_SLOPE_FD || !p.do_slope;
-    if (q.do_slope && q.do_d8)
-        return launch_strip<true, true>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
-    if (q.do_slope) return launch_strip<true, false>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
-    if (q.do_d8) return launch_strip<false, true>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
-    return cudaSuccess;
+    if (variant == kNumVariants + 1)
+        return launch_strip_minb<6>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    return launch_strip_minb<5>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
 }
 
 // The tensor map's box must be (kBoxW, focal_variant_rows(variant) + 2).

@@ -47,8 +47,8 @@ int focal_tma_box_rows();
 // Strip-walk form of the same kernel (warp-private TMA pipelines down 128-cell
 // column strips, segments claimed from `claim`).
 cudaError_t launch_focal_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
-                               const FocalParams& p, int fast_out, unsigned long long* counters, uint32_t* slow_items,
-                               int num_sms, cudaStream_t s);
+                               const FocalParams& p, int fast_out, int variant, unsigned long long* counters,
+                               uint32_t* slow_items, int num_sms, cudaStream_t s);
 int focal_strip_stage_rows();
 size_t focal_strip_slow_bytes(int64_t rows, int64_t cols);
 
