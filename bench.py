@@ -662,6 +662,84 @@ def run_mfd(args, ws, rank, local, side=8192):
     }
 
 
+def run_load(args, ws, rank, local, side=32768, grain=16):
+    """Load estimator: the intensity-ratio compute layer (grain 16, valid 1,
+    nodata 0) of the side^2 float32 hydro DEM (seed 1, 10% nodata blob), then
+    its 152-part row decomposition; a step is one pargo_compute_load call
+    (the compute layer stays on the device) and one pargo_load_decompose."""
+    import torch
+    from pargo_gb300 import abi
+    torch.cuda.set_device(local)
+    ctx = abi.Context(local)
+    dem = make_hydro(side, side)
+    cells = side * side
+    stream = torch.cuda.current_stream()
+    R = abi.raster
+    d = torch.from_numpy(dem).cuda()
+    cr, cc = abi.compute_load_dims(side, side, grain)
+    load = torch.empty((cr, cc), dtype=torch.float64, device="cuda")
+    rd, rl = R(d, ND), R(load, ND)
+    nparts = 152
+
+    def step():
+        ctx.compute_load(rd, rl, grain, 0.0, 1.0, stream=stream)
+        ctx.load_decompose(rl, (side, side), nparts, stream=stream)
+
+    barrier(ws)
+    clocks = ClockSampler(local)
+    clocks.start()
+    ms = timed_steps(step, args, stream)
+    clk = clocks.stop()
+    ms_k = timed_steps(lambda: ctx.compute_load(rd, rl, grain, 0.0, 1.0, stream=stream),
+                       argparse.Namespace(steps=args.steps, warmup=1), stream)
+    ms = max_over_ranks(ms, ws, torch.device("cuda", local))
+    hd = pinned(dem)
+    hl = torch.empty((cr, cc), dtype=torch.float64).pin_memory()
+    rh = (R(hd, ND), R(hl, ND))
+
+    def e2e():
+        ctx.compute_load(rh[0], rh[1], grain, 0.0, 1.0, stream=stream)
+        ctx.load_decompose(rh[1], (side, side), nparts, stream=stream)
+
+    e2e()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, ws, torch.device("cuda", local))
+    cpu = None
+    if rank == 0 and ws == 1:
+        import oracle
+        O = oracle.Oracle()
+        crop = np.ascontiguousarray(dem[:4096])
+        t0 = time.perf_counter()
+        lo = O.compute_load(crop, ND, grain, 0.0, 1.0)
+        O.load_decompose(lo, ND, crop.shape, nparts)
+        dt = time.perf_counter() - t0
+        cpu = {"value": round(crop.size / dt / 1e6, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
+               "sample": "the first 4096 rows: the oracle's compute layer + decomposition (serial, as the "
+                         "reference's Transformation::run), %.2f s" % dt}
+    peak, kind = hbm_peak()
+    achieved = cells * 4.0 / (ms_k * 1e-3) / 1e9
+    return {
+        "metric": "Mcells/s load estimate + decomposition", "value": round(ws * cells / (ms * 1e-3) / 1e6, 1),
+        "unit": "Mcells/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 sums", "data": "synthetic",
+        "config": {"workload": "load%d: intensity compute layer (grain %d) of the %dx%d float32 hydro DEM (seed 1), "
+                               "%d-part row decomposition" % (side, grain, side, side, nparts),
+                   "l2": "inputs larger than L2"},
+        "roofline": {"bound": "hbm", "kernel": "compute_load_kernel", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind, "traffic": None,
+                     "algorithmic_bytes_per_cell": 4, "kernel_ms": round(ms_k, 3)},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells * 4,
+                "d2h_bytes_per_step": cr * cc * 8},
+        "gpu_launches": args.steps * 2, "clocks": clk,
+    }
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return None
@@ -695,7 +773,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="hydro8192",
                     choices=["hydro8192", "hydro2048", "slope32768", "slope8192", "slope1024", "batch512",
-                             "sca16384", "sca4096", "grad8192", "mfd8192", "mfd2048"])
+                             "sca16384", "sca4096", "grad8192", "mfd8192", "mfd2048", "load32768", "load8192"])
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_setup()
@@ -705,6 +783,8 @@ def main():
         out = run_hydro(args, ws, rank, local, int(args.workload[5:]))
     elif args.workload.startswith("sca"):
         out = run_sca(args, ws, rank, local, int(args.workload[3:]))
+    elif args.workload.startswith("load"):
+        out = run_load(args, ws, rank, local, int(args.workload[4:]))
     elif args.workload.startswith("mfd"):
         out = run_mfd(args, ws, rank, local, int(args.workload[3:]))
     elif args.workload == "grad8192":

@@ -217,6 +217,36 @@ pargo_status pargo_mfd(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* we
 pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_raster* sca, const pargo_nbr* nbr,
                            void* stream);
 
+/* Load estimator, intensity-ratio mode: the compute layer of `count` data
+ * rasters (same shape, F32 or F64), replacing ComputeLayer::init +
+ * Transformation::run (gpro/computeLayer.h:210-262,
+ * gpro/transformation.h:155-229).  Compute cell (r, c) covers the data rows
+ * r*grain+1 .. (r+1)*grain and columns c*grain+1 .. (c+1)*grain of the 3x3
+ * work rectangle (clipped to the raster) and holds the sum, layer by layer and
+ * row by row, of valid_load per valid cell (|v - nodata| > 1e-7, each
+ * layer's own nodata) and nodata_load per other cell; the FP64 sums are the
+ * reference's bit for bit.  compute_ring != 0 gives the compute layer a 3x3
+ * neighbourhood of its own: its ring cells stay 0.  load: F64 or F32 of
+ * pargo_compute_load_dims.  An application's own estimate function (the
+ * reference's Transformation subclasses) writes its compute layer by other
+ * means and goes straight to pargo_load_decompose. */
+pargo_status pargo_compute_load_dims(int64_t rows, int64_t cols, int grain, int64_t* crows, int64_t* ccols);
+pargo_status pargo_compute_load(pargo_ctx* ctx, int count, const pargo_raster* data, const pargo_nbr* nbr, int grain,
+                                int compute_ring, double nodata_load, double valid_load, pargo_raster* load,
+                                void* stream);
+
+/* Row-wise decomposition of a compute layer into nparts by load, replacing
+ * DeComposition::valRowDcmp (gpro/deComposition.h:305-393) and the mapping to
+ * data rows of ComputeLayer::getCompuLoad (gpro/computeLayer.h:380-443): row
+ * loads (cells above -9999 and above the load raster's nodata by more than
+ * 1e-7) on the device, the greedy cuts on the host.  comp_rows (may be NULL)
+ * receives each part's compute rows {begin, end}; bounds each part's data
+ * rectangle {minRow, minCol, maxRow, maxCol} in a data_rows x data_cols
+ * raster with a 3x3 neighbourhood.  Synchronous. */
+pargo_status pargo_load_decompose(pargo_ctx* ctx, const pargo_raster* load, int compute_ring, int64_t data_rows,
+                                  int64_t data_cols, const pargo_nbr* nbr, int nparts, int64_t* comp_rows,
+                                  int64_t* bounds, void* stream);
+
 /* Batched fused slope + D8 over `count` independent rasters in one persistent
  * launch; slopes / d8s may be NULL (no such output) and all rasters must be on
  * the device. */

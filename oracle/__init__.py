@@ -52,6 +52,9 @@ class Oracle:
         lib.orc_twi.argtypes = [_c_f64p, _c_f64p, i, i, d, d, _c_f64p]
         lib.orc_mfd.argtypes = [vp, i, i, i, d, f, d, _c_f64p]
         lib.orc_sca_mfd.argtypes = [_c_f64p, i, i, d, _c_f64p]
+        ip = ctypes.POINTER(ctypes.c_int)
+        lib.orc_compute_load.argtypes = [vp, i, i, i, i, d, i, d, d, i, _c_f64p]
+        lib.orc_load_decompose.argtypes = [_c_f64p, i, i, d, i, i, i, i, ip, ip]
         self.lib = lib
 
     @staticmethod
@@ -139,6 +142,35 @@ class Oracle:
             raise OracleError("orc_sca_mfd rc=%d" % rc)
         return out
 
+    def compute_load(self, data, nodata, grain, nodata_load, valid_load, compute_ring=False):
+        """Intensity-ratio compute layer (ComputeLayer + Transformation) of one
+        raster (rows, cols) or several stacked (layers, rows, cols)."""
+        a = data if data.ndim == 3 else data[None]
+        f64 = a.dtype == np.float64
+        a = _c(a, np.float64 if f64 else np.float32)
+        L, R, C = a.shape
+        crows, ccols = (R - 2 + grain - 1) // grain, (C - 2 + grain - 1) // grain
+        out = np.empty((crows, ccols), np.float64)
+        rc = self.lib.orc_compute_load(a.ctypes.data, int(f64), L, R, C, nodata, grain, float(nodata_load),
+                                       float(valid_load), int(compute_ring), _p(out, _c_f64p))
+        if rc:
+            raise OracleError("orc_compute_load rc=%d" % rc)
+        return out
+
+    def load_decompose(self, load, nodata, data_shape, nparts, compute_ring=False):
+        """Row decomposition of a compute layer (valRowDcmp + getCompuLoad's
+        mapping): (compute row ranges (nparts, 2), data rectangles (nparts, 4))."""
+        a = _c(load, np.float64)
+        comp = np.zeros((nparts, 2), np.int32)
+        bounds = np.zeros((nparts, 4), np.int32)
+        ip = ctypes.POINTER(ctypes.c_int)
+        rc = self.lib.orc_load_decompose(_p(a, _c_f64p), a.shape[0], a.shape[1], nodata, int(compute_ring),
+                                         data_shape[0], data_shape[1], nparts, comp.ctypes.data_as(ip),
+                                         bounds.ctypes.data_as(ip))
+        if rc:
+            raise OracleError("orc_load_decompose rc=%d" % rc)
+        return comp, bounds
+
     def twi(self, slope, sca, nodata, out_nodata=None):
         """Topographic wetness index ln(sca / max(slope, 1e-7)) with the
         reference's nodata rule (TWIOperator.cpp:42-69), in FP64."""
@@ -166,6 +198,8 @@ class Reference:
         lib.ref_fill.argtypes = [cp, _c_f32p, i, i, d, d, _c_f64p, ctypes.POINTER(ctypes.c_int)]
         lib.ref_sca.argtypes = [cp, _c_f64p, i, i, d, d, i, _c_f64p, ctypes.POINTER(ctypes.c_int)]
         lib.ref_twi.argtypes = [cp, _c_f64p, _c_f64p, i, i, d, d, _c_f64p]
+        ip = ctypes.POINTER(ctypes.c_int)
+        lib.ref_compute_load.argtypes = [cp, _c_f32p, i, i, d, d, i, d, d, i, i, _c_f64p, ip, ip, ip, ip]
         self.lib = lib
         self.mfd_lib = None
         if os.path.exists(_build.REF_MFD_SO):
@@ -247,3 +281,24 @@ class Reference:
         if rc:
             raise OracleError("ref_twi rc=%d" % rc)
         return out
+
+    def compute_load(self, data, nodata, grain, nodata_load, valid_load, compute_ring=False, nparts=0,
+                     cellsize=1.0):
+        """(compute layer, compute row ranges (nparts, 2), rank 0's data rectangle)
+        from the reference ComputeLayer / Transformation / DeComposition."""
+        a = _c(data, np.float32)
+        R, C = a.shape
+        crows, ccols = (R - 2 + grain - 1) // grain, (C - 2 + grain - 1) // grain
+        out = np.empty((crows, ccols), np.float64)
+        comp = np.zeros((max(nparts, 1), 2), np.int32)
+        rank0 = np.zeros(4, np.int32)
+        cr, cc = ctypes.c_int(), ctypes.c_int()
+        ip = ctypes.POINTER(ctypes.c_int)
+        rc = self.lib.ref_compute_load(self._nbr.encode(), _p(a, _c_f32p), R, C, nodata, cellsize, grain,
+                                       float(nodata_load), float(valid_load), int(compute_ring), nparts,
+                                       _p(out, _c_f64p), ctypes.byref(cr), ctypes.byref(cc), comp.ctypes.data_as(ip),
+                                       rank0.ctypes.data_as(ip))
+        if rc:
+            raise OracleError("ref_compute_load rc=%d" % rc)
+        assert (cr.value, cc.value) == out.shape
+        return out, comp[:nparts], rank0

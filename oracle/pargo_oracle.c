@@ -622,3 +622,122 @@ int orc_sca_mfd(const double* w, int rows, int cols, double nodata, double* sca)
     free(deg);
     return 0;
 }
+
+/* Compute-intensity layer, restating ComputeLayer::_init (gpro/computeLayer.h:
+ * 210-262: ceil(work rows / grain) x ceil(work cols / grain) cells, all 0) and
+ * the intensity-ratio Transformation::Operator (gpro/transformation.h:155-197)
+ * for a 3x3 data neighbourhood (data work rectangle [1, rows-2] x [1, cols-2]):
+ * compute cell (r, c) sums, data row by data row, valid_load for a data cell
+ * with |v - nodata| > 1e-7 and nodata_load otherwise, over rows
+ * r*grain + 1 .. (r+1)*grain and columns c*grain + 1 .. (c+1)*grain, skipping
+ * cells past the raster's last row / column.  With compute_ring the compute
+ * layer has a 3x3 neighbourhood of its own and its ring cells stay 0.
+ * data: float (is_f64 = 0) or double.  `layers` data rasters are summed in turn. */
+int orc_compute_load(const void* data, int is_f64, int layers, int rows, int cols, double nodata, int grain,
+                     double nodata_load, double valid_load, int compute_ring, double* load) {
+    if (rows < 3 || cols < 3 || grain < 1 || layers < 1) return 1;
+    const int crows = (rows - 2 + grain - 1) / grain, ccols = (cols - 2 + grain - 1) / grain;
+    const size_t n = (size_t)rows * cols;
+    for (size_t i = 0; i < (size_t)crows * ccols; i++) load[i] = 0.0;
+    const int r0 = compute_ring ? 1 : 0, r1 = compute_ring ? crows - 2 : crows - 1;
+    const int c0 = compute_ring ? 1 : 0, c1 = compute_ring ? ccols - 2 : ccols - 1;
+    for (int cr = r0; cr <= r1; cr++)
+        for (int cc = c0; cc <= c1; cc++) {
+            double acc = 0.0;
+            for (int l = 0; l < layers; l++)
+                for (int dr = cr * grain + 1; dr < (cr + 1) * grain + 1; dr++)
+                    for (int dc = cc * grain + 1; dc < (cc + 1) * grain + 1; dc++) {
+                        if (dr > rows - 1 || dc > cols - 1) continue;
+                        const size_t i = (size_t)l * n + (size_t)dr * cols + dc;
+                        const double v = is_f64 ? ((const double*)data)[i] : (double)((const float*)data)[i];
+                        acc += fabs(v - nodata) > 0.0000001 ? valid_load : nodata_load;
+                    }
+            load[(size_t)cr * ccols + cc] = acc;
+        }
+    return 0;
+}
+
+/* Row-wise decomposition of a compute layer by load, restating
+ * DeComposition::valRowDcmp (gpro/deComposition.h:305-393) -- per-row loads
+ * (cells above -9999 and above nodata by more than 1e-7, summed left to
+ * right), then nparts-1 greedy cuts, each closing a part at the row where the
+ * running load passes the current average or just before it, whichever is
+ * nearer -- and the mapping of ComputeLayer::getCompuLoad
+ * (gpro/computeLayer.h:402-430) to data rows of a 3x3 data neighbourhood:
+ * part i starts at (int)(first compute row * data_rows / compute rows + 1).
+ * comp_rows[2i], [2i+1]: compute rows of part i; bounds[4i..4i+3]: its data
+ * rectangle {minRow, minCol, maxRow, maxCol}.  Returns 2 when the cuts run out
+ * of rows (the reference then indexes past its part list). */
+int orc_load_decompose(const double* load, int crows, int ccols, double nodata, int compute_ring, int data_rows,
+                       int data_cols, int nparts, int* comp_rows, int* bounds) {
+    const int work_rows = compute_ring ? crows - 2 : crows;
+    if (nparts < 1 || nparts > work_rows) return 1;
+    double* row_load = (double*)malloc(sizeof(double) * (size_t)(crows > 0 ? crows : 1));
+    if (!row_load) return 3;
+    double total = 0.0;
+    for (int r = 0; r < crows; r++) {
+        row_load[r] = 0.0;
+        for (int c = 0; c < ccols; c++) {
+            const double v = load[(size_t)r * ccols + c];
+            if ((v + 9999) > 0.0000001 && (v - nodata) > 0.0000001) row_load[r] += v;
+        }
+        total += row_load[r];
+    }
+    double aver = total / nparts, accu = 0.0;
+    int begin = 0, end = 0, k = 0;
+    for (int i = 0; i < nparts - 1; i++) {
+        double sub = 0.0, min_diff = 0.0;
+        int cut = 0;
+        for (int r = begin; r < crows; r++) {
+            sub += row_load[r];
+            accu += row_load[r];
+            if (sub <= aver && crows - 1 - r > nparts - 1 - i) {
+                if (fabs(min_diff) < 0.0000001 || (aver - sub) < min_diff) min_diff = aver - sub;
+            } else {
+                if (fabs(min_diff) < 0.0000001 || (sub - aver) <= min_diff || crows - 1 - r == nparts - 1 - i) {
+                    end = r;
+                    comp_rows[2 * k] = begin;
+                    comp_rows[2 * k + 1] = end;
+                    k++;
+                    aver = (total - accu) / (nparts - i - 1);
+                    begin = r + 1;
+                } else {
+                    end = r - 1;
+                    accu -= row_load[r];
+                    comp_rows[2 * k] = begin;
+                    comp_rows[2 * k + 1] = end;
+                    k++;
+                    sub -= row_load[r];
+                    aver = (total - accu) / (nparts - i - 1);
+                    begin = r;
+                }
+                cut = 1;
+                break;
+            }
+        }
+        if (!cut) {
+            free(row_load);
+            return 2;
+        }
+    }
+    comp_rows[2 * k] = begin;
+    comp_rows[2 * k + 1] = crows - 1;
+    free(row_load);
+    /* data rows */
+    const double convert = data_rows / (double)crows;
+    const int wmin_r = 1, wmax_r = data_rows - 2, wmin_c = 1, wmax_c = data_cols - 2;
+    int sub_begin = wmin_r, sub_end = wmin_r - 1, i = 0;
+    for (; i < nparts - 1; i++) {
+        sub_begin = (int)(comp_rows[2 * i] * convert + wmin_r);
+        sub_end = (int)(comp_rows[2 * (i + 1)] * convert + wmin_r - 1);
+        bounds[4 * i] = sub_begin;
+        bounds[4 * i + 1] = wmin_c;
+        bounds[4 * i + 2] = sub_end;
+        bounds[4 * i + 3] = wmax_c;
+    }
+    bounds[4 * i] = sub_end + 1;
+    bounds[4 * i + 1] = wmin_c;
+    bounds[4 * i + 2] = wmax_r;
+    bounds[4 * i + 3] = wmax_c;
+    return 0;
+}

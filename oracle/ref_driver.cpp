@@ -38,6 +38,10 @@
 #undef Eps
 #include "TWIOperator.h"
 #undef Eps
+#include "computeLayer.h"  // defines Eps 1e-7, which transformation.h uses
+#include "transformation.h"
+#include "deComposition.h"
+#undef Eps
 
 using namespace GPRO;
 
@@ -203,6 +207,48 @@ int ref_twi(const char* nbr, const double* slope, const double* sca, int rows, i
     op.twiLayer(twiLayer);
     if (!op.Run()) return 2;
     copy_out(twiLayer, out, rows, cols);
+    return 0;
+}
+
+/* Load estimation and row decomposition by the reference gpro classes, as
+ * apps/spatial/reclassify/pRelclassify.cpp:164-178 drives them (intensity-ratio
+ * mode): ComputeLayer::init(dataLayer, compute nbr, grain), Transformation(
+ * nodataLoad, validLoad).run(), then DeComposition::valRowDcmp on the compute
+ * layer and ComputeLayer::getCompuLoad(ROWWISE_DCMP) for rank 0's data rows.
+ * `load` receives the compute layer (crows x ccols); comp_rows the compute
+ * row range [begin, end] of every part; rank0 the data bounding rectangle
+ * {minRow, minCol, maxRow, maxCol} getCompuLoad returns to rank 0. */
+int ref_compute_load(const char* nbr, const float* data, int rows, int cols, double nodata, double cellsize,
+                     int grain, double nodata_load, double valid_load, int compute_nbr, int nparts, double* load,
+                     int* crows, int* ccols, int* comp_rows, int* rank0) {
+    start(MPI_Type);
+    pargo_shim_register("ref://load_data", data, GDT_Float32, rows, cols, nodata, cellsize);
+    RasterLayer<double> dataLayer("dataLayer");
+    dataLayer.readNeighborhood(nbr);
+    if (!dataLayer.readFile("ref://load_data", ROWWISE_DCMP)) return 1;
+    ComputeLayer<double> comptLayer("computLayer");
+    if (!comptLayer.init(&dataLayer, compute_nbr ? nbr : nullptr, grain)) return 2;
+    Transformation<double> trans(nodata_load, valid_load, &comptLayer);
+    if (!trans.run()) return 3;
+    const SpaceDims& cd = comptLayer._pMetaData->_glbDims;
+    *crows = cd.nRows();
+    *ccols = cd.nCols();
+    memcpy(load, comptLayer.cellSpace()->_matrix, sizeof(double) * (size_t)cd.nRows() * cd.nCols());
+    if (nparts < 1) return 0;
+    DeComposition<double> deComp(cd, *(comptLayer.nbrhood()));
+    vector<CoordBR> parts;
+    if (!deComp.valRowDcmp(parts, comptLayer, nparts)) return 4;
+    if ((int)parts.size() != nparts) return 5;
+    for (int i = 0; i < nparts; i++) {
+        comp_rows[2 * i] = parts[i].minIRow();
+        comp_rows[2 * i + 1] = parts[i].maxIRow();
+    }
+    CoordBR sub;
+    if (!comptLayer.getCompuLoad(ROWWISE_DCMP, nparts, sub)) return 6;
+    rank0[0] = sub.minIRow();
+    rank0[1] = sub.minICol();
+    rank0[2] = sub.maxIRow();
+    rank0[3] = sub.maxICol();
     return 0;
 }
 

@@ -80,6 +80,10 @@ def lib():
         L.pargo_twi.argtypes = [vp, R, R, R, N, vp]
         L.pargo_mfd.argtypes = [vp, R, R, N, ctypes.c_double, vp]
         L.pargo_sca_mfd.argtypes = [vp, R, R, N, vp]
+        i64, i64p = ctypes.c_int64, P(ctypes.c_int64)
+        L.pargo_compute_load_dims.argtypes = [i64, i64, i, i64p, i64p]
+        L.pargo_compute_load.argtypes = [vp, i, R, N, i, i, ctypes.c_double, ctypes.c_double, R, vp]
+        L.pargo_load_decompose.argtypes = [vp, R, i, i64, i64, N, i, i64p, i64p, vp]
         L.pargo_hydro_pipeline.argtypes = [vp, R, R, R, R, R, N, P(FillOpts), i, i, i, P(FillStats), vp]
         L.pargo_batch_slope_d8.argtypes = [vp, i, R, R, R, N, i, i, i, vp]
         L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
@@ -92,12 +96,22 @@ def lib():
         L.pargo_last_d8_fallbacks.argtypes = [vp]
         L.pargo_last_d8_fallbacks.restype = ctypes.c_int64
         for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
-                     "pargo_fill", "pargo_sca", "pargo_twi", "pargo_mfd", "pargo_sca_mfd",
+                     "pargo_fill", "pargo_sca", "pargo_twi", "pargo_mfd", "pargo_sca_mfd", "pargo_compute_load_dims",
+                     "pargo_compute_load", "pargo_load_decompose",
                      "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
                      "pargo_slope_loss_grad"):
             getattr(L, name).restype = st
         _lib = L
     return _lib
+
+
+def compute_load_dims(rows, cols, grain):
+    """Shape of the compute layer of a rows x cols raster at `grain`."""
+    cr, cc = ctypes.c_int64(), ctypes.c_int64()
+    rc = lib().pargo_compute_load_dims(rows, cols, grain, ctypes.byref(cr), ctypes.byref(cc))
+    if rc:
+        raise PargoError(rc, "bad compute layer arguments")
+    return cr.value, cc.value
 
 
 def nbr_parse(text):
@@ -239,6 +253,27 @@ class Context:
             raise ValueError("sca_mfd: 8 weight rasters")
         W = (Raster * 8)(*weights)
         self._check(lib().pargo_sca_mfd(self._p, W, ctypes.byref(sca), self._nbr(nbr), _stream_ptr(stream)))
+
+    def compute_load(self, data, load, grain, nodata_load=0.0, valid_load=1.0, compute_ring=False, nbr=None,
+                     stream=None):
+        """Intensity-ratio compute layer (ComputeLayer + Transformation) of one
+        or several data rasters into `load`."""
+        data = list(data) if isinstance(data, (list, tuple)) else [data]
+        D = (Raster * len(data))(*data)
+        self._check(lib().pargo_compute_load(self._p, len(data), D, self._nbr(nbr), int(grain), int(bool(compute_ring)),
+                                             float(nodata_load), float(valid_load), ctypes.byref(load),
+                                             _stream_ptr(stream)))
+
+    def load_decompose(self, load, data_shape, nparts, compute_ring=False, nbr=None, stream=None):
+        """Row decomposition by load: (compute rows (nparts, 2), data rectangles (nparts, 4))."""
+        import numpy as np
+        comp = np.zeros((nparts, 2), np.int64)
+        bounds = np.zeros((nparts, 4), np.int64)
+        P = ctypes.POINTER(ctypes.c_int64)
+        self._check(lib().pargo_load_decompose(self._p, ctypes.byref(load), int(bool(compute_ring)),
+                                               int(data_shape[0]), int(data_shape[1]), self._nbr(nbr), int(nparts),
+                                               comp.ctypes.data_as(P), bounds.ctypes.data_as(P), _stream_ptr(stream)))
+        return comp, bounds
 
     def batch_slope_d8(self, dems, slopes=None, d8s=None, method=SLOPE_FD, units=RATIO, dir_type=8, nbr=None,
                        stream=None):

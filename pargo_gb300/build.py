@@ -27,7 +27,7 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                      "-I" + INCLUDE]
-CU_SOURCES = ["abi.cu", "focal.cu", "focal64.cu", "fill.cu", "sca.cu", "sca_tiled.cu", "twi.cu", "mfd.cu", "grad.cu", "noalloc.cu"]
+CU_SOURCES = ["abi.cu", "focal.cu", "focal64.cu", "fill.cu", "sca.cu", "sca_tiled.cu", "twi.cu", "mfd.cu", "load.cu", "grad.cu", "noalloc.cu"]
 
 
 def nvcc():

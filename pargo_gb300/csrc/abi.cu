@@ -59,7 +59,7 @@ enum SlotId {
     kSlotScaIndeg, kSlotScaConv, kSlotScaShip, kSlotScaFlags, kSlotScaCounters, kSlotBatchMaps,
     kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut,
     kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotMfdLayer0,
-    kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotStripSlow, kSlotCount
+    kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotStripSlow, kSlotLoadRows, kSlotCount
 };
 static_assert(kSlotCount <= 48, "context slot table");
 
@@ -1213,6 +1213,170 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
         return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: %llu nodata cells carry positive weights", ht[2]);
     if (ht[0] != ht[1])
         return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: %llu of %llu valid cells processed (cycle)", ht[1], ht[0]);
+    return PARGO_OK;
+}
+
+// ------------------------------------------------------------------ load --
+pargo_status pargo_compute_load_dims(int64_t rows, int64_t cols, int grain, int64_t* crows, int64_t* ccols) {
+    if (rows < 3 || cols < 3 || grain < 1 || !crows || !ccols) return PARGO_ERR_INVALID_ARG;
+    *crows = (rows - 2 + grain - 1) / grain;  // ComputeLayer::_init over the 3x3 work rectangle
+    *ccols = (cols - 2 + grain - 1) / grain;
+    return PARGO_OK;
+}
+
+pargo_status pargo_compute_load(pargo_ctx* ctx, int count, const pargo_raster* data, const pargo_nbr* nbr, int grain,
+                                int compute_ring, double nodata_load, double valid_load, pargo_raster* load,
+                                void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if (count < 1 || count > kMaxLoadLayers || !data)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: 1 to %d data rasters", kMaxLoadLayers);
+    if (grain < 1) return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: grain must be >= 1");
+    if (nodata_load < 0 || valid_load < 0)  // transformation.h:169-172
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: the loads cannot be negative");
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    for (int l = 0; l < count; l++) {
+        if ((st = check_raster(ctx, &data[l], "data")) != PARGO_OK) return st;
+        if (data[l].dtype != PARGO_F32 && data[l].dtype != PARGO_F64)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: data must be F32 or F64");
+        if (l && (data[l].rows != data[0].rows || data[l].cols != data[0].cols))
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: data rasters differ in shape");
+    }
+    if ((st = check_dims(ctx, &data[0])) != PARGO_OK) return st;
+    int64_t crows, ccols;
+    pargo_compute_load_dims(data[0].rows, data[0].cols, grain, &crows, &ccols);
+    if ((st = check_raster(ctx, load, "load")) != PARGO_OK) return st;
+    if (load->rows != crows || load->cols != ccols)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: load must be %lld x %lld", (long long)crows,
+                    (long long)ccols);
+    if (load->dtype != PARGO_F64 && load->dtype != PARGO_F32)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "compute_load: load must be F64 or F32");
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    LoadParams p{};
+    p.rows = data[0].rows;
+    p.cols = data[0].cols;
+    p.count = count;
+    Staged sd[kMaxLoadLayers], so;
+    bool host = false;
+    for (int l = 0; l < count; l++) {
+        if ((st = stage_in(ctx, &data[l], kSlotMfdLayer0 + l, s, &sd[l])) != PARGO_OK) return st;
+        p.data[l] = sd[l].in;
+        host = host || sd[l].host;
+    }
+    if ((st = stage_out(ctx, load, kSlotOut0, &so)) != PARGO_OK) return st;
+    for (int l = 0; l < count; l++) {  // each layer's own nodata; |v - nd| <= 1e-7 is nodata
+        p.ndf[l] = float_band_incl(data[l].nodata, 0.0000001);
+        long long klo, khi;
+        band_keys(double_band_incl(data[l].nodata, 0.0000001), &klo, &khi);
+        p.nd_lo[l] = klo;
+        p.nd_hi[l] = khi;
+    }
+    p.grain = grain;
+    p.compute_ring = compute_ring ? 1 : 0;
+    p.nodata_load = nodata_load;
+    p.valid_load = valid_load;
+    p.crows = crows;
+    p.ccols = ccols;
+    p.load = so.out;
+    CU(ctx, launch_compute_load(p, ctx->num_sms, s));
+    if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
+    return finish_call(ctx, s, host || so.host);
+}
+
+pargo_status pargo_load_decompose(pargo_ctx* ctx, const pargo_raster* load, int compute_ring, int64_t data_rows,
+                                  int64_t data_cols, const pargo_nbr* nbr, int nparts, int64_t* comp_rows,
+                                  int64_t* bounds, void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    pargo_status st;
+    if ((st = check_raster(ctx, load, "load")) != PARGO_OK) return st;
+    if (load->dtype != PARGO_F64 && load->dtype != PARGO_F32)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "load_decompose: load must be F64 or F32");
+    if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
+    if (data_rows < 3 || data_cols < 3 || data_rows > INT32_MAX || data_cols > INT32_MAX)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "load_decompose: bad data dimensions");
+    if (!bounds) return fail(ctx, PARGO_ERR_INVALID_ARG, "load_decompose: bounds is required");
+    const int64_t crows = load->rows, ccols = load->cols;
+    const int64_t work_rows = compute_ring ? crows - 2 : crows;
+    if (nparts < 1 || nparts > work_rows)  // deComposition.h:314-320
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "load_decompose: %d parts for %lld compute rows", nparts,
+                    (long long)work_rows);
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    Staged sl;
+    if ((st = stage_in(ctx, load, kSlotIn0, s, &sl)) != PARGO_OK) return st;
+    cudaError_t e;
+    double* drow = (double*)slot(ctx, kSlotLoadRows, (size_t)crows * sizeof(double), &e);
+    if (!drow) return cuda_fail(ctx, e, "row loads");
+    CU(ctx, launch_row_load(sl.in, crows, ccols, load->nodata, drow, ctx->num_sms, s));
+    std::vector<double> row_load((size_t)crows);
+    CU(ctx, cudaMemcpyAsync(row_load.data(), drow, (size_t)crows * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+    // DeComposition::valRowDcmp (gpro/deComposition.h:337-385): nparts-1 greedy
+    // cuts, each where the running load first passes the average of what is
+    // left, moved one row back when that is nearer the average.
+    double total = 0.0;
+    for (double v : row_load) total += v;
+    std::vector<int64_t> cb((size_t)nparts), ce((size_t)nparts);
+    double aver = total / nparts, accu = 0.0;
+    int64_t begin = 0;
+    int k = 0;
+    for (int i = 0; i < nparts - 1; i++) {
+        double sub = 0.0, min_diff = 0.0;
+        bool cut = false;
+        for (int64_t r = begin; r < crows; r++) {
+            sub += row_load[(size_t)r];
+            accu += row_load[(size_t)r];
+            const bool room = crows - 1 - r > nparts - 1 - i;  // rows left for the remaining parts
+            if (sub <= aver && room) {
+                if (fabs(min_diff) < 0.0000001 || (aver - sub) < min_diff) min_diff = aver - sub;
+                continue;
+            }
+            if (fabs(min_diff) < 0.0000001 || (sub - aver) <= min_diff || crows - 1 - r == nparts - 1 - i) {
+                cb[(size_t)k] = begin;
+                ce[(size_t)k++] = r;
+                begin = r + 1;
+            } else {  // the row before is nearer the average: this row opens the next part
+                accu -= row_load[(size_t)r];
+                cb[(size_t)k] = begin;
+                ce[(size_t)k++] = r - 1;
+                begin = r;
+            }
+            aver = (total - accu) / (nparts - i - 1);
+            cut = true;
+            break;
+        }
+        if (!cut) return fail(ctx, PARGO_ERR_INVALID_ARG, "load_decompose: the cuts ran out of rows");
+    }
+    cb[(size_t)k] = begin;
+    ce[(size_t)k] = crows - 1;
+    // ComputeLayer::getCompuLoad (gpro/computeLayer.h:402-430): compute rows to
+    // data rows of the data work rectangle, scaled by data rows / compute rows
+    // and truncated.
+    const double convert = (double)data_rows / (double)crows;
+    const int64_t wr0 = 1, wr1 = data_rows - 2, wc0 = 1, wc1 = data_cols - 2;
+    int64_t sub_end = wr0 - 1;
+    for (int i = 0; i < nparts; i++) {
+        if (comp_rows) {
+            comp_rows[2 * i] = cb[(size_t)i];
+            comp_rows[2 * i + 1] = ce[(size_t)i];
+        }
+        int64_t b0, b1;
+        if (i < nparts - 1) {
+            b0 = (int64_t)(int)((double)cb[(size_t)i] * convert + (double)wr0);
+            b1 = (int64_t)(int)((double)cb[(size_t)i + 1] * convert + (double)wr0 - 1.0);
+            sub_end = b1;
+        } else {
+            b0 = sub_end + 1;
+            b1 = wr1;
+        }
+        bounds[4 * i] = b0;
+        bounds[4 * i + 1] = wc0;
+        bounds[4 * i + 2] = b1;
+        bounds[4 * i + 3] = wc1;
+    }
     return PARGO_OK;
 }
 

@@ -187,9 +187,11 @@ __device__ __forceinline__ int d8_fast(float x0, float x1, float x2, float x3, f
     const uint32_t ub = prmt(prmt(__float_as_uint(d56.x), __float_as_uint(d56.y), 0x00FB),
                              prmt(__float_as_uint(d78.x), __float_as_uint(d78.y), 0x00FB), 0x5410);
     const uint32_t w = (ua & 0x55555555u) | (ub & 0xAAAAAAAAu);
-    const int hb = 31 - __clz(w);
-    const int k = (hb >> 3) + (hb & 1) * 5;  // byte b of ua -> window b, of ub -> window b + 5
-    return m < kLowCut ? -1 : (m > kHighCut && __popc(w) == 4) ? k : kD8Unsure;
+    uint32_t hb;
+    asm("bfind.u32 %0, %1;" : "=r"(hb) : "r"(w));  // position of the highest set bit
+    const int k = (int)((hb >> 3) + (hb & 1) * 5);  // byte b of ua -> window b, of ub -> window b + 5
+    const bool sure = (m > kHighCut) & (__popc(w) == 4);  // no short-circuit branch
+    return m < kLowCut ? -1 : sure ? k : kD8Unsure;
 }
 #endif
 

@@ -32,6 +32,23 @@ struct FocalParams {
     int* error_flag;                // device flag: a bounded wait gave up
 };
 
+// load.cu: the load estimator (compute-intensity layer, row loads).
+constexpr int kMaxLoadLayers = 8;
+struct LoadParams {
+    int64_t rows, cols;            // data rasters
+    int count;                     // data layers summed
+    InView data[kMaxLoadLayers];
+    Band<float> ndf[kMaxLoadLayers];               // per layer: |v - nodata| <= 1e-7 for float data
+    long long nd_lo[kMaxLoadLayers], nd_hi[kMaxLoadLayers];  // the same bands as keys for double data
+    int grain, compute_ring;
+    double nodata_load, valid_load;
+    int64_t crows, ccols;
+    OutView load;
+};
+cudaError_t launch_compute_load(const LoadParams& p, int num_sms, cudaStream_t s);
+cudaError_t launch_row_load(const InView& load, int64_t crows, int64_t ccols, double nodata, double* row_load,
+                            int num_sms, cudaStream_t s);
+
 // focal.cu
 cudaError_t launch_focal_tma(const CUtensorMap* map, const FocalParams& p, int fast_out, int variant, int num_sms,
                              cudaStream_t s);

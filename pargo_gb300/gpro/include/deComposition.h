@@ -1,3 +1,3 @@
-// deComposition.h -- include name of the reference framework (gpro/deComposition.h); the GPU
-// build's declarations all live in gpro/gpro.h.
-#include "gpro/gpro.h"
+// deComposition.h -- include name of the reference header; the load estimator is
+// declared in gpro/load.h.
+#include "gpro/load.h"

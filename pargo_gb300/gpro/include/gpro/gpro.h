@@ -329,6 +329,18 @@ public:
         return true;
     }
 
+    // gpro/rasterLayer.h: a neighbourhood of the cell itself (no halo).
+    bool newLocalNbrhood() {
+        newNbrhood();
+        return _pNbrhood->parse("1\n0 0 1.0\n");
+    }
+    // A new cell space of the metadata's local dims, every cell `init`.
+    bool newCellSpace(const SpaceDims& dims, elemType init) {
+        delete _pCellSpace;
+        _pCellSpace = new CellSpace<elemType>(dims, init);
+        return true;
+    }
+
     // gpro/rasterLayer.h:739-745: same metadata and neighbourhood, cells = nodata.
     bool copyLayerInfo(const RasterLayer<elemType>& rhs) {
         if (!rhs._pMetaData) return false;

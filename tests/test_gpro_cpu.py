@@ -34,6 +34,16 @@ def test_gpro_selftest(tmp_path):
     assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr
 
 
+def test_load_estimator_classes_compile(tmp_path):
+    """The gpro ComputeLayer / Transformation / DeComposition headers with an
+    estimate-function subclass (tests/cpp/load_selftest.cpp) build and link."""
+    exe = tmp_path / "load_selftest"
+    cmd = ["g++", "-std=c++14", "-O1", "-Wall"] + ["-I" + d for d in INC] + \
+          [os.path.join(ROOT, "tests", "cpp", "load_selftest.cpp"), "-o", str(exe)] + _link_args()
+    subprocess.run(cmd, check=True)
+    assert os.access(exe, os.X_OK)
+
+
 def test_tiff_written_by_python_reads_in_cpp_and_back(tmp_path):
     from tiff_io import read_tiff, write_tiff
     a = (np.arange(60, dtype=np.float32).reshape(6, 10) * 1.5 - 7).astype(np.float32)

@@ -154,3 +154,31 @@ def test_oracle_mfd_matches_reference_binary(slp_exp, oracle_lib):
     b = R.mfd(w, -9999.0, 30.0, slp_exp)
     assert bits_equal(a.reshape(8, -1), b.reshape(8, -1))
     assert bits_equal(O.sca_mfd(b, -9999.0), R.sca_mfd(b, -9999.0))
+
+
+@pytest.mark.parametrize("shape,grain,ring,nparts,loads", [
+    ((203, 157), 1, False, 5, (0.0, 1.0)),
+    ((203, 157), 4, False, 7, (0.3, 1.7)),
+    ((120, 333), 10, True, 3, (0.0, 1.0)),
+    ((97, 61), 7, True, 9, (2.5, 0.25)),
+    ((64, 64), 16, False, 2, (1.0, 1.0)),
+    ((300, 40), 3, False, 90, (0.1, 3.0)),
+])
+def test_oracle_load_matches_reference_binary(shape, grain, ring, nparts, loads, oracle_lib):
+    """The load estimator: the intensity-ratio compute layer (ComputeLayer +
+    Transformation) bit for bit, the valRowDcmp cuts and getCompuLoad's data
+    rows for rank 0, against the reference gpro classes on a DEM with a nodata
+    blob and a nodata border."""
+    from pargo_gb300 import synth
+    R = _ref()
+    dem = synth.hydro_dem(shape[0], shape[1], seed=shape[0] + grain, blob_fraction=0.2)
+    dem[0, :] = -9999.0
+    ref, comp, rank0 = R.compute_load(dem, -9999.0, grain, loads[0], loads[1], ring, nparts=nparts)
+    got = oracle_lib.compute_load(dem, -9999.0, grain, loads[0], loads[1], ring)
+    assert bits_equal(got, ref)
+    oc, ob = oracle_lib.load_decompose(got, -9999.0, shape, nparts, ring)
+    assert np.array_equal(oc, comp)
+    assert np.array_equal(ob[0], rank0)
+    # the parts tile the data work rectangle
+    assert ob[0, 0] == 1 and ob[-1, 2] == shape[0] - 2
+    assert all(ob[i + 1, 0] == ob[i, 2] + 1 for i in range(nparts - 1))
