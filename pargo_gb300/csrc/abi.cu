@@ -1277,6 +1277,13 @@ pargo_status pargo_compute_load(pargo_ctx* ctx, int count, const pargo_raster* d
     p.compute_ring = compute_ring ? 1 : 0;
     p.nodata_load = nodata_load;
     p.valid_load = valid_load;
+    {
+        // sums of integer loads below 2^53 are exact in any order
+        const double mx = std::max(nodata_load, valid_load);
+        const double cells = (double)count * grain * grain;
+        p.integral = nodata_load == std::floor(nodata_load) && valid_load == std::floor(valid_load) &&
+                     mx * cells < 9007199254740992.0;
+    }
     p.crows = crows;
     p.ccols = ccols;
     p.load = so.out;

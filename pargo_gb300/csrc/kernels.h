@@ -42,6 +42,7 @@ struct LoadParams {
     long long nd_lo[kMaxLoadLayers], nd_hi[kMaxLoadLayers];  // the same bands as keys for double data
     int grain, compute_ring;
     double nodata_load, valid_load;
+    int integral;                  // integer loads whose sums stay below 2^53: count, then scale
     int64_t crows, ccols;
     OutView load;
 };

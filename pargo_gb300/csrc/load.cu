@@ -42,10 +42,21 @@ __global__ void __launch_bounds__(256) compute_load_kernel(const LoadParams p) {
         const bool work = !p.compute_ring || (cr >= 1 && cc >= 1 && cr <= p.crows - 2 && cc <= p.ccols - 2);
         if (work) {
             const int64_t r_end = min((cr + 1) * p.grain + 1, p.rows), c_end = min((cc + 1) * p.grain + 1, p.cols);
-            for (int l = 0; l < p.count; l++)
-                for (int64_t r = cr * p.grain + 1; r < r_end; r++)
-                    for (int64_t c = cc * p.grain + 1; c < c_end; c++)
-                        acc = __dadd_rn(acc, load_nodata(p, l, r, c) ? p.nodata_load : p.valid_load);
+            if (p.integral) {
+                // integer loads: every partial sum is an integer below 2^53, so
+                // the sequential sum is exact and equals counts times loads
+                long long nd = 0, total = 0;
+                for (int l = 0; l < p.count; l++)
+                    for (int64_t r = cr * p.grain + 1; r < r_end; r++)
+                        for (int64_t c = cc * p.grain + 1; c < c_end; c++) nd += load_nodata(p, l, r, c) ? 1 : 0;
+                total = (long long)p.count * (r_end - (cr * p.grain + 1)) * (c_end - (cc * p.grain + 1));
+                acc = __dadd_rn(__dmul_rn((double)(total - nd), p.valid_load), __dmul_rn((double)nd, p.nodata_load));
+            } else {
+                for (int l = 0; l < p.count; l++)
+                    for (int64_t r = cr * p.grain + 1; r < r_end; r++)
+                        for (int64_t c = cc * p.grain + 1; c < c_end; c++)
+                            acc = __dadd_rn(acc, load_nodata(p, l, r, c) ? p.nodata_load : p.valid_load);
+            }
         }
         put_value(p.load, cr, cc, acc);
     }
