@@ -39,7 +39,8 @@ MEASURED_PEAKS = os.path.join(HERE, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 # dram__bytes_read.sum + dram__bytes_write.sum per cell of focal_tma_kernel,
 # from its ncu capture on 8192^2 (301.3 MB + 289.3 MB over 67108864 cells)
-FOCAL_DRAM_BYTES_PER_CELL = (301.330688e6 + 289.264128e6) / 67108864
+FOCAL_DRAM_BYTES_PER_CELL = (301.330688e6 + 289.264128e6) / 67108864   # tiled kernel, 8192^2 ncu capture
+STRIP_DRAM_BYTES_PER_CELL = (289.425152e6 + 284.340224e6) / 67108864   # strip walk, 8192^2 ncu capture
 
 
 def hbm_peak():
@@ -293,6 +294,8 @@ def run_slope(args, ws, rank, local, side):
     rd, rs, rc = R(d, ND, 30.0), R(s, ND), R(c, -128)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if cells * 9 < (256 << 20) else None
     best, tune_ms = ctx.tune_focal(rd, reps=3)
+    forced = os.environ.get("PARGO_FOCAL_VARIANT")
+    strip = (int(forced) if forced else best) >= 5   # variants 5 and 6: the strip walk
     for _ in range(args.warmup):
         ctx.slope_d8(rd, rs, rc, stream=stream)
     torch.cuda.synchronize()
@@ -321,11 +324,12 @@ def run_slope(args, ws, rank, local, side):
         "FP64 fallback)", "data": "synthetic",
         "config": {"workload": "slope%d: fused Horn slope + D8, %dx%d float32 fBm DEM" % (side, side, side),
                    "l2": "flushed between iterations" if flush is not None else "inputs larger than L2"},
-        "roofline": {"bound": "hbm", "kernel": "focal_tma_kernel", "achieved": round(achieved, 1), "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "focal_strip_kernel" if strip else "focal_tma_kernel",
+                     "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
-                     # DRAM read + write of one launch, scaled by cells from the 8192^2 ncu capture
-                     # (590.6 MB per 67.1 M cells; the traffic grows with the cell count)
-                     "traffic": round(FOCAL_DRAM_BYTES_PER_CELL * cells),
+                     # DRAM read + write of one launch, scaled by cells from the 8192^2 ncu capture of the
+                     # same kernel (the traffic grows with the cell count)
+                     "traffic": round((STRIP_DRAM_BYTES_PER_CELL if strip else FOCAL_DRAM_BYTES_PER_CELL) * cells),
                      "traffic_source": "ncu 8192^2 capture scaled per cell", "variant": best, "variant_ms": tune_ms},
         "gpu_launches": args.steps, "clocks": clk,
     }
