@@ -613,13 +613,16 @@ struct SPair {
     float e2[5];
 };
 
+// ND: the row's own nodata test; without it the caller knows the row's stage
+// holds no value in the nodata band.
+template <bool ND = true>
 __device__ __forceinline__ void s_load_row(const float* row, int lane, SRow& r, const Band<float>& nd6) {
     const float* q = row + 4 * lane + 3;
     const float4 c = *reinterpret_cast<const float4*>(q + 1);
     r.v[0] = q[0]; r.v[1] = c.x; r.v[2] = c.y; r.v[3] = c.z; r.v[4] = c.w; r.v[5] = q[5];
 #pragma unroll
     for (int j = 0; j < 4; j++) r.sh[j] = __fsub_rn(r.v[j + 2], r.v[j]);
-    r.nd = row6_maybe_nodata(r.v, nd6);
+    r.nd = ND ? row6_maybe_nodata(r.v, nd6) : false;
 }
 
 __device__ __forceinline__ void s_pair(const SRow& u, const SRow& l, SPair& p) {
@@ -636,24 +639,24 @@ __device__ __forceinline__ void s_pair(const SRow& u, const SRow& l, SPair& p) {
 // Where the fast path cannot finish a lane's four cells of a row (the ring,
 // windows that may touch nodata, uncertain D8, lanes at the raster's edge),
 // the (row, lane) goes to a device list -- index y * lanes_per_row + gx0 / 4,
-// appended once per warp by a single atomic -- and strip_fixup_kernel
-// recomputes those cells afterwards through the general path.
+// collected as one bit per row through a stage and appended after it -- and
+// strip_fixup_kernel recomputes those cells afterwards through the general
+// path.
 struct SlowList {
     uint32_t* items;
     unsigned long long* count;
     int64_t lanes_per_row;  // ceil(cols / 4)
-    int64_t cols;
 };
 
 // Output row y from the window rows A (y-1), B (y), C (y+1); C is loaded
 // here from stage row `crow`, and the pair B/C is formed for the next row.
 // `sp` / `dp` point to this lane's four slope / code cells of row y.  Only the
 // plain configuration runs here (Horn, rise/run, dirType 8).
-template <bool SLOPE, bool D8>
+template <bool SLOPE, bool D8, bool ND>
 __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, SRow& C, const SPair& PAB, SPair& PBC,
                                            int y, int rows, int64_t gx0, bool lane_int, float k_fd, const Band<float>& nd6,
-                                           char* sp, char* dp, int lane, const SlowList& slow) {
-    s_load_row(crow, lane, C, nd6);
+                                           char* sp, char* dp, uint32_t& pend, int64_t cols) {
+    s_load_row<ND>(crow, threadIdx.x & 31, C, nd6);
     s_pair(B, C, PBC);
     float sl[4];
     int cd[4];
@@ -689,15 +692,34 @@ __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, 
             *reinterpret_cast<uint32_t*>(dp) = __byte_perm(__byte_perm((uint32_t)cd[0], (uint32_t)cd[1], 0x0040),
                                                           __byte_perm((uint32_t)cd[2], (uint32_t)cd[3], 0x0040), 0x5410);
     }
-    const bool slow_here = live & !fast & (gx0 < slow.cols);
-    const unsigned m = __ballot_sync(0xffffffffu, slow_here);
-    if (m) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(slow.count, (unsigned long long)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (slow_here)
-            slow.items[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)((int64_t)y * slow.lanes_per_row + (gx0 >> 2));
+    // one bit per row of the stage, shifted in (the stage's first row ends highest)
+    pend = (pend << 1) | (uint32_t)(live & !fast & (gx0 < cols));
+}
+
+// Appends the (row, lane) items of a stage's rows the fast path left (bit b
+// of `pend`: row y_last - b), one atomic per lane that has any.
+__device__ __noinline__ void strip_flush(uint32_t pend, int y_last, int64_t gx0, const SlowList slow) {
+    unsigned long long base = atomicAdd(slow.count, (unsigned long long)__popc(pend));
+    while (pend) {
+        const int b = __ffs(pend) - 1;
+        pend &= pend - 1;
+        slow.items[base++] = (uint32_t)((int64_t)(y_last - b) * slow.lanes_per_row + (gx0 >> 2));
     }
+}
+
+// Whether any value of a stage (kSR rows of the box) may lie in the nodata
+// band: the warp's lanes scan it as float4 and vote.
+__device__ __forceinline__ bool stage_maybe_nodata(const float* st, const Band<float>& b) {
+    const float4* s4 = reinterpret_cast<const float4*>(st);
+    constexpr int kQuads = kSR * kBoxW / 4;
+    float mn = INFINITY, mx = -INFINITY;
+#pragma unroll
+    for (int q = threadIdx.x & 31; q < kQuads; q += 32) {
+        const float4 v = s4[q];
+        mn = fmin3f(fmin3f(v.x, v.y, v.z), v.w, mn);
+        mx = fmax3f(fmax3f(v.x, v.y, v.z), v.w, mx);
+    }
+    return __any_sync(0xffffffffu, (mn <= b.hi) & (mx >= b.lo));
 }
 
 // Warp-uniform bounded wait on an mbarrier phase.
@@ -787,20 +809,39 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
                 return;
             }
             sphase ^= 1u << buf;
+            const int64_t spp = SLOPE ? p.slope.pitch : 0, dpp = D8 ? p.d8.pitch : 0;
+            uint32_t pend = 0;
+            const int ys = (int)y0 + k * kSR;
+            if (stage_maybe_nodata(stage(buf), p.nd6f)) {
 #pragma unroll 1
-            for (int t = 0; t < kSR; t += 3) {
-                const float* st = stage(buf) + t * kBoxW;
-                const int y = (int)y0 + k * kSR + t;
-                const int64_t spp = SLOPE ? p.slope.pitch : 0, dpp = D8 ? p.d8.pitch : 0;
-                strip_step<SLOPE, D8>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp, lane,
-                                      slow);
-                strip_step<SLOPE, D8>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd, p.nd6f,
-                                      sp + spp, dp + dpp, lane, slow);
-                strip_step<SLOPE, D8>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd, p.nd6f,
-                                      sp + 2 * spp, dp + 2 * dpp, lane, slow);
-                sp += 3 * spp;
-                dp += 3 * dpp;
+                for (int t = 0; t < kSR; t += 3) {
+                    const float* st = stage(buf) + t * kBoxW;
+                    const int y = ys + t;
+                    strip_step<SLOPE, D8, true>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
+                                                pend, p.cols);
+                    strip_step<SLOPE, D8, true>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd,
+                                                p.nd6f, sp + spp, dp + dpp, pend, p.cols);
+                    strip_step<SLOPE, D8, true>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
+                                                p.nd6f, sp + 2 * spp, dp + 2 * dpp, pend, p.cols);
+                    sp += 3 * spp;
+                    dp += 3 * dpp;
+                }
+            } else {  // no value of the stage in the nodata band: its rows skip the test
+#pragma unroll 1
+                for (int t = 0; t < kSR; t += 3) {
+                    const float* st = stage(buf) + t * kBoxW;
+                    const int y = ys + t;
+                    strip_step<SLOPE, D8, false>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
+                                                 pend, p.cols);
+                    strip_step<SLOPE, D8, false>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd,
+                                                 p.nd6f, sp + spp, dp + dpp, pend, p.cols);
+                    strip_step<SLOPE, D8, false>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
+                                                 p.nd6f, sp + 2 * spp, dp + 2 * dpp, pend, p.cols);
+                    sp += 3 * spp;
+                    dp += 3 * dpp;
+                }
             }
+            if (pend) strip_flush(pend, ys + kSR - 1, gx0, slow);
             __syncwarp();
             // refill this buffer with the item two ahead
             if (k + 2 < kSegStages) {
@@ -929,7 +970,7 @@ static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap*
     const int64_t need = (nsegs + kSWarps - 1) / kSWarps;
     if (grid > need) grid = need;
     if ((e = cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
-    const SlowList slow{slow_items, counters + 1, (p.cols + 3) / 4, p.cols};
+    const SlowList slow{slow_items, counters + 1, (p.cols + 3) / 4};
     kern<<<(unsigned)grid, kSWarps * 32, smem, s>>>(*map_stage, *map_prime, p, nstrips, nsegs, counters, slow);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     strip_fixup_kernel<<<(unsigned)num_sms * 4, 128, 0, s>>>(dem, p, slow);
