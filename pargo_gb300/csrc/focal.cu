@@ -652,11 +652,13 @@ struct SlowList {
 // here from stage row `crow`, and the pair B/C is formed for the next row.
 // `sp` / `dp` point to this lane's four slope / code cells of row y.  Only the
 // plain configuration runs here (Horn, rise/run, dirType 8).
-template <bool SLOPE, bool D8, bool ND>
+// CLEAN: the stage lies inside the raster's ring and holds no value in the
+// nodata band, so the row needs neither test.
+template <bool SLOPE, bool D8, bool CLEAN>
 __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, SRow& C, const SPair& PAB, SPair& PBC,
                                            int y, int rows, int64_t gx0, bool lane_int, float k_fd, const Band<float>& nd6,
                                            char* sp, char* dp, uint32_t& pend, int64_t cols) {
-    s_load_row<ND>(crow, threadIdx.x & 31, C, nd6);
+    s_load_row<!CLEAN>(crow, threadIdx.x & 31, C, nd6);
     s_pair(B, C, PBC);
     float sl[4];
     int cd[4];
@@ -684,21 +686,24 @@ __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, 
             sure &= ok;
         }
     }
-    const bool live = y < rows;
-    const bool fast = lane_int & ((unsigned)(y - 1) < (unsigned)(rows - 2)) & !(A.nd | B.nd | C.nd) & sure;
+    const bool live = CLEAN || y < rows;
+    const bool fast = CLEAN ? lane_int & !(A.nd | B.nd) & sure
+                            : lane_int & ((unsigned)(y - 1) < (unsigned)(rows - 2)) & !(A.nd | B.nd | C.nd) & sure;
     if (live & fast) {
         if (SLOPE) *reinterpret_cast<float4*>(sp) = make_float4(sl[0], sl[1], sl[2], sl[3]);
         if (D8)
             *reinterpret_cast<uint32_t*>(dp) = __byte_perm(__byte_perm((uint32_t)cd[0], (uint32_t)cd[1], 0x0040),
                                                           __byte_perm((uint32_t)cd[2], (uint32_t)cd[3], 0x0040), 0x5410);
     }
-    // one bit per row of the stage, shifted in (the stage's first row ends highest)
-    pend = (pend << 1) | (uint32_t)(live & !fast & (gx0 < cols));
+    // one bit per row of the stage, shifted in (the stage's first row ends
+    // highest); lanes past the raster's last column are dropped at the flush
+    pend = pend * 2u + (uint32_t)(live & !fast);
 }
 
 // Appends the (row, lane) items of a stage's rows the fast path left (bit b
 // of `pend`: row y_last - b), one atomic per lane that has any.
 __device__ __noinline__ void strip_flush(uint32_t pend, int y_last, int64_t gx0, const SlowList slow) {
+    if ((gx0 >> 2) >= slow.lanes_per_row) return;  // past the raster's last column
     unsigned long long base = atomicAdd(slow.count, (unsigned long long)__popc(pend));
     while (pend) {
         const int b = __ffs(pend) - 1;
@@ -812,30 +817,31 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
             const int64_t spp = SLOPE ? p.slope.pitch : 0, dpp = D8 ? p.d8.pitch : 0;
             uint32_t pend = 0;
             const int ys = (int)y0 + k * kSR;
-            if (stage_maybe_nodata(stage(buf), p.nd6f)) {
-#pragma unroll 1
-                for (int t = 0; t < kSR; t += 3) {
-                    const float* st = stage(buf) + t * kBoxW;
-                    const int y = ys + t;
-                    strip_step<SLOPE, D8, true>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
-                                                pend, p.cols);
-                    strip_step<SLOPE, D8, true>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd,
-                                                p.nd6f, sp + spp, dp + dpp, pend, p.cols);
-                    strip_step<SLOPE, D8, true>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
-                                                p.nd6f, sp + 2 * spp, dp + 2 * dpp, pend, p.cols);
-                    sp += 3 * spp;
-                    dp += 3 * dpp;
-                }
-            } else {  // no value of the stage in the nodata band: its rows skip the test
+            const bool inside = (ys >= 1) & (ys + kSR - 1 <= rows - 2);
+            if (stage_maybe_nodata(stage(buf), p.nd6f) | !inside) {
 #pragma unroll 1
                 for (int t = 0; t < kSR; t += 3) {
                     const float* st = stage(buf) + t * kBoxW;
                     const int y = ys + t;
                     strip_step<SLOPE, D8, false>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
-                                                 pend, p.cols);
+                                                pend, p.cols);
                     strip_step<SLOPE, D8, false>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd,
-                                                 p.nd6f, sp + spp, dp + dpp, pend, p.cols);
+                                                p.nd6f, sp + spp, dp + dpp, pend, p.cols);
                     strip_step<SLOPE, D8, false>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
+                                                p.nd6f, sp + 2 * spp, dp + 2 * dpp, pend, p.cols);
+                    sp += 3 * spp;
+                    dp += 3 * dpp;
+                }
+            } else {  // inside the ring, no value in the nodata band: the rows skip both tests
+#pragma unroll 1
+                for (int t = 0; t < kSR; t += 3) {
+                    const float* st = stage(buf) + t * kBoxW;
+                    const int y = ys + t;
+                    strip_step<SLOPE, D8, true>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
+                                                 pend, p.cols);
+                    strip_step<SLOPE, D8, true>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd,
+                                                 p.nd6f, sp + spp, dp + dpp, pend, p.cols);
+                    strip_step<SLOPE, D8, true>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
                                                  p.nd6f, sp + 2 * spp, dp + 2 * dpp, pend, p.cols);
                     sp += 3 * spp;
                     dp += 3 * dpp;
