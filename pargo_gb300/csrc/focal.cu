@@ -866,21 +866,20 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
     }
 }
 
-// The (row, lane) items the strip walk left: each lane's four cells through
-// cell_general on the window read from the DEM.
+// The (row, lane) items the strip walk left: their cells, one thread each,
+// through cell_general on the window read from the DEM.
 __global__ void __launch_bounds__(128) strip_fixup_kernel(const InView dem, const __grid_constant__ FocalParams p,
                                                           const SlowList slow) {
-    const unsigned long long n = *((volatile unsigned long long*)slow.count);
+    const unsigned long long n = *((volatile unsigned long long*)slow.count) * 4;  // one thread per cell
     int fell_back = 0;
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
-        const uint32_t e = slow.items[i];
+        const uint32_t e = slow.items[i >> 2];
         const int64_t y = (int64_t)(e / (uint64_t)slow.lanes_per_row);
         const int64_t gx0 = (int64_t)(e % (uint64_t)slow.lanes_per_row) * 4;
-#pragma unroll 1
-        for (int j = 0; j < 4; j++) {
-            const int64_t gx = gx0 + j;
-            if (gx >= p.cols) break;
+        {
+            const int64_t gx = gx0 + (int64_t)(i & 3);
+            if (gx >= p.cols) continue;
             const bool ring = y <= 0 || gx <= 0 || y >= p.rows - 1 || gx >= p.cols - 1;
             float z[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
             if (!ring) {
@@ -979,7 +978,7 @@ static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap*
     const SlowList slow{slow_items, counters + 1, (p.cols + 3) / 4};
     kern<<<(unsigned)grid, kSWarps * 32, smem, s>>>(*map_stage, *map_prime, p, nstrips, nsegs, counters, slow);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    strip_fixup_kernel<<<(unsigned)num_sms * 4, 128, 0, s>>>(dem, p, slow);
+    strip_fixup_kernel<<<(unsigned)num_sms * 8, 128, 0, s>>>(dem, p, slow);
     return cudaGetLastError();
 }
 
