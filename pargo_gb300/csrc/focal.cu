@@ -714,10 +714,21 @@ __device__ __noinline__ void strip_flush(uint32_t pend, int y_last, int64_t gx0,
 
 // Whether any value of a stage (kSR rows of the box) may lie in the nodata
 // band: the warp's lanes scan it as float4 and vote.
+// A band below zero (the usual negative nodata) needs only the minimum: a
+// stage with values below the band is flagged too, which only sends it
+// through the per-row tests.
 __device__ __forceinline__ bool stage_maybe_nodata(const float* st, const Band<float>& b) {
     const float4* s4 = reinterpret_cast<const float4*>(st);
     constexpr int kQuads = kSR * kBoxW / 4;
     float mn = INFINITY, mx = -INFINITY;
+    if (b.hi < 0.0f) {
+#pragma unroll
+        for (int q = threadIdx.x & 31; q < kQuads; q += 32) {
+            const float4 v = s4[q];
+            mn = fmin3f(fmin3f(v.x, v.y, v.z), v.w, mn);
+        }
+        return __any_sync(0xffffffffu, mn <= b.hi);
+    }
 #pragma unroll
     for (int q = threadIdx.x & 31; q < kQuads; q += 32) {
         const float4 v = s4[q];
