@@ -652,8 +652,9 @@ struct SlowList {
 // here from stage row `crow`, and the pair B/C is formed for the next row.
 // `sp` / `dp` point to this lane's four slope / code cells of row y.  Only the
 // plain configuration runs here (Horn, rise/run, dirType 8).
-// CLEAN: the stage lies inside the raster's ring and holds no value in the
-// nodata band, so the row needs neither test.
+// CLEAN: the stage lies inside the raster's ring, holds no value in the
+// nodata band and follows two rows without one, so the row needs none of the
+// tests.
 template <bool SLOPE, bool D8, bool CLEAN>
 __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, SRow& C, const SPair& PAB, SPair& PBC,
                                            int y, int rows, int64_t gx0, bool lane_int, float k_fd, const Band<float>& nd6,
@@ -687,7 +688,7 @@ __device__ __forceinline__ void strip_step(const float* crow, SRow& A, SRow& B, 
         }
     }
     const bool live = CLEAN || y < rows;
-    const bool fast = CLEAN ? lane_int & !(A.nd | B.nd) & sure
+    const bool fast = CLEAN ? lane_int & sure
                             : lane_int & ((unsigned)(y - 1) < (unsigned)(rows - 2)) & !(A.nd | B.nd | C.nd) & sure;
     if (live & fast) {
         if (SLOPE) *reinterpret_cast<float4*>(sp) = make_float4(sl[0], sl[1], sl[2], sl[3]);
@@ -714,10 +715,11 @@ __device__ __noinline__ void strip_flush(uint32_t pend, int y_last, int64_t gx0,
 
 // Whether any value of a stage (kSR rows of the box) may lie in the nodata
 // band: the warp's lanes scan it as float4 and vote.
-// A band below zero (the usual negative nodata) needs only the minimum: a
-// stage with values below the band is flagged too, which only sends it
-// through the per-row tests.
-__device__ __forceinline__ bool stage_maybe_nodata(const float* st, const Band<float>& b) {
+// This lane's share of the stage scan: whether any of its quarter-rows may
+// hold a value in the nodata band.  A band below zero (the usual negative
+// nodata) needs only the minimum: a stage with values below the band is
+// flagged too, which only sends it through the per-row tests.
+__device__ __forceinline__ bool stage_lane_maybe_nodata(const float* st, const Band<float>& b) {
     const float4* s4 = reinterpret_cast<const float4*>(st);
     constexpr int kQuads = kSR * kBoxW / 4;
     float mn = INFINITY, mx = -INFINITY;
@@ -727,7 +729,7 @@ __device__ __forceinline__ bool stage_maybe_nodata(const float* st, const Band<f
             const float4 v = s4[q];
             mn = fmin3f(fmin3f(v.x, v.y, v.z), v.w, mn);
         }
-        return __any_sync(0xffffffffu, mn <= b.hi);
+        return mn <= b.hi;
     }
 #pragma unroll
     for (int q = threadIdx.x & 31; q < kQuads; q += 32) {
@@ -735,7 +737,7 @@ __device__ __forceinline__ bool stage_maybe_nodata(const float* st, const Band<f
         mn = fmin3f(fmin3f(v.x, v.y, v.z), v.w, mn);
         mx = fmax3f(fmax3f(v.x, v.y, v.z), v.w, mx);
     }
-    return __any_sync(0xffffffffu, (mn <= b.hi) & (mx >= b.lo));
+    return (mn <= b.hi) & (mx >= b.lo);
 }
 
 // Warp-uniform bounded wait on an mbarrier phase.
@@ -829,7 +831,8 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
             uint32_t pend = 0;
             const int ys = (int)y0 + k * kSR;
             const bool inside = (ys >= 1) & (ys + kSR - 1 <= rows - 2);
-            if (stage_maybe_nodata(stage(buf), p.nd6f) | !inside) {
+            // one vote: the stage's values and the two rows above it
+            if (__any_sync(0xffffffffu, stage_lane_maybe_nodata(stage(buf), p.nd6f) | A.nd | B.nd) | !inside) {
 #pragma unroll 1
                 for (int t = 0; t < kSR; t += 3) {
                     const float* st = stage(buf) + t * kBoxW;
@@ -843,7 +846,7 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
                     sp += 3 * spp;
                     dp += 3 * dpp;
                 }
-            } else {  // inside the ring, no value in the nodata band: the rows skip both tests
+            } else {  // inside the ring, no nodata in any row it reads: the rows skip the tests
 #pragma unroll 1
                 for (int t = 0; t < kSR; t += 3) {
                     const float* st = stage(buf) + t * kBoxW;
