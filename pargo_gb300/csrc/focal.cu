@@ -772,30 +772,38 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
         if (lane == 0) v = atomicAdd(claim, 1ULL);
         return (int64_t)__shfl_sync(0xffffffffu, v, 0);
     };
-    auto issue_prime = [&](int64_t seg, int buf) {
+    // a segment's first column and first output row (segment ids fit 32 bits:
+    // the launcher requires rows * ceil(cols / 4) < 2^32), computed once
+    struct Origin {
+        int x0, y0;
+    };
+    const uint32_t ns32 = (uint32_t)nstrips;
+    auto origin = [&](int64_t seg) {
+        const uint32_t sg = (uint32_t)seg;
+        return Origin{(int)((sg % ns32) * kTW), (int)((sg / ns32) * kSegRows)};
+    };
+    auto issue_prime = [&](const Origin& o, int buf) {
         if (lane == 0) {
-            const int64_t x0 = (seg % nstrips) * kTW, y0 = (seg / nstrips) * kSegRows;
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&bar[2 + buf], kSPrimeBytes);
-            tma_load_2d(prime(buf), &map_prime, (int32_t)(x0 - 4), (int32_t)(y0 - 1), &bar[2 + buf]);
+            tma_load_2d(prime(buf), &map_prime, o.x0 - 4, o.y0 - 1, &bar[2 + buf]);
         }
     };
-    auto issue_stage = [&](int64_t seg, int k, int buf) {
+    auto issue_stage = [&](const Origin& o, int k, int buf) {
         if (lane == 0) {
-            const int64_t x0 = (seg % nstrips) * kTW, y0 = (seg / nstrips) * kSegRows;
-            int64_t yb = y0 + 1 + (int64_t)k * kSR;
-            if (yb > box_y_max) yb = box_y_max;  // rows past the raster: never stored
+            const int yb = min(o.y0 + 1 + k * kSR, (int)box_y_max);  // rows past the raster: never stored
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&bar[buf], kSStageBytes);
-            tma_load_2d(stage(buf), &map_stage, (int32_t)(x0 - 4), (int32_t)yb, &bar[buf]);
+            tma_load_2d(stage(buf), &map_stage, o.x0 - 4, yb, &bar[buf]);
         }
     };
 
     int64_t cur = claim_seg();
     if (cur >= nsegs) return;
-    issue_prime(cur, 0);
-    issue_stage(cur, 0, 0);
-    issue_stage(cur, 1, 1);
+    Origin co = origin(cur);
+    issue_prime(co, 0);
+    issue_stage(co, 0, 0);
+    issue_stage(co, 1, 1);
     uint32_t sphase = 0, pphase = 0;
     int pb = 0;
     SRow A, B, C;
@@ -805,12 +813,13 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
     // the fast path's configuration: Horn rise/run slope, dirType 8, vector stores
     const bool plain = p.fd && p.fast_out && !p.sk.degrees && (!D8 || p.dir_type == 8);
     while (true) {
-        const int64_t x0 = (cur % nstrips) * kTW, y0 = (cur / nstrips) * kSegRows;
+        const int64_t x0 = co.x0, y0 = co.y0;
         const int64_t gx0 = x0 + 4 * lane;
         const bool lane_int = plain && gx0 >= 1 && gx0 + 4 <= p.cols - 1;
         char* sp = SLOPE ? p.slope.base + y0 * p.slope.pitch + 4 * gx0 : nullptr;
         char* dp = D8 ? p.d8.base + y0 * p.d8.pitch + gx0 : nullptr;
         int64_t nxt = nsegs;
+        Origin no = co;
         if (!warp_wait(&bar[2 + pb], (pphase >> pb) & 1u)) {
             if (lane == 0 && p.error_flag) atomicExch(p.error_flag, 1);
             return;
@@ -865,17 +874,21 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
             __syncwarp();
             // refill this buffer with the item two ahead
             if (k + 2 < kSegStages) {
-                issue_stage(cur, k + 2, buf);
+                issue_stage(co, k + 2, buf);
             } else {
                 if (k + 2 == kSegStages) {
                     nxt = claim_seg();
-                    if (nxt < nsegs) issue_prime(nxt, pb ^ 1);
+                    if (nxt < nsegs) {
+                        no = origin(nxt);
+                        issue_prime(no, pb ^ 1);
+                    }
                 }
-                if (nxt < nsegs) issue_stage(nxt, k + 2 - kSegStages, buf);
+                if (nxt < nsegs) issue_stage(no, k + 2 - kSegStages, buf);
             }
         }
         if (nxt >= nsegs) break;
         cur = nxt;
+        co = no;
         pb ^= 1;
     }
 }
