@@ -410,9 +410,9 @@ def run_batch(args, ws, rank, local):
         "config": {"workload": "batch512: 512 fBm rasters, seeds 100-611, sides log-uniform [256, 4096], "
                                "Hurst U(0.6, 0.9), %d cells" % cells,
                    "l2": "inputs larger than L2 (%.1f GB per step)" % (cells * 9 / 1e9)},
-        "roofline": {"bound": "hbm", "kernel": "batch_tma_kernel", "achieved": round(achieved, 1), "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "batch_strip_kernel (+ batch_strip_fixup_kernel)", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind, "traffic": None},
-        "gpu_launches": args.steps, "plain_gpu_launches": args.steps * 512, "clocks": clk,
+        "gpu_launches": 2 * args.steps, "plain_gpu_launches": args.steps * 512, "clocks": clk,
     }
 
 

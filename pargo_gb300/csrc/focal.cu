@@ -893,6 +893,215 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
     }
 }
 
+// Batched strip walk: one persistent launch walks the segments of many
+// rasters.  Segments are numbered raster by raster (seg_start), claimed from
+// a device counter, and each carries its raster's tensor maps (maps[2k]: the
+// stage box, maps[2k+1]: the priming box) and parameters; the rows the fast
+// path leaves go to one list of 64-bit items (raster << 40 | row * lanes +
+// lane) for batch_strip_fixup_kernel.
+struct BatchStripTables {
+    const CUtensorMap* maps;
+    const FocalParams* params;
+    const InView* dems;
+    const int64_t* seg_start;  // count + 1
+    const int* nstrips;
+    int count;
+    int64_t nsegs;
+    unsigned long long* claim;
+    unsigned long long* slow_count;
+    uint64_t* slow_items;
+    int* error_flag;
+};
+
+__device__ __noinline__ void batch_strip_flush(uint32_t pend, int y_last, int64_t gx0, int item, int64_t cols,
+                                               const BatchStripTables t) {
+    const int64_t lanes = (cols + 3) / 4;
+    if ((gx0 >> 2) >= lanes) return;  // past the raster's last column
+    unsigned long long base = atomicAdd(t.slow_count, (unsigned long long)__popc(pend));
+    while (pend) {
+        const int b = __ffs(pend) - 1;
+        pend &= pend - 1;
+        t.slow_items[base++] = ((uint64_t)item << 40) | (uint64_t)((int64_t)(y_last - b) * lanes + (gx0 >> 2));
+    }
+}
+
+template <bool SLOPE, bool D8>
+__global__ void __launch_bounds__(kSWarps * 32, 5) batch_strip_kernel(const BatchStripTables t) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[kSWarps][4];  // stage 0, stage 1, prime 0, prime 1
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned char* wbase = smem + warp * kSWarpBytes;
+    auto stage = [&](int b) { return reinterpret_cast<float*>(wbase + b * kSStageStride); };
+    auto prime = [&](int b) { return reinterpret_cast<float*>(wbase + 2 * kSStageStride + b * kSPrimeStride); };
+    uint64_t* bar = bars[warp];
+    if (lane == 0) {
+        for (int i = 0; i < 4; i++) mbar_init(&bar[i], 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+    auto claim_seg = [&]() -> int64_t {
+        unsigned long long v = 0;
+        if (lane == 0) v = atomicAdd(t.claim, 1ULL);
+        return (int64_t)__shfl_sync(0xffffffffu, v, 0);
+    };
+    struct Origin {
+        int x0, y0, item, rows;
+    };
+    auto origin = [&](int64_t g) {
+        int lo = 0, hi = t.count - 1;  // the last raster whose first segment is <= g
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (t.seg_start[mid] <= g) lo = mid; else hi = mid - 1;
+        }
+        const uint32_t local = (uint32_t)(g - t.seg_start[lo]), ns = (uint32_t)t.nstrips[lo];
+        return Origin{(int)((local % ns) * kTW), (int)((local / ns) * kSegRows), lo, (int)t.params[lo].rows};
+    };
+    auto issue_prime = [&](const Origin& o, int buf) {
+        if (lane == 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[2 + buf], kSPrimeBytes);
+            tma_load_2d(prime(buf), &t.maps[2 * o.item + 1], o.x0 - 4, o.y0 - 1, &bar[2 + buf]);
+        }
+    };
+    auto issue_stage = [&](const Origin& o, int k, int buf) {
+        if (lane == 0) {
+            const int yb = min(o.y0 + 1 + k * kSR, o.rows - 1);  // rows past the raster: never stored
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bar[buf], kSStageBytes);
+            tma_load_2d(stage(buf), &t.maps[2 * o.item], o.x0 - 4, yb, &bar[buf]);
+        }
+    };
+
+    int64_t cur = claim_seg();
+    if (cur >= t.nsegs) return;
+    Origin co = origin(cur);
+    issue_prime(co, 0);
+    issue_stage(co, 0, 0);
+    issue_stage(co, 1, 1);
+    uint32_t sphase = 0, pphase = 0;
+    int pb = 0;
+    SRow A, B, C;
+    SPair PAB, PBC, PCA;
+    while (true) {
+        const FocalParams& p = t.params[co.item];
+        const int rows = co.rows;
+        const int64_t cols = p.cols;
+        const float k_fd = p.sk.k_fd;
+        const Band<float> nd6 = p.nd6f;
+        const bool plain = p.fd && p.fast_out && !p.sk.degrees && (!D8 || p.dir_type == 8);
+        const int64_t x0 = co.x0, y0 = co.y0;
+        const int64_t gx0 = x0 + 4 * lane;
+        const bool lane_int = plain && gx0 >= 1 && gx0 + 4 <= cols - 1;
+        const int64_t spp = SLOPE ? p.slope.pitch : 0, dpp = D8 ? p.d8.pitch : 0;
+        char* sp = SLOPE ? p.slope.base + y0 * spp + 4 * gx0 : nullptr;
+        char* dp = D8 ? p.d8.base + y0 * dpp + gx0 : nullptr;
+        int64_t nxt = t.nsegs;
+        Origin no = co;
+        if (!warp_wait(&bar[2 + pb], (pphase >> pb) & 1u)) {
+            if (lane == 0 && t.error_flag) atomicExch(t.error_flag, 1);
+            return;
+        }
+        pphase ^= 1u << pb;
+        s_load_row(prime(pb), lane, A, nd6);
+        s_load_row(prime(pb) + kBoxW, lane, B, nd6);
+        s_pair(A, B, PAB);
+#pragma unroll 1
+        for (int k = 0; k < kSegStages; k++) {
+            const int buf = k & 1;
+            if (!warp_wait(&bar[buf], (sphase >> buf) & 1u)) {
+                if (lane == 0 && t.error_flag) atomicExch(t.error_flag, 1);
+                return;
+            }
+            sphase ^= 1u << buf;
+            uint32_t pend = 0;
+            const int ys = (int)y0 + k * kSR;
+            const bool inside = (ys >= 1) & (ys + kSR - 1 <= rows - 2);
+            if (__any_sync(0xffffffffu, stage_lane_maybe_nodata(stage(buf), nd6) | A.nd | B.nd) | !inside) {
+#pragma unroll 1
+                for (int tt = 0; tt < kSR; tt += 3) {
+                    const float* st = stage(buf) + tt * kBoxW;
+                    const int y = ys + tt;
+                    strip_step<SLOPE, D8, false>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, nd6, sp, dp,
+                                                pend, cols);
+                    strip_step<SLOPE, D8, false>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd, nd6,
+                                                sp + spp, dp + dpp, pend, cols);
+                    strip_step<SLOPE, D8, false>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
+                                                nd6, sp + 2 * spp, dp + 2 * dpp, pend, cols);
+                    sp += 3 * spp;
+                    dp += 3 * dpp;
+                }
+            } else {
+#pragma unroll 1
+                for (int tt = 0; tt < kSR; tt += 3) {
+                    const float* st = stage(buf) + tt * kBoxW;
+                    const int y = ys + tt;
+                    strip_step<SLOPE, D8, true>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, nd6, sp, dp,
+                                                pend, cols);
+                    strip_step<SLOPE, D8, true>(st + kBoxW, B, C, A, PBC, PCA, y + 1, rows, gx0, lane_int, k_fd, nd6,
+                                                sp + spp, dp + dpp, pend, cols);
+                    strip_step<SLOPE, D8, true>(st + 2 * kBoxW, C, A, B, PCA, PAB, y + 2, rows, gx0, lane_int, k_fd,
+                                                nd6, sp + 2 * spp, dp + 2 * dpp, pend, cols);
+                    sp += 3 * spp;
+                    dp += 3 * dpp;
+                }
+            }
+            if (pend) batch_strip_flush(pend, ys + kSR - 1, gx0, co.item, cols, t);
+            __syncwarp();
+            if (k + 2 < kSegStages) {
+                issue_stage(co, k + 2, buf);
+            } else {
+                if (k + 2 == kSegStages) {
+                    nxt = claim_seg();
+                    if (nxt < t.nsegs) {
+                        no = origin(nxt);
+                        issue_prime(no, pb ^ 1);
+                    }
+                }
+                if (nxt < t.nsegs) issue_stage(no, k + 2 - kSegStages, buf);
+            }
+        }
+        if (nxt >= t.nsegs) break;
+        cur = nxt;
+        co = no;
+        pb ^= 1;
+    }
+}
+
+__global__ void __launch_bounds__(128) batch_strip_fixup_kernel(const BatchStripTables t,
+                                                                unsigned long long* fallbacks) {
+    const unsigned long long n = *((volatile unsigned long long*)t.slow_count) * 4;  // one thread per cell
+    int fell_back = 0;
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const uint64_t e = t.slow_items[i >> 2];
+        const int item = (int)(e >> 40);
+        const uint64_t local = e & ((1ULL << 40) - 1);
+        const FocalParams& p = t.params[item];
+        const InView& dem = t.dems[item];
+        const uint64_t lanes = (uint64_t)((p.cols + 3) / 4);
+        const int64_t y = (int64_t)(local / lanes), gx = (int64_t)(local % lanes) * 4 + (int64_t)(i & 3);
+        if (gx >= p.cols) continue;
+        const bool ring = y <= 0 || gx <= 0 || y >= p.rows - 1 || gx >= p.cols - 1;
+        float z[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (!ring) {
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+                z[q] = reinterpret_cast<const float*>(dem.base + (y + q / 3 - 1) * dem.pitch)[gx + q % 3 - 1];
+        }
+        const CellOut o = cell_general<float>(z[0], z[1], z[2], z[3], z[4], z[5], z[6], z[7], z[8], &p, ring);
+        fell_back += (o.flags >> 2) & 1;
+        if (p.do_slope) {
+            if (o.flags & 1) put_value(p.slope, y, gx, p.slope.nodata);
+            else put_float(p.slope, y, gx, o.slope);
+        }
+        if (p.do_d8) {
+            if (o.flags & 2) put_value(p.d8, y, gx, p.d8.nodata);
+            else put_int(p.d8, y, gx, o.code);
+        }
+    }
+    count_fallbacks(fell_back, fallbacks);
+}
+
 // The (row, lane) items the strip walk left: their cells, one thread each,
 // through cell_general on the window read from the DEM.
 __global__ void __launch_bounds__(128) strip_fixup_kernel(const InView dem, const __grid_constant__ FocalParams p,
@@ -1071,6 +1280,42 @@ cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params,
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)grid, kThreads, smem, s>>>(maps, params, tile_start, ntx_of, count, total_tiles, claim,
                                                 fallbacks, error_flag);
+    return cudaGetLastError();
+}
+
+// Batched strip walk over `count` rasters: maps[2k] / maps[2k+1] are raster
+// k's stage (kBoxW x focal_strip_stage_rows()) and priming (kBoxW x 2) tensor
+// maps; seg_start[k] its first segment (batch_strip_segments() per raster);
+// counters[0..1] the claim and slow-item counters; slow_items room for one
+// 64-bit item per (row, 4-cell lane) of every raster.
+int64_t batch_strip_segments(int64_t rows, int64_t cols, int* nstrips) {
+    *nstrips = (int)((cols + kTW - 1) / kTW);
+    return (int64_t)*nstrips * ((rows + kSegRows - 1) / kSegRows);
+}
+
+cudaError_t launch_batch_strip(const CUtensorMap* maps, const FocalParams* params, const InView* dems,
+                               const int64_t* seg_start, const int* nstrips, int count, int64_t nsegs, int do_slope,
+                               int do_d8, unsigned long long* counters, uint64_t* slow_items,
+                               unsigned long long* fallbacks, int* error_flag, int num_sms, cudaStream_t s) {
+    if (nsegs == 0) return cudaSuccess;
+    const BatchStripTables t{maps, params, dems, seg_start, nstrips, count, nsegs, counters, counters + 1, slow_items,
+                             error_flag};
+    const size_t smem = (size_t)kSWarps * kSWarpBytes;
+    auto kern = do_slope ? (do_d8 ? batch_strip_kernel<true, true> : batch_strip_kernel<true, false>)
+                         : batch_strip_kernel<false, true>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSWarps * 32, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    int64_t grid = (int64_t)num_sms * per_sm;
+    const int64_t need = (nsegs + kSWarps - 1) / kSWarps;
+    if (grid > need) grid = need;
+    if ((e = cudaMemsetAsync(counters, 0, 2 * sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    kern<<<(unsigned)grid, kSWarps * 32, smem, s>>>(t);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    batch_strip_fixup_kernel<<<(unsigned)num_sms * 8, 128, 0, s>>>(t, fallbacks);
     return cudaGetLastError();
 }
 

@@ -75,6 +75,11 @@ cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params,
                              const int64_t* ntx_of, int count, int64_t total_tiles, int do_slope, int do_d8,
                              unsigned long long* claim, unsigned long long* fallbacks, int* error_flag, int num_sms,
                              cudaStream_t s);
+int64_t batch_strip_segments(int64_t rows, int64_t cols, int* nstrips);
+cudaError_t launch_batch_strip(const CUtensorMap* maps, const FocalParams* params, const InView* dems,
+                               const int64_t* seg_start, const int* nstrips, int count, int64_t nsegs, int do_slope,
+                               int do_d8, unsigned long long* counters, uint64_t* slow_items,
+                               unsigned long long* fallbacks, int* error_flag, int num_sms, cudaStream_t s);
 cudaError_t launch_batch_generic(const FocalParams* params, const InView* dems, const int64_t* cell_start, int count,
                                  int64_t total_cells, unsigned long long* fallbacks, int num_sms, cudaStream_t s);
 

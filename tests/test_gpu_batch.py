@@ -46,3 +46,24 @@ def test_batch_mixed_outputs_and_cache(ctx, oracle_lib):
                            dir_type=256)
         for k, dem in enumerate(dems):
             assert bits_equal(host(outs[k]), oracle_lib.d8(dem, -9999.0, dir_type=256))
+
+
+@pytest.mark.parametrize("outputs", ["both", "slope", "d8"])
+def test_batch_strip_walk_with_nodata_and_edge_sizes(outputs, ctx, oracle_lib):
+    """The batched strip walk (aligned float32 / int8 outputs, Horn, dirType 8)
+    on DEMs with nodata blobs and shapes at the 48-row segment and 128-column
+    strip boundaries: identical to the per-raster launches and the oracle."""
+    shapes = [(3, 3), (47, 129), (48, 128), (49, 127), (97, 385), (200, 130), (143, 257), (1024, 700)]
+    dems = [synth.hydro_dem(r, c, seed=11 + k) for k, (r, c) in enumerate(shapes)]
+    dd = [dev(d, 16) for d in dems]
+    want_s, want_c = outputs in ("both", "slope"), outputs in ("both", "d8")
+    bs = [empty_dev(d.shape, np.float32, 16) for d in dems] if want_s else None
+    bc = [empty_dev(d.shape, np.int8, 16) for d in dems] if want_c else None
+    ctx.batch_slope_d8([abi.raster(d, -9999.0, 30.0) for d in dd], [abi.raster(s, -9999.0) for s in bs] if bs else None,
+                       [abi.raster(c, -128) for c in bc] if bc else None)
+    for k, dem in enumerate(dems):
+        if want_s:
+            ok, mx, _ = slope_close(host(bs[k]), oracle_lib.slope(dem, -9999.0, 30.0))
+            assert ok, (k, mx)
+        if want_c:
+            assert bits_equal(d8_as_f64(host(bc[k]), -128), oracle_lib.d8(dem, -9999.0)), k
