@@ -1162,13 +1162,33 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     p.cnt = (int32_t*)slot(ctx, kSlotMfdCnt, (size_t)n * 4, &e);
     p.flags = (uint8_t*)slot(ctx, kSlotMfdFlags, (size_t)n, &e);
     p.sca = (double*)slot(ctx, kSlotMfdSca, (size_t)n * 8, &e);
-    int32_t* lists = (int32_t*)slot(ctx, kSlotMfdLists, (size_t)(2 * n + 8) * 4 + 64, &e);
+    int32_t* lists = (int32_t*)slot(ctx, kSlotMfdLists, (size_t)(3 * n + 16) * 4 + 64, &e);
     if (!p.cnt || !p.flags || !p.sca || !lists) return cuda_fail(ctx, e, "sca_mfd scratch");
     p.list_a = lists;
     p.list_b = lists + n;
-    p.counts = lists + 2 * n;
-    p.totals = (unsigned long long*)(((uintptr_t)(lists + 2 * n + 8) + 7) & ~(uintptr_t)7);
+    p.list_c = lists + 2 * n;
+    p.counts = lists + 3 * n;
+    p.barrier = (unsigned int*)(lists + 3 * n + 4);
+    p.totals = (unsigned long long*)(((uintptr_t)(lists + 3 * n + 8) + 7) & ~(uintptr_t)7);
+    p.error_flag = ctx->d_error;
     CU(ctx, launch_sca_mfd_init(p, ctx->num_sms, s));
+    int32_t* hc = (int32_t*)pinned(ctx, 128, &e);
+    if (!hc) return cuda_fail(ctx, e, "pinned counters");
+    // Every round in one cooperative launch (a grid barrier between rounds);
+    // where a cooperative launch is not available, rounds as CUDA graphs.
+    if (launch_sca_mfd_persistent(p, ctx->num_sms, s) == cudaSuccess) {
+        CU(ctx, launch_sca_mfd_output(p, ctx->num_sms, s));
+        if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
+        unsigned long long* ht = (unsigned long long*)(hc + 8);
+        CU(ctx, cudaMemcpyAsync(ht, p.totals, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+        if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+        if (ht[2] != 0)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: %llu nodata cells carry positive weights", ht[2]);
+        if (ht[0] != ht[1])
+            return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: %llu of %llu valid cells processed (cycle)", ht[1], ht[0]);
+        return PARGO_OK;
+    }
+    cudaGetLastError();  // clear the refused cooperative launch
     // Frontier rounds, 32 per CUDA graph (an even number: list A is current
     // again after each graph), until both lists are empty.
     constexpr int kRounds = 32;
@@ -1185,11 +1205,6 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     ee = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     if (ee != cudaSuccess) return cuda_fail(ctx, ee, "sca_mfd graph instantiate");
-    int32_t* hc = (int32_t*)pinned(ctx, 128, &e);
-    if (!hc) {
-        cudaGraphExecDestroy(ge);
-        return cuda_fail(ctx, e, "pinned counters");
-    }
     pargo_status rs = PARGO_OK;
     for (int64_t launched = 0;; launched += kRounds) {
         if ((e = cudaGraphLaunch(ge, ctx->own)) != cudaSuccess ||

@@ -145,7 +145,6 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdPara
             if (valid) {
                 f = kValid | (indeg == 0 ? kSource : 0) | (indeg > cnt ? kNeverDone : 0);
                 nvalid++;
-                if (cnt == 0) p.list_a[atomicAdd(&p.counts[0], 1)] = (int32_t)i;
             } else {
                 bool out = false;
                 for (int q = 0; q < 8; q++) out = out || positive(p.w[q], r, c);
@@ -154,6 +153,18 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdPara
         }
         p.flags[i] = f;
         p.cnt[i] = cnt;
+        // the first frontier: valid cells with no inflow from a valid work cell,
+        // appended with one atomic per warp
+        const bool first = (f & kValid) && cnt == 0;
+        const unsigned act = __activemask();
+        const unsigned m = __ballot_sync(act, first);
+        if (m) {
+            const int lane = threadIdx.x & 31, leader = __ffs(act) - 1;
+            int32_t base = 0;
+            if (lane == leader) base = atomicAdd(&p.counts[0], __popc(m));
+            base = __shfl_sync(act, base, leader);
+            if (first) p.list_a[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+        }
     }
     if (nvalid) atomicAdd(&p.totals[0], nvalid);
     if (bad) atomicAdd(&p.totals[2], bad);
@@ -213,6 +224,95 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdPar
     }
 }
 
+// One cell of a frontier: its sum and done flag, then the counters of the
+// cells it flows into; a counter reaching zero queues that cell in `next`.
+__device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, int32_t* next, int32_t* next_count) {
+    const int64_t r = i / p.cols, c = i % p.cols;
+    double sum = 1.0;
+    bool done = !(p.flags[i] & kNeverDone);
+    for (int k = 0; k < 9; k++) {  // window order, as the reference sweeps it
+        if (k == 4) continue;
+        const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
+        const InView& wv = p.w[layer_towards_centre(k)];
+        if (!positive(wv, qr, qc)) continue;
+        const int64_t q = qr * p.cols + qc;
+        const uint8_t fq = p.flags[q];
+        const bool pulled = (fq & kValid) && ((fq & kSource) || (q < i && (fq & kDone)));
+        if (pulled) sum = __dadd_rn(sum, __dmul_rn(p.sca[q], load_d(wv, qr, qc)));
+        else done = false;
+    }
+    p.sca[i] = sum;
+    p.flags[i] = p.flags[i] | (done ? kDone : 0);
+    for (int q = 0; q < 8; q++) {
+        if (!positive(p.w[q], r, c)) continue;
+        const int pos = pos_of_layer(q);
+        const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
+        if (dr < 1 || dc < 1 || dr > p.rows - 2 || dc > p.cols - 2) continue;
+        const int64_t d = dr * p.cols + dc;
+        if (!(p.flags[d] & kValid)) continue;
+        if (atomicSub(&p.cnt[d], 1) == 1) next[atomicAdd(next_count, 1)] = (int32_t)d;
+    }
+}
+
+constexpr long long kBarrierBudget = 4000000000LL;  // ~2 s of SM clocks without the barrier opening
+
+// Grid-wide barrier of the cooperative launch: arrivals counted, the last
+// arriver opens the next generation.  Bounded: a block that waits longer than
+// the budget reports false (and sets the error flag) instead of spinning on.
+__device__ bool grid_barrier(const ScaMfdParams& p) {
+    __shared__ bool ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* gen = &p.barrier[1];
+        const unsigned int g = *gen;
+        __threadfence();
+        ok = true;
+        if (atomicAdd(&p.barrier[0], 1u) == gridDim.x - 1) {
+            p.barrier[0] = 0;
+            __threadfence();
+            atomicAdd(&p.barrier[1], 1u);
+        } else {
+            const long long t0 = clock64();
+            while (*gen == g) {
+                if (clock64() - t0 > kBarrierBudget || *((volatile int*)p.error_flag) != 0) {
+                    ok = false;
+                    atomicExch(p.error_flag, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok;
+}
+
+// Every round in one launch: round k processes list k mod 3, queues into
+// list k+1 mod 3 and empties list k+2 mod 3 (processed in round k-1, filled
+// again in round k+1), so one grid barrier separates rounds.
+__global__ void __launch_bounds__(512) sca_mfd_persistent_kernel(const ScaMfdParams p) {
+    auto list = [&](int i) { return i == 0 ? p.list_a : (i == 1 ? p.list_b : p.list_c); };
+    auto count = [&](int i) { return i == 0 ? &p.counts[0] : (i == 1 ? &p.counts[1] : &p.counts[3]); };
+    unsigned long long done_cells = 0;
+    for (int k = 0;; k++) {
+        const int cur = k % 3, nxt = (k + 1) % 3, old = (k + 2) % 3;
+        const int32_t ncur = *((volatile int32_t*)count(cur));
+        const int32_t* cl = list(cur);
+        int32_t* nl = list(nxt);
+        int32_t* nc = count(nxt);
+        for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < ncur;
+             idx += (int64_t)gridDim.x * blockDim.x) {
+            sca_mfd_cell(p, cl[idx], nl, nc);
+            done_cells++;
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) *count(old) = 0;
+        if (!grid_barrier(p)) break;
+        if (*((volatile int32_t*)nc) == 0) break;  // the same value in every block
+    }
+    if (done_cells) atomicAdd(&p.totals[1], done_cells);
+}
+
 __global__ void __launch_bounds__(kThreads) sca_mfd_output_kernel(const ScaMfdParams p) {
     const int64_t n = p.rows * p.cols;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -247,6 +347,19 @@ cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms,
     // a grid sized for the frontier the image can hold at once; the kernel strides
     sca_mfd_round_kernel<<<(unsigned)num_sms * 4, kThreads, 0, st>>>(p, parity);
     return cudaGetLastError();
+}
+
+cudaError_t launch_sca_mfd_persistent(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sca_mfd_persistent_kernel, 512, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
+    if (per_sm > 2) per_sm = 2;  // fewer arrivals per barrier
+    if ((e = cudaMemsetAsync(p.barrier, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(&p.counts[3], 0, sizeof(int32_t), st)) != cudaSuccess) return e;
+    void* args[] = {(void*)&p};
+    return cudaLaunchCooperativeKernel((const void*)sca_mfd_persistent_kernel, dim3((unsigned)(num_sms * per_sm)),
+                                       dim3(512), args, 0, st);
 }
 
 cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
