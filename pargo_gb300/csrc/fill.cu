@@ -193,7 +193,9 @@ __device__ void ring_push(const FillScratch& s, int32_t t, long long patience) {
     }
 }
 
-// Next tile to visit, or -1 once the work is done (or a wait gave up).
+// Next tile to visit, or -1 once the work is done (or a wait gave up).  The
+// slot is taken by exchanging it with -1: an empty slot stays empty, a full
+// one is taken by exactly one of the visitors that share it.
 __device__ int32_t ring_pop(const FillScratch& s, long long patience) {
     const unsigned long long pos = atomicAdd(&s.q[kQHead], 1ULL);
     int32_t* slot = &s.ring[pos % (unsigned long long)s.ring_cap];
@@ -201,11 +203,8 @@ __device__ int32_t ring_pop(const FillScratch& s, long long patience) {
     long long t0 = clock64();
     unsigned ns = 32;
     for (;;) {
-        const int32_t v = *((volatile int32_t*)slot);
-        if (v >= 0) {
-            if (atomicCAS(slot, v, -1) == v) return v;
-            continue;  // another visitor that shares this slot took it
-        }
+        const int32_t v = atomicExch(slot, -1);
+        if (v >= 0) return v;
         if (vload64(&s.q[kQPending]) == 0 || vload64(&s.q[kQError]) != 0) return -1;
         const unsigned long long pr = vload64(&s.q[kQProgress]);
         if (pr != seen) {
@@ -227,7 +226,7 @@ __device__ int32_t ring_pop(const FillScratch& s, long long patience) {
 constexpr int32_t kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3;
 
 __device__ void request_tile(const FillScratch& s, int32_t t, long long patience) {
-    int32_t st = *((volatile int32_t*)&s.queued[t]);
+    int32_t st = kIdle;  // the common state: the first CAS either queues the tile or returns its state
     for (int guard = 0; guard < 64; guard++) {  // each failed CAS means another thread moved the state
         int32_t want;
         if (st == kIdle) want = kQueued;
