@@ -326,20 +326,37 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
         const int64_t ty = t / p.tiles_x, tx = t % p.tiles_x;
         const int64_t y0 = ty * kT - 1, x0 = tx * kT - 1;  // global coords of lv[0][0]
         if (!held) {
-            for (int i = tid; i < kH * kH; i += kThreads) {
-                const int a = i / kH, b = i % kH;
-                const int64_t r = y0 + a, c = x0 + b;
-                int64_t k = kKeyInf;
-                if (r >= 0 && c >= 0 && r < p.rows && c < p.cols) k = dkey(((volatile double*)p.w)[r * p.w_stride + c]);
-                lv[a * kLS + b] = k;
+            // Every load of a thread is issued before the first is used (one
+            // memory round trip per visit instead of one per loop trip).
+            constexpr int kLvPer = (kH * kH + kThreads - 1) / kThreads;  // 5
+            constexpr int kZPer = kT * kT / kThreads;                    // 4
+            double wv[kLvPer];
+#pragma unroll
+            for (int q = 0; q < kLvPer; q++) {
+                const int i = tid + q * kThreads;
+                const int64_t r = y0 + i / kH, c = x0 + i % kH;
+                wv[q] = INFINITY;  // key kKeyInf: beyond the raster
+                if (i < kH * kH && r >= 0 && c >= 0 && r < p.rows && c < p.cols)
+                    wv[q] = ((volatile double*)p.w)[r * p.w_stride + c];
+            }
+#pragma unroll
+            for (int q = 0; q < kLvPer; q++) {
+                const int i = tid + q * kThreads;
+                if (i < kH * kH) lv[(i / kH) * kLS + i % kH] = dkey(wv[q]);
             }
             // DEM keys; kKeyInf where a level never moves (the raster's ring, beyond the raster)
-            for (int i = tid; i < kT * kT; i += kThreads) {
-                const int r = i / kT, c = i % kT;
-                const int64_t gr = y0 + 1 + r, gc = x0 + 1 + c;
-                int64_t z = kKeyInf;
-                if (gr > 0 && gc > 0 && gr < p.rows - 1 && gc < p.cols - 1) z = dkey(dem_at(p, gr, gc));
-                zs[r * kZS + c] = z;
+            double zv[kZPer];
+#pragma unroll
+            for (int q = 0; q < kZPer; q++) {
+                const int i = tid + q * kThreads;
+                const int64_t gr = y0 + 1 + i / kT, gc = x0 + 1 + i % kT;
+                zv[q] = INFINITY;
+                if (gr > 0 && gc > 0 && gr < p.rows - 1 && gc < p.cols - 1) zv[q] = dem_at(p, gr, gc);
+            }
+#pragma unroll
+            for (int q = 0; q < kZPer; q++) {
+                const int i = tid + q * kThreads;
+                zs[(i / kT) * kZS + i % kT] = dkey(zv[q]);
             }
         } else if (tid < 4 * kH - 4) {
             // The same tile again: only its halo can have moved (this CTA

@@ -260,31 +260,46 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
         ia = ib;
         ib = ic;
     }
-    // Rows the integer path did not finish: the general FP64 path on the staged window.
-    while (redo) {
-        const int i = __ffs(redo) - 1;
-        redo &= redo - 1;
-        const int64_t gy = gy0 + i;
-        if (gy >= p.rows) break;
+    // Rows the integer path did not finish: the general FP64 path on the
+    // staged window.  Their cells are first gathered across the warp, so the
+    // FP64 work (a slow pipe on this part) runs on full warps rather than on
+    // the few lanes of each row that need it.
+    __shared__ uint16_t redo_items[kWarps][kRows * 64];  // (row << 6) | tile column
+    uint16_t* items = redo_items[warp];
+    const unsigned lt = (1u << lane) - 1u;
+    int n = 0;
 #pragma unroll 1
-        for (int j = 0; j < 2; j++) {
-            const int64_t gx = gx0 + j;
-            if (gx >= p.cols) break;
-            const bool ring = gy <= 0 || gx <= 0 || gy >= p.rows - 1 || gx >= p.cols - 1;
-            const double* w = s + (r0 + i) * kBoxW + 2 * lane + j + 1;  // window's top-left
-            const CellOut o = cell_general64(w[0], w[1], w[2], w[kBoxW], w[kBoxW + 1], w[kBoxW + 2], w[2 * kBoxW],
-                                             w[2 * kBoxW + 1], w[2 * kBoxW + 2], &p, ring);
-            fell_back += (o.flags >> 2) & 1;
-            if (p.do_slope) {
-                if (o.flags & 1) put_value(p.slope, gy, gx, p.slope.nodata);
-                else put_float(p.slope, gy, gx, o.slope);
-            }
-            if (p.do_d8) {
-                if (o.flags & 2) put_value(p.d8, gy, gx, p.d8.nodata);
-                else put_int(p.d8, gy, gx, o.code);
-            }
+    for (int i = 0; i < kRows; i++) {
+        const bool rb = (redo >> i) & 1u;
+        const unsigned b = __ballot_sync(0xFFFFFFFFu, rb);
+        if (rb) {
+            const int pos = n + 2 * __popc(b & lt);
+            items[pos] = (uint16_t)((i << 6) | (2 * lane));
+            items[pos + 1] = (uint16_t)((i << 6) | (2 * lane + 1));
+        }
+        n += 2 * __popc(b);
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int q = lane; q < n; q += 32) {
+        const int i = items[q] >> 6, cc = items[q] & 63;
+        const int64_t gy = gy0 + i, gx = x0 + cc;
+        if (gy >= p.rows || gx >= p.cols) continue;
+        const bool ring = gy <= 0 || gx <= 0 || gy >= p.rows - 1 || gx >= p.cols - 1;
+        const double* w = s + (r0 + i) * kBoxW + cc + 1;  // window's top-left
+        const CellOut o = cell_general64(w[0], w[1], w[2], w[kBoxW], w[kBoxW + 1], w[kBoxW + 2], w[2 * kBoxW],
+                                         w[2 * kBoxW + 1], w[2 * kBoxW + 2], &p, ring);
+        fell_back += (o.flags >> 2) & 1;
+        if (p.do_slope) {
+            if (o.flags & 1) put_value(p.slope, gy, gx, p.slope.nodata);
+            else put_float(p.slope, gy, gx, o.slope);
+        }
+        if (p.do_d8) {
+            if (o.flags & 2) put_value(p.d8, gy, gx, p.d8.nodata);
+            else put_int(p.d8, gy, gx, o.code);
         }
     }
+    __syncwarp();  // the list is rewritten by the next tile
 }
 
 __global__ void __launch_bounds__(kThreads, 4) focal64_tma_kernel(const __grid_constant__ CUtensorMap map,
