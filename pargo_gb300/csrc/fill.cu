@@ -113,31 +113,31 @@ __global__ void fill_init_tiles_kernel(const FillParams p, FillScratch s) {
 // (its cells see init_level or +inf around them, and init_level + gap is
 // above init_level) until a neighbour's border moves and requests it.
 __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
-    const int64_t n = p.rows * p.cols;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / p.cols, c = i % p.cols;
-        double w = INFINITY;
-        const bool inner = r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
-        if (inner) {
-            const double z = dem_at(p, r, c);
-            if (!dem_nodata(p, z)) {
-                w = p.init_level;
-                if (p.init_level > z) {
-                    bool outlet = false;
-                    for (int a = -1; a <= 1; a++)
-                        for (int b = -1; b <= 1; b++) {
-                            const int64_t rr = r + a, cc = c + b;
-                            const bool ring = rr <= 0 || cc <= 0 || rr >= p.rows - 1 || cc >= p.cols - 1;
-                            if (ring || dem_nodata(p, dem_at(p, rr, cc))) outlet = true;
+    for (int64_t r = blockIdx.y; r < p.rows; r += gridDim.y) {
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < p.cols; c += (int64_t)gridDim.x * blockDim.x) {
+            double w = INFINITY;
+            const bool inner = r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
+            if (inner) {
+                const double z = dem_at(p, r, c);
+                if (!dem_nodata(p, z)) {
+                    w = p.init_level;
+                    if (p.init_level > z) {
+                        bool outlet = false;
+                        for (int a = -1; a <= 1; a++)
+                            for (int b = -1; b <= 1; b++) {
+                                const int64_t rr = r + a, cc = c + b;
+                                const bool ring = rr <= 0 || cc <= 0 || rr >= p.rows - 1 || cc >= p.cols - 1;
+                                if (ring || dem_nodata(p, dem_at(p, rr, cc))) outlet = true;
+                            }
+                        if (outlet) {
+                            w = z;
+                            s.halo_chg[((r / kT) * p.tiles_x + c / kT) * 5 + 4] = kHaloAll;
                         }
-                    if (outlet) {
-                        w = z;
-                        s.halo_chg[((r / kT) * p.tiles_x + c / kT) * 5 + 4] = kHaloAll;
                     }
                 }
             }
+            p.w[r * p.w_stride + c] = w;
         }
-        p.w[r * p.w_stride + c] = w;
     }
 }
 
@@ -535,14 +535,14 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
 }
 
 __global__ void fill_finish_kernel(const FillParams p, const OutView out, unsigned long long* raised) {
-    const int64_t n = p.rows * p.cols;
     unsigned long long cnt = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / p.cols, c = i % p.cols;
-        const double w = p.w[r * p.w_stride + c];
-        const bool nd = isinf(w);
-        if (!nd && w > dem_at(p, r, c)) cnt++;
-        put_value(out, r, c, nd ? out.nodata : w);
+    for (int64_t r = blockIdx.y; r < p.rows; r += gridDim.y) {
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < p.cols; c += (int64_t)gridDim.x * blockDim.x) {
+            const double w = p.w[r * p.w_stride + c];
+            const bool nd = isinf(w);
+            if (!nd && w > dem_at(p, r, c)) cnt++;
+            put_value(out, r, c, nd ? out.nodata : w);
+        }
     }
     cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
     if (raised && (threadIdx.x & 31) == 0 && cnt) atomicAdd(raised, cnt);
@@ -592,14 +592,15 @@ static cudaError_t upload_steps(double gap, cudaStream_t st) {
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st) {
     cudaError_t e = upload_steps(p.gap, st);
     if (e != cudaSuccess) return e;
-    const int64_t n = p.rows * p.cols;
-    int64_t blocks = (n + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
+    // levels: a block per row (up to 4096 rows in flight), threads along it
+    int64_t bx = (p.cols + 255) / 256;
+    if (bx > 64) bx = 64;
+    const dim3 lgrid((unsigned)bx, (unsigned)(p.rows < 4096 ? p.rows : 4096));
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     int64_t tblocks = (ntiles + 255) / 256;
     if (tblocks > 4096) tblocks = 4096;
     fill_init_tiles_kernel<<<(unsigned)tblocks, 256, 0, st>>>(p, s);
-    fill_init_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, s);
+    fill_init_kernel<<<lgrid, 256, 0, st>>>(p, s);
     fill_seed_kernel<<<(unsigned)tblocks, 256, 0, st>>>(p, s);
     return cudaGetLastError();
 }
@@ -629,10 +630,10 @@ cudaError_t fill_persistent(const FillParams& p, const FillScratch& s, long long
 }
 
 cudaError_t fill_finish(const FillParams& p, const OutView& out, unsigned long long* raised, cudaStream_t st) {
-    const int64_t n = p.rows * p.cols;
-    int64_t blocks = (n + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
-    fill_finish_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, out, raised);
+    int64_t bx = (p.cols + 255) / 256;
+    if (bx > 64) bx = 64;
+    const dim3 grid((unsigned)bx, (unsigned)(p.rows < 4096 ? p.rows : 4096));
+    fill_finish_kernel<<<grid, 256, 0, st>>>(p, out, raised);
     return cudaGetLastError();
 }
 
