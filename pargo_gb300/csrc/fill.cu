@@ -113,7 +113,11 @@ __global__ void fill_init_tiles_kernel(const FillParams p, FillScratch s) {
 // (its cells see init_level or +inf around them, and init_level + gap is
 // above init_level) until a neighbour's border moves and requests it.
 __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
-    for (int64_t r = blockIdx.y; r < p.rows; r += gridDim.y) {
+    // a band of consecutive rows per block row: a row's neighbour rows were
+    // just read by the same blocks
+    const int64_t per = (p.rows + gridDim.y - 1) / gridDim.y;
+    const int64_t r_end = min(p.rows, ((int64_t)blockIdx.y + 1) * per);
+    for (int64_t r = (int64_t)blockIdx.y * per; r < r_end; r++) {
         for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < p.cols; c += (int64_t)gridDim.x * blockDim.x) {
             double w = INFINITY;
             const bool inner = r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
@@ -592,10 +596,12 @@ static cudaError_t upload_steps(double gap, cudaStream_t st) {
 cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st) {
     cudaError_t e = upload_steps(p.gap, st);
     if (e != cudaSuccess) return e;
-    // levels: a block per row (up to 4096 rows in flight), threads along it
+    // levels: ~4096 blocks of 256 threads, each block row a band of rows
+    // (tens of cells per thread)
     int64_t bx = (p.cols + 255) / 256;
     if (bx > 64) bx = 64;
-    const dim3 lgrid((unsigned)bx, (unsigned)(p.rows < 4096 ? p.rows : 4096));
+    const int64_t by = p.rows < 4096 / bx ? p.rows : 4096 / bx;
+    const dim3 lgrid((unsigned)bx, (unsigned)by);
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     int64_t tblocks = (ntiles + 255) / 256;
     if (tblocks > 4096) tblocks = 4096;
@@ -632,7 +638,8 @@ cudaError_t fill_persistent(const FillParams& p, const FillScratch& s, long long
 cudaError_t fill_finish(const FillParams& p, const OutView& out, unsigned long long* raised, cudaStream_t st) {
     int64_t bx = (p.cols + 255) / 256;
     if (bx > 64) bx = 64;
-    const dim3 grid((unsigned)bx, (unsigned)(p.rows < 4096 ? p.rows : 4096));
+    const int64_t by = p.rows < 4096 / bx ? p.rows : 4096 / bx;
+    const dim3 grid((unsigned)bx, (unsigned)by);
     fill_finish_kernel<<<grid, 256, 0, st>>>(p, out, raised);
     return cudaGetLastError();
 }
