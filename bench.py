@@ -41,6 +41,9 @@ FALLBACK_HBM_GBS = 6800.0
 # from its ncu capture on 8192^2 (301.3 MB + 289.3 MB over 67108864 cells)
 FOCAL_DRAM_BYTES_PER_CELL = (301.330688e6 + 289.264128e6) / 67108864   # tiled kernel, 8192^2 ncu capture
 STRIP_DRAM_BYTES_PER_CELL = (289.425152e6 + 284.340224e6) / 67108864   # strip walk, 8192^2 ncu capture
+# dram__bytes_read.sum + dram__bytes_write.sum of one fill_tiles_kernel<true>
+# launch on the default 8192^2 workload (one-pass ncu capture of that launch)
+FILL_DRAM_BYTES_8192 = 2444316416 + 757925632
 
 
 def hbm_peak():
@@ -244,11 +247,15 @@ def run_hydro(args, ws, rank, local, side=8192):
     roofline = {"bound": "hbm", "kernel": "fill_tiles_kernel<true> (persistent)" if rounds == args.steps
                 else "fill_tiles_kernel<false> (rounds)", "achieved": round(achieved, 2), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": peak_kind,
-                "traffic": None, "rounds_per_step": rounds // args.steps,
+                "traffic": FILL_DRAM_BYTES_8192 if (side == 8192 and rounds == args.steps) else None,
+                "traffic_source": "ncu capture of one launch of this workload" if side == 8192 else None,
+                "rounds_per_step": rounds // args.steps,
                 "tile_visits_per_step": visits // args.steps,
                 "local_iterations_per_visit": round(iters / max(visits, 1), 2), "fill_share_of_step": round(fill_share, 4)
                 if fill_share else None}
-    launches = args.steps * 2 + rounds  # fill init + relaxation launches + float64 slope/D8, per step
+    # per step: tile bookkeeping, level init, outlet-tile seeding, the
+    # relaxation launch(es) and the float64 slope/D8
+    launches = args.steps * 4 + rounds
 
     cpu = None
     if rank == 0 and ws == 1:
@@ -331,7 +338,8 @@ def run_slope(args, ws, rank, local, side):
                      # same kernel (the traffic grows with the cell count)
                      "traffic": round((STRIP_DRAM_BYTES_PER_CELL if strip else FOCAL_DRAM_BYTES_PER_CELL) * cells),
                      "traffic_source": "ncu 8192^2 capture scaled per cell", "variant": best, "variant_ms": tune_ms},
-        "gpu_launches": args.steps, "clocks": clk,
+        # the strip walk is a walk launch and a fix-up launch per step; the tiled kernel one
+        "gpu_launches": args.steps * (2 if strip else 1), "clocks": clk,
     }
 
 
@@ -494,13 +502,14 @@ def run_sca(args, ws, rank, local, side=16384):
         "data": "synthetic",
         "config": {"workload": "sca%d: D8 SCA on the filled %dx%d hydro DEM (seed 2, 10 m cells), int8 codes in, "
                                "float64 out" % (side, side, side), "l2": "inputs larger than L2"},
-        "roofline": {"bound": "hbm", "kernel": "sca init + walk + finish (one call)", "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": "sca_tile_kernel x2 + exit forest (3 kernels) + sca_output_kernel "
+                               "(one call)", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
                      "traffic": None, "algorithmic_bytes_per_cell": 9},
         "cpu_baseline": cpu,
         "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells,
                 "d2h_bytes_per_step": cells * 8},
-        "gpu_launches": args.steps * 3, "clocks": clk,
+        "gpu_launches": args.steps * 6, "clocks": clk,  # the six kernels of one tiled SCA call
     }
 
 

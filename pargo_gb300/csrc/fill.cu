@@ -61,7 +61,10 @@ constexpr uint32_t kHaloAll = 0x80000000u;  // halo_chg corner-word flag: relax 
 // is the same for every x of the binade, else -1 (subnormals, inf/nan, a sum
 // that can leave the binade, and the binade in which gap is an odd number of
 // half-ulps, where the tie rounds by the parity of x): those use the double add.
-__device__ int64_t g_step[2048];
+// In constant memory: the cells a warp relaxes together mostly share a
+// binade, so the lookup is a broadcast (8192^2 fill 12.7 -> 12.3 ms against
+// a global-memory table).
+__constant__ int64_t g_step[2048];
 
 __device__ __forceinline__ int64_t dkey(double x) {
     int64_t b = __double_as_longlong(x);
