@@ -41,11 +41,6 @@ __device__ __forceinline__ int layer_towards_centre(int k) {
 }
 __device__ __forceinline__ int pos_of_layer(int i) { return i < 4 ? i : i + 1; }
 
-__device__ __forceinline__ double load_d(const InView& v, int64_t r, int64_t c) {
-    const char* row = v.base + r * v.pitch;
-    return v.dtype == PARGO_F64 ? reinterpret_cast<const double*>(row)[c]
-                                : (double)reinterpret_cast<const float*>(row)[c];
-}
 // weight > 0 without an FP64 compare
 __device__ __forceinline__ bool positive(const InView& v, int64_t r, int64_t c) {
     const char* row = v.base + r * v.pitch;
@@ -170,6 +165,79 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdPara
     if (bad) atomicAdd(&p.totals[2], bad);
 }
 
+// A weight: whether it is > 0 (positive() above) and its value, from one load.
+__device__ __forceinline__ double weight_at(const InView& v, int64_t r, int64_t c, bool& pos) {
+    const char* row = v.base + r * v.pitch;
+    if (v.dtype == PARGO_F64) {
+        const long long b = reinterpret_cast<const long long*>(row)[c];
+        pos = b > 0 && b <= 0x7FF0000000000000LL;
+        return __longlong_as_double(b);
+    }
+    const float f = reinterpret_cast<const float*>(row)[c];
+    pos = f > 0.0f;
+    return (double)f;
+}
+
+// One cell of a frontier: its sum and done flag, then the counters of the
+// cells it flows into; a counter reaching zero queues that cell in `next`.
+// A frontier cell is a work cell, so its 8 neighbours are in the raster, and
+// every cell it may pull from was finished in an earlier round: all its loads
+// (the 8 inflow weights, flags and sums, then the 8 outflow weights and
+// flags) are issued before the first is used, and the counter decrements go
+// out together -- a level costs a few memory round trips, not one per
+// neighbour.  The sum is still taken in the reference's window order.
+__device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, int32_t* next, int32_t* next_count) {
+    const int64_t r = i / p.cols, c = i % p.cols;
+    double wq[8], sq[8];
+    bool pq[8];
+    uint8_t fq[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        const int k = t < 4 ? t : t + 1;  // window position
+        const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
+        wq[t] = weight_at(p.w[layer_towards_centre(k)], qr, qc, pq[t]);
+        const int64_t q = qr * p.cols + qc;
+        fq[t] = p.flags[q];
+        sq[t] = p.sca[q];
+    }
+    const uint8_t fi = p.flags[i];
+    double sum = 1.0;
+    bool done = !(fi & kNeverDone);
+#pragma unroll
+    for (int t = 0; t < 8; t++) {  // window order, as the reference sweeps it
+        if (!pq[t]) continue;
+        const int k = t < 4 ? t : t + 1;
+        const int64_t q = i + (int64_t)(k / 3 - 1) * p.cols + (k % 3 - 1);
+        const bool pulled = (fq[t] & kValid) && ((fq[t] & kSource) || (q < i && (fq[t] & kDone)));
+        if (pulled) sum = __dadd_rn(sum, __dmul_rn(sq[t], wq[t]));
+        else done = false;
+    }
+    p.sca[i] = sum;
+    p.flags[i] = fi | (done ? kDone : 0);
+    bool po[8];
+    uint8_t fd[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        (void)weight_at(p.w[q], r, c, po[q]);
+        const int pos = pos_of_layer(q);
+        fd[q] = p.flags[i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1)];
+    }
+    int left[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int pos = pos_of_layer(q);
+        const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
+        const bool go = po[q] && dr >= 1 && dc >= 1 && dr <= p.rows - 2 && dc <= p.cols - 2 && (fd[q] & kValid);
+        left[q] = go ? atomicSub(&p.cnt[dr * p.cols + dc], 1) : 0;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        if (left[q] != 1) continue;
+        const int pos = pos_of_layer(q);
+        next[atomicAdd(next_count, 1)] = (int32_t)(i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1));
+    }
+}
+
 // One round: process the current frontier, queue the cells whose last inflow it was.
 __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdParams p, int parity) {
     int32_t* cur = parity ? p.list_b : p.list_a;
@@ -180,33 +248,8 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdPar
     unsigned long long done_cells = 0;
     for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < ncur;
          idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = cur[idx];
-        const int64_t r = i / p.cols, c = i % p.cols;
-        double sum = 1.0;
-        bool done = !(p.flags[i] & kNeverDone);
-        for (int k = 0; k < 9; k++) {  // window order, as the reference sweeps it
-            if (k == 4) continue;
-            const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
-            const InView& wv = p.w[layer_towards_centre(k)];
-            if (!positive(wv, qr, qc)) continue;
-            const int64_t q = qr * p.cols + qc;
-            const uint8_t fq = p.flags[q];
-            const bool pulled = (fq & kValid) && ((fq & kSource) || (q < i && (fq & kDone)));
-            if (pulled) sum = __dadd_rn(sum, __dmul_rn(p.sca[q], load_d(wv, qr, qc)));
-            else done = false;
-        }
-        p.sca[i] = sum;
-        p.flags[i] = p.flags[i] | (done ? kDone : 0);
+        sca_mfd_cell(p, cur[idx], next, next_count);
         done_cells++;
-        for (int q = 0; q < 8; q++) {
-            if (!positive(p.w[q], r, c)) continue;
-            const int pos = pos_of_layer(q);
-            const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
-            if (dr < 1 || dc < 1 || dr > p.rows - 2 || dc > p.cols - 2) continue;
-            const int64_t d = dr * p.cols + dc;
-            if (!(p.flags[d] & kValid)) continue;
-            if (atomicSub(&p.cnt[d], 1) == 1) next[atomicAdd(next_count, 1)] = (int32_t)d;
-        }
     }
     if (done_cells) atomicAdd(&p.totals[1], done_cells);
     // the last block to finish empties the consumed list
@@ -221,36 +264,6 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdPar
         *cur_count = 0;
         p.counts[2] = 0;
         __threadfence();
-    }
-}
-
-// One cell of a frontier: its sum and done flag, then the counters of the
-// cells it flows into; a counter reaching zero queues that cell in `next`.
-__device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, int32_t* next, int32_t* next_count) {
-    const int64_t r = i / p.cols, c = i % p.cols;
-    double sum = 1.0;
-    bool done = !(p.flags[i] & kNeverDone);
-    for (int k = 0; k < 9; k++) {  // window order, as the reference sweeps it
-        if (k == 4) continue;
-        const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
-        const InView& wv = p.w[layer_towards_centre(k)];
-        if (!positive(wv, qr, qc)) continue;
-        const int64_t q = qr * p.cols + qc;
-        const uint8_t fq = p.flags[q];
-        const bool pulled = (fq & kValid) && ((fq & kSource) || (q < i && (fq & kDone)));
-        if (pulled) sum = __dadd_rn(sum, __dmul_rn(p.sca[q], load_d(wv, qr, qc)));
-        else done = false;
-    }
-    p.sca[i] = sum;
-    p.flags[i] = p.flags[i] | (done ? kDone : 0);
-    for (int q = 0; q < 8; q++) {
-        if (!positive(p.w[q], r, c)) continue;
-        const int pos = pos_of_layer(q);
-        const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
-        if (dr < 1 || dc < 1 || dr > p.rows - 2 || dc > p.cols - 2) continue;
-        const int64_t d = dr * p.cols + dc;
-        if (!(p.flags[d] & kValid)) continue;
-        if (atomicSub(&p.cnt[d], 1) == 1) next[atomicAdd(next_count, 1)] = (int32_t)d;
     }
 }
 
