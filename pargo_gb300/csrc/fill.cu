@@ -279,8 +279,8 @@ __device__ __forceinline__ void put_tile(const FillScratch& s, int32_t* next, in
 // visits are latency bound, and occupancy measured worth more than the few
 // registers spilled at this bound (8192^2: 25.0 -> 22.8 ms).  Runs of 8 cells
 // (128 threads, 12 CTAs per SM) took fewer passes but more visits and more
-// time (19.9 ms against 12.8), and so did fewer resident CTAs (6 per SM:
-// 13.4 ms).
+// time (19.9 ms against 12.8); fewer resident CTAs took fewer visits but
+// more time (6 per SM: 13.4 ms).
 template <bool PERSIST>
 __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParams p, FillScratch s, int parity,
                                                               long long patience) {
