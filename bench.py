@@ -671,7 +671,9 @@ def run_mfd(args, ws, rank, local, side=8192):
         "cpu_baseline": cpu,
         "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells * 8,
                 "d2h_bytes_per_step": cells * (32 + 8)},
-        "gpu_launches": None, "clocks": clk,
+        # per step: weights, SCA in-degrees, the cooperative launch of every
+        # frontier round, output (the launch list of this workload shows it)
+        "gpu_launches": args.steps * 4, "clocks": clk,
     }
 
 
