@@ -236,17 +236,20 @@ def run_hydro(args, ws, rank, local, side=8192):
 
     # roofline of the dominant kernel: the fill relaxation (one persistent
     # launch per step; PARGO_FILL_ROUNDS=1 selects the round launches).
-    # Algorithmic bytes: 8 B per cell a visit covers (4 B DEM read + 4 B level
-    # written, the minimum of any pass), 1024 cells per tile visit; duration:
-    # the relaxation's device time (CUDA events on its stream) / launches.
+    # Algorithmic bytes: 8 B per cell of the raster per step (4 B DEM read +
+    # 4 B level written, the minimum any fill must move), the number of tile
+    # visits reported beside it; duration: the relaxation's device time (CUDA
+    # events on its stream).  The same 8 B counted once per cell of every tile
+    # visit is reported as achieved_per_cell_visit.
     peak, peak_kind = hbm_peak()
-    avg_round_ms = rounds_ms / max(rounds, 1)
-    bytes_per_round = 8.0 * 1024 * visits / max(rounds, 1)
-    achieved = bytes_per_round / (avg_round_ms * 1e-3) / 1e9 if avg_round_ms > 0 else 0.0
+    fill_s = rounds_ms * 1e-3 / max(args.steps, 1)  # per step
+    achieved = 8.0 * cells / fill_s / 1e9 if fill_s > 0 else 0.0
+    achieved_visit = 8.0 * 1024 * visits / max(args.steps, 1) / fill_s / 1e9 if fill_s > 0 else 0.0
     fill_share = rounds_ms / (ms * args.steps) if ms > 0 else None
     roofline = {"bound": "hbm", "kernel": "fill_tiles_kernel<true> (persistent)" if rounds == args.steps
                 else "fill_tiles_kernel<false> (rounds)", "achieved": round(achieved, 2), "peak": peak,
                 "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": peak_kind,
+                "algorithmic_bytes_per_cell": 8, "achieved_per_cell_visit": round(achieved_visit, 2),
                 "traffic": FILL_DRAM_BYTES_8192 if (side == 8192 and rounds == args.steps) else None,
                 "traffic_source": "ncu capture of one launch of this workload" if side == 8192 else None,
                 "rounds_per_step": rounds // args.steps,
