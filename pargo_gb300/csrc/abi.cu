@@ -702,7 +702,7 @@ namespace {
 // (dense rows x cols doubles, +inf on nodata levels) and returns its params.
 pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* dem, const pargo_fill_opts& o,
                        FillParams* out_p, pargo_fill_stats* stats, bool* converged, cudaStream_t s) {
-    const int64_t rows = dem->rows, cols = dem->cols, n = rows * cols;
+    const int64_t rows = dem->rows, cols = dem->cols;
     const int T = fill_tile_rows();
     FillParams p{};
     p.rows = rows;
@@ -999,7 +999,6 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
     // slope + D8 on the float64 levels (+inf marks their nodata cells); the
     // same pass copies the levels out as the filled DEM
     OutView codes{};
-    bool codes_internal = false;
     if (d8) {
         codes = sd.out;
     } else if (sca) {
@@ -1007,7 +1006,6 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
         char* buf = (char*)slot(ctx, kSlotPipeCodes, (size_t)(p.rows * p.cols), &e);
         if (!buf) return cuda_fail(ctx, e, "pipeline codes");
         codes = OutView{buf, p.cols, PARGO_I8, -128.0};
-        codes_internal = true;
     }
     if (slope || d8 || sca) {
         FocalParams f{};
@@ -1051,7 +1049,6 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
         q.shipped = sca_contract == PARGO_SCA_SHIPPED;
         if ((st = sca_launch(ctx, q, s, "pipeline sca")) != PARGO_OK) return st;
     }
-    (void)codes_internal;
     if (wdem && (st = unstage_out(ctx, sw, s)) != PARGO_OK) return st;
     if (slope && (st = unstage_out(ctx, ss, s)) != PARGO_OK) return st;
     if (d8 && (st = unstage_out(ctx, sd, s)) != PARGO_OK) return st;
