@@ -279,7 +279,11 @@ pargo_status pargo_slope_loss_grad(pargo_ctx* ctx, const pargo_raster* z, const 
  * the library until the process exits.  All calls share that array: calls that
  * overlap on the GPU race, so serialise them.  The first call on a device looks
  * up the array's address (once per device); make it before any stream capture.
- * Synchronous: returns after the result and the completion count are known. */
+ * The address is kept until the process exits, so calls after cudaDeviceReset
+ * are not supported.  Layout rules as elsewhere (pitch a whole number of
+ * elements covering a row, data aligned to its element size; otherwise
+ * PARGO_ERR_INVALID_ARG).  Synchronous: returns after the result and the
+ * completion count are known. */
 #define PARGO_SCA_NOALLOC_MAX_CELLS (1LL << 20)
 pargo_status pargo_sca_noalloc(const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr, int contract,
                                void* stream);

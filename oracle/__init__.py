@@ -120,6 +120,17 @@ class Oracle:
             raise OracleError("orc_sca_topo rc=%d" % rc)
         return ship if shipped else conv
 
+    def sca_both(self, d8, nodata):
+        """(converged, shipped) SCA from one topological accumulation."""
+        a = _c(d8, np.float64)
+        conv = np.empty(a.shape, np.float64)
+        ship = np.empty(a.shape, np.float64)
+        rc = self.lib.orc_sca_topo(_p(a, _c_f64p), a.shape[0], a.shape[1], nodata, _p(conv, _c_f64p),
+                                   _p(ship, _c_f64p))
+        if rc:
+            raise OracleError("orc_sca_topo rc=%d" % rc)
+        return conv, ship
+
 
 
     def mfd(self, dem, nodata, cellsize, slp_exp):

@@ -20,7 +20,13 @@
 //    per-cell scratch, the counters are cleared with a memset).
 // The first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (once per device, with that device current); make that
-// first call before any stream capture begins.
+// first call before any stream capture begins.  The address is kept for the
+// life of the process: after cudaDeviceReset (which unloads the library's
+// device image) the cached address is stale, so calls after a reset are not
+// supported.
+//
+// Every call is synchronous: it waits on `stream` for the completion count
+// before it returns.
 
 #include <math.h>
 
@@ -77,11 +83,18 @@ extern "C" pargo_status pargo_sca_noalloc(const pargo_raster* d8, pargo_raster* 
         return PARGO_ERR_INVALID_ARG;
     if (d8->rows < 3 || d8->cols < 3 || d8->rows != sca->rows || d8->cols != sca->cols)
         return PARGO_ERR_INVALID_ARG;
-    if (d8->rows * d8->cols > kMaxCells) return PARGO_ERR_INVALID_ARG;  // beyond the fixed scratch
+    if (d8->rows > INT32_MAX || d8->cols > INT32_MAX) return PARGO_ERR_INVALID_ARG;
+    if (d8->rows > kMaxCells / d8->cols) return PARGO_ERR_INVALID_ARG;  // beyond the fixed scratch (no overflow)
     if (elem_size(d8->dtype) == 0 || (sca->dtype != PARGO_F64 && sca->dtype != PARGO_F32))
         return PARGO_ERR_INVALID_ARG;
-    if (pitch_or_dense(d8) < d8->cols * elem_size(d8->dtype) || pitch_or_dense(sca) < sca->cols * elem_size(sca->dtype))
-        return PARGO_ERR_INVALID_ARG;
+    // The same layout rules as every other entry point: pitches cover a row and
+    // are whole elements, and the data is aligned to its element size (a
+    // misaligned load or store in a kernel would end the CUDA context).
+    for (const pargo_raster* r : {(const pargo_raster*)d8, (const pargo_raster*)sca}) {
+        const int64_t es = (int64_t)elem_size(r->dtype);
+        if (r->pitch < 0 || (r->pitch != 0 && r->pitch < r->cols * es) || r->pitch % es != 0) return PARGO_ERR_INVALID_ARG;
+        if ((uintptr_t)r->data % (uintptr_t)es != 0) return PARGO_ERR_INVALID_ARG;
+    }
     if (contract != PARGO_SCA_CONVERGED && contract != PARGO_SCA_SHIPPED) return PARGO_ERR_INVALID_ARG;
     if (nbr) {
         const int half = ((int)sqrt((double)nbr->count)) / 2;
