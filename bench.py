@@ -17,9 +17,16 @@ hydro2048 and sca4096 are small cases of the same code for profiler captures.
 Multi-GPU: replicas only -- each rank runs the same workload on its own GPU,
 nothing is exchanged on the data path; value = all ranks' cells / max time.
 
+The default line also carries, under "sub", the rest of the headline metric
+timed in the same run: slope32768 (fused slope + D8 on the 32768^2 DEM, % of
+HBM) and batch512 (the batched launch against the per-raster launches).
+
 --impl reference: the reference's own CPU algorithm (the pinned C port of the
-reference operators: raster-order Gauss-Seidel pit removal, OpenMP slope/D8)
-on the machine's host cores, each step a bounded crop of the same workload.
+reference operators) on the host cores: each step slope + D8 over the full
+8192^2 DEM with every core (OpenMP rows) plus the serial raster-order
+Gauss-Seidel pit removal on a 1024^2 crop, its per-cell time scaled to the
+full raster; once, a one-thread slope + D8 and the fill on 512^2 and 2048^2
+crops show how the CPU rates depend on threads and size.
 """
 import argparse
 import json
@@ -154,21 +161,43 @@ def make_hydro(rows=8192, cols=8192):
     return synth.hydro_dem(rows, cols, seed=1, hurst=0.75, relief=3000.0)
 
 
-def cpu_sample_hydro(dem, threads):
-    """Reference CPU algorithm on a 1024 x 1024 crop: raster-order Gauss-Seidel
-    pit removal (serial, the only valid reference mode), then slope + D8 on the
-    filled levels (OpenMP over rows)."""
+def cpu_fill_crop(dem, side, O=None):
+    """The reference's pit removal (raster-order Gauss-Seidel sweeps, serial:
+    its OpenMP path races) on a centred side x side crop of `dem`, gap 1e-3.
+    Returns (cells, seconds, sweeps)."""
     import oracle
-    O = oracle.Oracle()
-    r0 = max(0, min(2000, dem.shape[0] - 1024))
-    c0 = max(0, min(3000, dem.shape[1] - 1024))
-    crop = np.ascontiguousarray(dem[r0:r0 + 1024, c0:c0 + 1024])
+    O = O or oracle.Oracle()
+    r0 = max(0, (dem.shape[0] - side) // 2)
+    c0 = max(0, (dem.shape[1] - side) // 2)
+    crop = np.ascontiguousarray(dem[r0:r0 + side, c0:c0 + side])
     t0 = time.perf_counter()
-    w, sweeps = O.fill_gs(crop, ND, gap=1e-3)
-    O.slope(w, ND, 30.0, threads=threads)
-    O.d8(w, ND, threads=threads)
-    dt = time.perf_counter() - t0
-    return crop.size, dt, sweeps
+    _, sweeps = O.fill_gs(crop, ND, gap=1e-3)
+    return crop.size, time.perf_counter() - t0, sweeps
+
+
+def cpu_slope_d8(dem, threads, O=None):
+    """The reference's Horn slope and D8 over the whole raster (its OpenMP row
+    loop, `threads` threads).  Returns (cells, seconds)."""
+    import oracle
+    O = O or oracle.Oracle()
+    t0 = time.perf_counter()
+    O.slope(dem, ND, 30.0, threads=threads)
+    O.d8(dem, ND, threads=threads)
+    return dem.size, time.perf_counter() - t0
+
+
+def cpu_sample_hydro(dem, threads, crop=1024, O=None):
+    """One bounded CPU sample of the hydro step: slope + D8 over the full
+    raster on `threads` cores, and the serial Gauss-Seidel fill on a crop x
+    crop crop.  Returns (Mcells/s of the composite, details): the composite
+    is the full raster's cells over (slope+D8 time + the crop's fill time per
+    cell x the full raster's cells) -- the fill's per-cell cost taken from the
+    crop, which favours the CPU (its sweep count grows with the raster)."""
+    n_sd8, t_sd8 = cpu_slope_d8(dem, threads, O)
+    n_f, t_f, sweeps = cpu_fill_crop(dem, crop, O)
+    t_full = t_sd8 + t_f / n_f * dem.size
+    return dem.size / t_full / 1e6, {"slope_d8_s": round(t_sd8, 3), "fill_crop_s": round(t_f, 3),
+                                     "fill_crop_side": crop, "fill_crop_sweeps": sweeps}
 
 
 def run_hydro(args, ws, rank, local, side=8192):
@@ -263,11 +292,13 @@ def run_hydro(args, ws, rank, local, side=8192):
     cpu = None
     if rank == 0 and ws == 1:
         thr = os.cpu_count() or 1
-        n, dt, sweeps = cpu_sample_hydro(dem, thr)
-        cpu = {"value": round(n / dt / 1e6, 3), "unit": "Mcells/s", "cores": thr, "kind": "port",
-               "sample": "1024x1024 crop of the same DEM: reference-order Gauss-Seidel pit removal (serial, %d "
-                         "sweeps) + slope + D8 (OpenMP, %d threads), %.1f s; sweeps grow with raster size, so "
-                         "the full 8192^2 CPU rate is lower still" % (sweeps, thr, dt)}
+        v, det = cpu_sample_hydro(dem, thr)
+        cpu = {"value": round(v, 3), "unit": "Mcells/s", "cores": thr, "kind": "port",
+               "sample": "slope + D8 over the full %dx%d DEM (the reference's OpenMP loop, %d threads, %.2f s) and "
+                         "the serial Gauss-Seidel fill on a centred 1024x1024 crop (%d sweeps, %.2f s) scaled per "
+                         "cell to the full raster; the fill's sweep count grows with raster size, so the CPU's "
+                         "true full-size rate is lower still" % (rows, cols, thr, det["slope_d8_s"],
+                                                                 det["fill_crop_sweeps"], det["fill_crop_s"])}
     return {
         "metric": "Mcells/s slope+D8+fill", "value": round(value, 2), "unit": "Mcells/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
@@ -448,16 +479,16 @@ def timed_steps(fn, args, stream, flush=None):
 
 
 def run_sca(args, ws, rank, local, side=16384):
-    """D8 specific catchment area on the filled side^2 DEM of the hydro
-    generator (seed 2, 10 m cells): setup (untimed) fills the DEM and derives
-    the int8 D8 codes on the GPU; a step is one SCA call (topological
-    accumulation, float64 output)."""
+    """D8 specific catchment area on the filled side^2 DEM of the slope
+    generator (seed 2, Hurst 0.8, 0-2000 m, 1-cell nodata border, 10 m
+    cells): setup (untimed) fills the DEM (gap 1e-3) and derives the int8 D8
+    codes on the GPU; a step is one SCA call (float64 output)."""
     import torch
     from pargo_gb300 import abi
     torch.cuda.set_device(local)
     ctx = abi.Context(local)
     from pargo_gb300 import synth
-    dem = synth.hydro_dem(side, side, seed=2, hurst=0.75, relief=3000.0)
+    dem = synth.slope_dem(side, side, seed=2, hurst=0.8, relief=2000.0)
     cells = side * side
     stream = torch.cuda.current_stream()
     R = abi.raster
@@ -503,8 +534,9 @@ def run_sca(args, ws, rank, local, side=16384):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 accumulation (u64 counts)",
         "data": "synthetic",
-        "config": {"workload": "sca%d: D8 SCA on the filled %dx%d hydro DEM (seed 2, 10 m cells), int8 codes in, "
-                               "float64 out" % (side, side, side), "l2": "inputs larger than L2"},
+        "config": {"workload": "sca%d: D8 SCA on the filled %dx%d fBm DEM (seed 2, H 0.8, 0-2000 m, 10 m cells, "
+                               "gap 1e-3), int8 codes in, float64 out" % (side, side, side),
+                   "l2": "inputs larger than L2"},
         "roofline": {"bound": "hbm", "kernel": "sca_tile_kernel x2 + exit forest (3 kernels) + sca_output_kernel "
                                "(one call)", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
@@ -658,7 +690,10 @@ def run_mfd(args, ws, rank, local, side=8192):
                "sample": "1024x1024 crop of the same levels: the oracle's MFD-md weights + one-sweep MFD SCA "
                          "(serial, as the reference), %.2f s" % dt}
     peak, kind = hbm_peak()
-    achieved = cells * 40.0 / (ms_w * 1e-3) / 1e9
+    # the dominant kernel is the MFD SCA (the weights are ~1.5% of the step):
+    # 8 float32 weight layers read (32 B) and the float64 SCA written (8 B) per cell
+    achieved = cells * 40.0 / (ms_s * 1e-3) / 1e9
+    achieved_w = cells * 40.0 / (ms_w * 1e-3) / 1e9
     return {
         "metric": "Mcells/s MFD-md weights + MFD SCA", "value": round(ws * cells / (ms * 1e-3) / 1e6, 1),
         "unit": "Mcells/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -667,10 +702,14 @@ def run_mfd(args, ws, rank, local, side=8192):
         "config": {"workload": "mfd%d: MFD-md weights (exponent 1.1) + MFD SCA on the pit-removed %dx%d hydro "
                                "DEM (seed 1, 30 m cells, float64 levels), 8 float32 layers, float64 SCA"
                                % (side, side, side), "l2": "inputs larger than L2"},
-        "roofline": {"bound": "hbm", "kernel": "mfd_weights_kernel", "achieved": round(achieved, 1),
-                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
-                     "traffic": None, "algorithmic_bytes_per_cell": 40, "weights_ms": round(ms_w, 3),
-                     "sca_ms": round(ms_s, 3)},
+        "roofline": {"bound": "hbm", "kernel": "sca_mfd_persistent_kernel (MFD SCA, every frontier round in one "
+                                               "cooperative launch)", "achieved": round(achieved, 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": kind,
+                     "traffic": None, "algorithmic_bytes_per_cell": 40, "sca_ms": round(ms_s, 3),
+                     "sca_share_of_step": round(ms_s / ms, 4) if ms > 0 else None,
+                     "weights_kernel": {"kernel": "mfd_weights_kernel", "ms": round(ms_w, 3),
+                                        "achieved": round(achieved_w, 1), "frac": round(achieved_w / peak, 4),
+                                        "algorithmic_bytes_per_cell": 40}},
         "cpu_baseline": cpu,
         "e2e": {"value": round(ws * cells / e2e_s / 1e6, 1), "unit": "Mcells/s", "h2d_bytes_per_step": cells * 8,
                 "d2h_bytes_per_step": cells * (32 + 8)},
@@ -759,27 +798,56 @@ def run_load(args, ws, rank, local, side=32768, grain=16):
 
 
 def run_reference(args, ws, rank):
+    """The reference's CPU algorithm (the oracle's C port of the reference
+    operators; the reference's own build needs its sources, which only the
+    build container holds) on this host's cores, on the hydro8192 workload.
+    Each step: slope + D8 over the full 8192^2 DEM with every core (the
+    reference's OpenMP loop) and the serial Gauss-Seidel fill (its only valid
+    mode) on a centred 1024^2 crop; value = the full raster's cells over the
+    slope+D8 time plus the crop's per-cell fill time scaled to the full
+    raster.  Once, untimed by the steps: slope + D8 on one thread, and the
+    fill on 512^2 and 2048^2 crops, to show how its rate falls with size."""
     if rank != 0:
         return None
+    import oracle
+    O = oracle.Oracle()
     thr = os.cpu_count() or 1
     dem = make_hydro()
-    vals = []
+    n1, t1 = cpu_slope_d8(dem, 1, O)
+    crops = []
+    for side in (512, 1024, 2048):
+        n, t, sw = cpu_fill_crop(dem, side, O)
+        crops.append({"side": side, "sweeps": sw, "s": round(t, 3), "Mcells_s": round(n / t / 1e6, 4)})
     for _ in range(args.warmup):
-        cpu_sample_hydro(dem, thr)
+        cpu_sample_hydro(dem, thr, O=O)
+    vals, dets = [], []
     for _ in range(args.steps):
-        n, dt, sweeps = cpu_sample_hydro(dem, thr)
-        vals.append(n / dt / 1e6)
+        v, det = cpu_sample_hydro(dem, thr, O=O)
+        vals.append(v)
+        dets.append(det)
     v = float(np.mean(vals))
+    sd8 = float(np.mean([d["slope_d8_s"] for d in dets]))
+    fc = float(np.mean([d["fill_crop_s"] for d in dets]))
+    sweeps = dets[-1]["fill_crop_sweeps"]
+    desc = ("hydro8192: slope + D8 over the full 8192x8192 DEM on %d cores (%.2f s), serial Gauss-Seidel fill "
+            "(gap 1e-3) on a centred 1024x1024 crop (%d sweeps, %.2f s), its per-cell time scaled to the full "
+            "raster" % (thr, sd8, sweeps, fc))
     return {
-        "impl": "reference", "metric": "Mcells/s slope+D8+fill", "value": round(v, 3), "unit": "Mcells/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1024 * 1024 / v / 1e3, 3),
+        "impl": "reference", "metric": "Mcells/s slope+D8+fill", "value": round(v, 4), "unit": "Mcells/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dem.size / v / 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "config": {"workload": "hydro8192 (crop 1024x1024 per step)"},
-        "cpu_baseline": {"value": round(v, 3), "unit": "Mcells/s", "cores": thr, "kind": "port",
-                         "sample": "1024x1024 crop per step: reference-order Gauss-Seidel pit removal (serial, "
-                                   "%d sweeps) + slope + D8 (OpenMP, %d threads); the reference itself compiles "
-                                   "only here (x86), its pinned C port runs on this host" % (sweeps, thr)},
-        "e2e": {"value": round(v, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "data": "synthetic (seeded fBm, same DEM as the GPU arm)",
+        "config": {"workload": desc, "rows": 8192, "cols": 8192,
+                   "slope_d8_size": "8192x8192 (full)", "fill_size": "1024x1024 crop (scaled per cell)"},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mcells/s", "cores": thr, "kind": "port", "sample": desc},
+        "slope_d8_full_size": {"threads": thr, "s": round(sd8, 3), "Mcells_s": round(dem.size / sd8 / 1e6, 2)},
+        "slope_d8_one_thread": {"threads": 1, "s": round(t1, 3), "Mcells_s": round(n1 / t1 / 1e6, 2)},
+        "fill_crops": crops,
+        # the crops' fill rate fitted as a power of the side and carried to the full raster (informative)
+        "fill_rate_extrapolated_8192": {"Mcells_s": round(float(np.exp(np.polyval(np.polyfit(
+            np.log([c["side"] for c in crops]), np.log([c["Mcells_s"] for c in crops]), 1), np.log(8192)))), 5),
+            "method": "least-squares line through log(rate) against log(side) of the three crops"},
+        "e2e": {"value": round(v, 4), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
 
@@ -789,6 +857,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-sub", action="store_true", help="default workload only: skip the slope32768 and "
+                    "batch512 sub-records")
     ap.add_argument("--workload", default="hydro8192",
                     choices=["hydro8192", "hydro2048", "slope32768", "slope8192", "slope1024", "batch512",
                              "sca16384", "sca4096", "grad8192", "mfd8192", "mfd2048", "load32768", "load8192"])
@@ -799,6 +869,19 @@ def main():
         out = run_reference(args, ws, rank)
     elif args.workload.startswith("hydro"):
         out = run_hydro(args, ws, rank, local, int(args.workload[5:]))
+        if args.workload == "hydro8192" and not args.no_sub:
+            # the rest of the headline metric, timed in the same run: slope+D8
+            # on the 32768^2 DEM (% of HBM), and the batched launch over 512
+            # uneven rasters against the per-raster launches
+            import gc
+            import torch
+            sub = {}
+            for name, fn in (("slope32768", lambda: run_slope(args, ws, rank, local, 32768)),
+                             ("batch512", lambda: run_batch(args, ws, rank, local))):
+                gc.collect()
+                torch.cuda.empty_cache()
+                sub[name] = fn()
+            out["sub"] = sub
     elif args.workload.startswith("sca"):
         out = run_sca(args, ws, rank, local, int(args.workload[3:]))
     elif args.workload.startswith("load"):
