@@ -13,9 +13,9 @@
  *   pargo_nbr_parse               operator>>(istream&, Neighborhood&) gpro/neighborhood.h:626-662
  *                                 + Neighborhood::_initCoords checks :110-194
  *
- * and three additions with no reference counterpart: batched slope+D8 over
- * many rasters in one launch, and the forward/backward (adjoint) pair of Horn
- * slope.
+ * and additions with no reference counterpart: batched slope+D8 and batched
+ * pit removal over many rasters in one launch, and the forward/backward
+ * (adjoint) pair of Horn slope.
  *
  * Conventions
  *  - Plain C: pointers, sizes, enums.  `stream` is a cudaStream_t passed as
@@ -169,6 +169,20 @@ pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps,
 pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* wdem, const pargo_nbr* nbr,
                         const pargo_fill_opts* opts, pargo_fill_stats* stats, void* stream);
 
+/* Batched pit removal: `count` independent rasters (all on the device) in one
+ * persistent relaxation.  The rasters are packed side by side into one mosaic
+ * whose nodata separates them -- each raster's ring is a nodata level in the
+ * reference (PitRemoveOperator's wdem is initialised from copyLayerInfo), so
+ * no level of one raster is a neighbour of a level of another -- and every
+ * output holds exactly what pargo_fill gives for its raster.  dems: all F32 or
+ * all F64 with one nodata value (otherwise the rasters are filled one by one,
+ * with the same results); wdems: F64 or F32.  stats (may be NULL) covers the
+ * whole batch.  No reference counterpart: the reference removes pits raster by
+ * raster (pPitRemove.cpp).  Synchronous. */
+pargo_status pargo_batch_fill(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* wdems,
+                              const pargo_nbr* nbr, const pargo_fill_opts* opts, pargo_fill_stats* stats,
+                              void* stream);
+
 /* Device-resident hydrology chain, as the reference runs it through files
  * (pPitRemove.cpp:129 -> pD8.cpp:113 -> pSCA.cpp:59): pit removal, then slope
  * and D8 on the float64 levels (what the reference D8 reads from the Float64
@@ -249,10 +263,48 @@ pargo_status pargo_load_decompose(pargo_ctx* ctx, const pargo_raster* load, int 
 
 /* Batched fused slope + D8 over `count` independent rasters in one persistent
  * launch; slopes / d8s may be NULL (no such output) and all rasters must be on
- * the device. */
+ * the device.  The launch's warps claim work items -- 128-column by 48-row
+ * segments of every raster -- from one device queue.  The queue is ordered
+ * heaviest first by the load estimator's intensity-ratio estimate
+ * (Transformation::Operator, gpro/transformation.h:155-197: valid_load per
+ * cell with |v - nodata| > 1e-7, nodata_load per other cell), counted per
+ * segment on the device the first time a batch description (buffers, shapes,
+ * options) is seen and kept with the batch's other device tables; the order
+ * balances the work only and never changes an output.  pargo_batch_slope_d8
+ * uses the defaults: by intensity, nodata_load 0, valid_load 1 (the
+ * reference's "-nodataLoad 0 -validLoad 1", apps/spatial/reclassify/
+ * pRelclassify.cpp:22).  Configurations outside the strip walk (slope methods
+ * other than Horn, degrees, dirType 256, unaligned rows) run a tiled launch
+ * whose queue is ordered by raster size. */
+typedef enum pargo_batch_order {
+    PARGO_BATCH_BY_INTENSITY = 0, /* segments by estimated load, heaviest first */
+    PARGO_BATCH_BY_SIZE = 1       /* raster by raster, largest raster first */
+} pargo_batch_order;
+
+typedef struct pargo_batch_opts {
+    double nodata_load;  /* Transformation::_nodataLoad (gpro/transformation.h:67), >= 0 */
+    double valid_load;   /* Transformation::_validLoad (gpro/transformation.h:68), >= 0 */
+    int32_t order;       /* pargo_batch_order */
+    int32_t reserved;    /* 0 */
+} pargo_batch_opts;
+
 pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* slopes,
                                   pargo_raster* d8s, const pargo_nbr* nbr, int method, int units, int dir_type,
                                   void* stream);
+pargo_status pargo_batch_slope_d8_ex(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* slopes,
+                                     pargo_raster* d8s, const pargo_nbr* nbr, int method, int units, int dir_type,
+                                     const pargo_batch_opts* opts, void* stream);
+
+/* The work queue the batched strip walk uses for these rasters and options:
+ * *n_out = the number of segments; for the first `cap` queue positions i,
+ * raster[i] (the caller's index), segment[i] (within its raster: strip
+ * segment % strips, band segment / strips, strips = ceil(cols / 128)) and
+ * load[i] (its estimated load); any output pointer may be NULL.  dems: F32 on
+ * the device.  Synchronous.  No reference counterpart (the reference splits
+ * rows among MPI ranks by the same estimate, deComposition.h:305-393). */
+pargo_status pargo_batch_queue(pargo_ctx* ctx, int count, const pargo_raster* dems, const pargo_batch_opts* opts,
+                               int64_t cap, int64_t* n_out, int32_t* raster, int64_t* segment, double* load,
+                               void* stream);
 
 /* Differentiable Horn (FD) slope.  Forward: slope of z into `slope`.
  * Backward: given dL/dslope per cell (`gslope`, F32), accumulate dL/dz into

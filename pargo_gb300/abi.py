@@ -50,6 +50,14 @@ class FillOpts(ctypes.Structure):
     _fields_ = [("gap", ctypes.c_double), ("init_level", ctypes.c_double), ("max_rounds", ctypes.c_int64)]
 
 
+class BatchOpts(ctypes.Structure):
+    _fields_ = [("nodata_load", ctypes.c_double), ("valid_load", ctypes.c_double), ("order", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+BATCH_BY_INTENSITY, BATCH_BY_SIZE = 0, 1
+
+
 class FillStats(ctypes.Structure):
     _fields_ = [("rounds", ctypes.c_int64), ("active_rounds", ctypes.c_int64), ("tile_visits", ctypes.c_int64),
                 ("local_iterations", ctypes.c_int64), ("raised_cells", ctypes.c_int64), ("rounds_ms", ctypes.c_double)]
@@ -86,6 +94,10 @@ def lib():
         L.pargo_load_decompose.argtypes = [vp, R, i, i64, i64, N, i, i64p, i64p, vp]
         L.pargo_hydro_pipeline.argtypes = [vp, R, R, R, R, R, N, P(FillOpts), i, i, i, P(FillStats), vp]
         L.pargo_batch_slope_d8.argtypes = [vp, i, R, R, R, N, i, i, i, vp]
+        L.pargo_batch_fill.argtypes = [vp, i, R, R, N, P(FillOpts), P(FillStats), vp]
+        L.pargo_batch_slope_d8_ex.argtypes = [vp, i, R, R, R, N, i, i, i, P(BatchOpts), vp]
+        L.pargo_batch_queue.argtypes = [vp, i, R, P(BatchOpts), ctypes.c_int64, P(ctypes.c_int64),
+                                        P(ctypes.c_int32), P(ctypes.c_int64), P(ctypes.c_double), vp]
         L.pargo_slope_fwd.argtypes = [vp, R, R, N, vp]
         L.pargo_slope_bwd.argtypes = [vp, R, R, R, N, vp]
         L.pargo_slope_loss_grad.argtypes = [vp, R, R, R, P(ctypes.c_double), N, vp]
@@ -98,7 +110,9 @@ def lib():
         for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
                      "pargo_fill", "pargo_sca", "pargo_twi", "pargo_mfd", "pargo_sca_mfd", "pargo_compute_load_dims",
                      "pargo_compute_load", "pargo_load_decompose",
-                     "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_slope_fwd", "pargo_slope_bwd",
+                     "pargo_hydro_pipeline", "pargo_batch_slope_d8", "pargo_batch_fill", "pargo_batch_slope_d8_ex",
+                     "pargo_batch_queue", "pargo_slope_fwd",
+                     "pargo_slope_bwd",
                      "pargo_slope_loss_grad"):
             getattr(L, name).restype = st
         _lib = L
@@ -276,13 +290,50 @@ class Context:
         return comp, bounds
 
     def batch_slope_d8(self, dems, slopes=None, d8s=None, method=SLOPE_FD, units=RATIO, dir_type=8, nbr=None,
-                       stream=None):
+                       stream=None, nodata_load=None, valid_load=None, order=None):
+        """Batched slope + D8; the queue options default to the library's
+        (by intensity, nodata_load 0, valid_load 1)."""
         n = len(dems)
         D = (Raster * n)(*dems)
         S = (Raster * n)(*slopes) if slopes else None
         C = (Raster * n)(*d8s) if d8s else None
-        self._check(lib().pargo_batch_slope_d8(self._p, n, D, S, C, self._nbr(nbr), method, units, dir_type,
-                                               _stream_ptr(stream)))
+        if nodata_load is None and valid_load is None and order is None:
+            self._check(lib().pargo_batch_slope_d8(self._p, n, D, S, C, self._nbr(nbr), method, units, dir_type,
+                                                   _stream_ptr(stream)))
+            return
+        o = BatchOpts(0.0 if nodata_load is None else nodata_load, 1.0 if valid_load is None else valid_load,
+                      BATCH_BY_INTENSITY if order is None else order, 0)
+        self._check(lib().pargo_batch_slope_d8_ex(self._p, n, D, S, C, self._nbr(nbr), method, units, dir_type,
+                                                  ctypes.byref(o), _stream_ptr(stream)))
+
+    def batch_queue(self, dems, nodata_load=0.0, valid_load=1.0, order=BATCH_BY_INTENSITY, stream=None):
+        """The batched strip walk's work queue: (raster index, segment, load) arrays in queue order."""
+        n = len(dems)
+        D = (Raster * n)(*dems)
+        o = BatchOpts(nodata_load, valid_load, order, 0)
+        total = ctypes.c_int64(0)
+        self._check(lib().pargo_batch_queue(self._p, n, D, ctypes.byref(o), 0, ctypes.byref(total), None, None, None,
+                                            _stream_ptr(stream)))
+        m = total.value
+        ras = np.zeros(m, np.int32)
+        seg = np.zeros(m, np.int64)
+        ld = np.zeros(m, np.float64)
+        self._check(lib().pargo_batch_queue(
+            self._p, n, D, ctypes.byref(o), m, ctypes.byref(total), ras.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+            seg.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), ld.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+            _stream_ptr(stream)))
+        return ras, seg, ld
+
+    def batch_fill(self, dems, wdems, gap=0.0005, init_level=10000.0, max_rounds=0, nbr=None, stream=None):
+        """Pit removal of many device rasters in one persistent relaxation; returns the batch's FillStats."""
+        n = len(dems)
+        D = (Raster * n)(*dems)
+        W = (Raster * n)(*wdems)
+        opts = FillOpts(gap, init_level, max_rounds)
+        stats = FillStats()
+        self._check(lib().pargo_batch_fill(self._p, n, D, W, self._nbr(nbr), ctypes.byref(opts), ctypes.byref(stats),
+                                           _stream_ptr(stream)))
+        return stats
 
     def slope_fwd(self, z, slope, nbr=None, stream=None):
         self._check(lib().pargo_slope_fwd(self._p, ctypes.byref(z), ctypes.byref(slope), self._nbr(nbr),

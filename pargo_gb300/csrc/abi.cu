@@ -47,6 +47,7 @@ struct pargo_ctx {
     std::string fill_graph_key;
     // batch table cache
     std::string batch_key;
+    bool batch_ordered = false;  // the cached batch has an intensity-ordered queue (kSlotBatchOrder)
     // autotuned focal kernel variant per size class (log2 of the cell count); -1 = untuned
     int focal_variant[64];
     pargo_ctx() {
@@ -60,7 +61,8 @@ enum SlotId {
     kSlotBatchParams, kSlotBatchStart, kSlotBatchNtx, kSlotBatchDems, kSlotClaim, kSlotLoss, kSlotGradOut,
     kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotMfdLayer0,
     kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotStripSlow, kSlotLoadRows,
-    kSlotBatchStripMaps, kSlotBatchSegStart, kSlotBatchNstrips, kSlotBatchSlow, kSlotCount
+    kSlotBatchStripMaps, kSlotBatchSegStart, kSlotBatchNstrips, kSlotBatchSlow, kSlotFillMosaic, kSlotFillItems,
+    kSlotBatchSegLoad, kSlotBatchOrder, kSlotCount
 };
 static_assert(kSlotCount <= 48, "context slot table");
 
@@ -905,6 +907,145 @@ pargo_status pargo_fill(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* w
     return PARGO_OK;
 }
 
+// ------------------------------------------------------------ batch fill --
+// Pit removal of many rasters in one persistent relaxation: the rasters are
+// shelf-packed into one mosaic DEM (each raster's ring and nodata cells, and
+// the mosaic cells outside the rasters, become nodata -- two neighbouring
+// rasters meet at two rows or columns of nodata levels, so they never see
+// each other), the mosaic is filled by the single-raster machinery, and each
+// raster's rectangle of levels goes to its own output.  Rasters whose nodata
+// differ from the first one's (a common nodata is what the mosaic needs) are
+// filled one by one instead.
+static pargo_status batch_fill_one_by_one(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* wdems,
+                                   const pargo_nbr* nbr, const pargo_fill_opts* opts, pargo_fill_stats* stats,
+                                   void* stream) {
+    pargo_fill_stats total{};
+    for (int i = 0; i < count; i++) {
+        pargo_fill_stats one{};
+        pargo_status st = pargo_fill(ctx, &dems[i], &wdems[i], nbr, opts, &one, stream);
+        if (st != PARGO_OK) return st;
+        total.rounds += one.rounds;
+        total.active_rounds += one.active_rounds;
+        total.tile_visits += one.tile_visits;
+        total.local_iterations += one.local_iterations;
+        total.raised_cells += one.raised_cells;
+        total.rounds_ms += one.rounds_ms;
+    }
+    if (stats) *stats = total;
+    return PARGO_OK;
+}
+
+pargo_status pargo_batch_fill(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* wdems,
+                                         const pargo_nbr* nbr, const pargo_fill_opts* opts, pargo_fill_stats* stats,
+                                         void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (count < 0 || (count > 0 && (!dems || !wdems)))
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "batch fill: bad count, dems or wdems");
+    if (stats) *stats = pargo_fill_stats{};
+    if (count == 0) return PARGO_OK;
+    pargo_status st;
+    pargo_fill_opts o;
+    bool mosaic = true;
+    for (int i = 0; i < count; i++) {
+        if ((st = check_fill_args(ctx, &dems[i], nbr, opts, &o)) != PARGO_OK) return st;
+        if ((st = check_raster(ctx, &wdems[i], "batch wdem")) != PARGO_OK) return st;
+        if ((st = check_same(ctx, &dems[i], &wdems[i], "batch wdem")) != PARGO_OK) return st;
+        if (wdems[i].dtype != PARGO_F64 && wdems[i].dtype != PARGO_F32)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "batch fill: wdem %d must be F64 or F32", i);
+        if (dems[i].location != PARGO_DEVICE || wdems[i].location != PARGO_DEVICE)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "batch fill: raster %d must be on the device", i);
+        if (dems[i].dtype != dems[0].dtype || !(dems[i].nodata == dems[0].nodata)) mosaic = false;
+    }
+    const bool f64 = dems[0].dtype == PARGO_F64;
+    const Band<float> bf = float_band(dems[0].nodata, kEpsHydro);
+    const Band<double> bd = double_band(dems[0].nodata, kEpsHydro);
+    if (!f64 && !(bf.lo <= bf.hi)) mosaic = false;  // no float value stands for this nodata
+    if (!(bd.lo <= bd.hi)) mosaic = false;
+    if (!mosaic) return batch_fill_one_by_one(ctx, count, dems, wdems, nbr, opts, stats, stream);
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    // Shelf packing: tallest rasters first, left to right on shelves of the
+    // mosaic's width (at least the widest raster, about square overall).
+    std::vector<int> order(count);
+    int64_t total = 0, max_cols = 0, max_cells = 0;
+    for (int i = 0; i < count; i++) {
+        order[i] = i;
+        total += dems[i].rows * dems[i].cols;
+        max_cols = std::max(max_cols, dems[i].cols);
+        max_cells = std::max(max_cells, dems[i].rows * dems[i].cols);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dems[a].rows > dems[b].rows; });
+    const int64_t width = std::max(max_cols, (int64_t)ceil(sqrt((double)total * 1.15)));
+    std::vector<FillBatchItem> items(count);
+    int64_t x = 0, y = 0, shelf = 0;
+    for (int k = 0; k < count; k++) {
+        const int i = order[k];
+        if (x + dems[i].cols > width) {
+            y += shelf;
+            x = 0;
+            shelf = 0;
+        }
+        FillBatchItem& it = items[k];
+        it.dem = dems[i].data;
+        it.pitch = pitch_of(&dems[i]);
+        it.rows = dems[i].rows;
+        it.cols = dems[i].cols;
+        it.oy = y;
+        it.ox = x;
+        it.nd6f = bf;
+        it.nd6d = bd;
+        it.out = OutView{(char*)wdems[i].data, pitch_of(&wdems[i]), wdems[i].dtype, wdems[i].nodata};
+        x += dems[i].cols;
+        shelf = std::max(shelf, dems[i].rows);
+    }
+    const int64_t mrows = std::max<int64_t>(y + shelf, 3), mcols = std::max<int64_t>(width, 3);
+    if (mrows > INT32_MAX || mcols > INT32_MAX) return fail(ctx, PARGO_ERR_INVALID_ARG, "batch fill: batch too large");
+    const int64_t es = f64 ? 8 : 4;
+    const int64_t mstride = (mcols * es + 15) / 16 * 16 / es;
+    cudaError_t e;
+    void* md = slot(ctx, kSlotFillMosaic, (size_t)(mrows * mstride * es), &e);
+    if (!md) return cuda_fail(ctx, e, "batch fill mosaic");
+    FillBatchItem* ditems = (FillBatchItem*)slot(ctx, kSlotFillItems, (size_t)count * sizeof(FillBatchItem), &e);
+    if (!ditems) return cuda_fail(ctx, e, "batch fill table");
+    CU(ctx, cudaMemcpyAsync(ditems, items.data(), (size_t)count * sizeof(FillBatchItem), cudaMemcpyHostToDevice, s));
+    // the stored nodata: a value of the batch's own nodata band
+    const double nd_store = f64 ? dems[0].nodata : (double)bf.lo;
+    {
+        cudaError_t ee = fill_mosaic_pack(ditems, count, max_cells, md, mrows, mstride, f64 ? 1 : 0, nd_store, s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "batch fill pack");
+    }
+    pargo_raster mr{};
+    mr.data = md;
+    mr.dtype = dems[0].dtype;
+    mr.location = PARGO_DEVICE;
+    mr.rows = mrows;
+    mr.cols = mcols;
+    mr.pitch = mstride * es;
+    mr.nodata = dems[0].nodata;
+    mr.cellsize = dems[0].cellsize;
+    Staged sm;
+    sm.in = InView{(const char*)md, mstride * es, mr.dtype};
+    FillParams p;
+    bool converged = false;
+    pargo_fill_stats local{};
+    if ((st = fill_core(ctx, sm, &mr, o, &p, &local, &converged, s)) != PARGO_OK) return st;
+    {
+        cudaError_t ee = fill_mosaic_finish(p, ditems, count, max_cells, &ctx->d_counters[3], s);
+        if (ee != cudaSuccess) return cuda_fail(ctx, ee, "batch fill finish");
+    }
+    unsigned long long* hp = (unsigned long long*)pinned(ctx, 128, &e);
+    if (!hp) return cuda_fail(ctx, e, "pinned counters");
+    CU(ctx, cudaMemcpyAsync(hp, &ctx->d_counters[3], sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_call(ctx, s, true)) != PARGO_OK) return st;
+    local.raised_cells = (int64_t)hp[0];
+    if (stats) *stats = local;
+    if (!converged)
+        return fail(ctx, PARGO_ERR_NOT_CONVERGED, "batch fill: worklist not empty after %lld rounds",
+                    (long long)local.rounds);
+    return PARGO_OK;
+}
+
 // SCA by tiled subtree sums: scratch, launches (stream-ordered), and the
 // check of the completion counts once the stream has been synchronised.
 pargo_status sca_launch(pargo_ctx* ctx, const ScaParams& q, cudaStream_t s, const char* what) {
@@ -1484,15 +1625,148 @@ pargo_status pargo_sca(pargo_ctx* ctx, const pargo_raster* d8, pargo_raster* sca
 }
 
 // ------------------------------------------------------------------ batch --
+// Defaults of the batched queue: ordered by compute intensity with the
+// reference's example loads (a nodata cell 0, a valid cell 1: the
+// "-nodataLoad 0 -validLoad 1" of apps/spatial/reclassify/pRelclassify.cpp:22).
+static pargo_batch_opts batch_defaults(const pargo_batch_opts* opts) {
+    pargo_batch_opts o{0.0, 1.0, PARGO_BATCH_BY_INTENSITY, 0};
+    if (opts) o = *opts;
+    return o;
+}
+
+static pargo_status check_batch_opts(pargo_ctx* ctx, const pargo_batch_opts& o) {
+    if (o.order != PARGO_BATCH_BY_INTENSITY && o.order != PARGO_BATCH_BY_SIZE)
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "batch: unknown queue order %d", o.order);
+    if (!(o.nodata_load >= 0.0) || !(o.valid_load >= 0.0) || !std::isfinite(o.nodata_load) ||
+        !std::isfinite(o.valid_load))  // transformation.h:168-171 rejects negative loads
+        return fail(ctx, PARGO_ERR_INVALID_ARG, "batch: loads must be finite and not negative");
+    return PARGO_OK;
+}
+
+// The strip-walk queue of a batch ordered by compute intensity: every
+// segment's load (valid_load per valid cell, nodata_load per nodata cell,
+// counted on the device) and the segments sorted heaviest first (ties keep
+// the raster-by-raster order, largest raster first).  `korder[k]` is the
+// caller's index of the k-th raster by size; seg_start / nstrips follow k.
+// Returns queue position -> (k << 40 | segment of raster k) and the loads.
+static pargo_status batch_intensity_queue(pargo_ctx* ctx, int count, const pargo_raster* dems,
+                                          const std::vector<int>& korder, const std::vector<int64_t>& seg_start,
+                                          const std::vector<int>& nstrips, int64_t nsegs, const pargo_batch_opts& o,
+                                          cudaStream_t s, std::vector<uint64_t>* queue, std::vector<double>* loads) {
+    std::vector<SegLoadRaster> rs(count);
+    for (int k = 0; k < count; k++) {
+        const pargo_raster* d = &dems[korder[k]];
+        rs[k].dem = InView{(const char*)d->data, pitch_of(d), d->dtype};
+        rs[k].rows = d->rows;
+        rs[k].cols = d->cols;
+        rs[k].nd = float_band_incl(d->nodata, 0.0000001);  // transformation.h:187: |v - noData| > Eps is valid
+        rs[k].seg_start = seg_start[k];
+        rs[k].nstrips = nstrips[k];
+    }
+    const size_t tb = ((size_t)count * sizeof(SegLoadRaster) + 255) / 256 * 256;
+    cudaError_t e;
+    char* buf = (char*)slot(ctx, kSlotBatchSegLoad, tb + (size_t)nsegs * 4, &e);
+    if (!buf) return cuda_fail(ctx, e, "batch intensity table");
+    CU(ctx, cudaMemcpyAsync(buf, rs.data(), (size_t)count * sizeof(SegLoadRaster), cudaMemcpyHostToDevice, s));
+    uint32_t* dvalid = (uint32_t*)(buf + tb);
+    CU(ctx, launch_batch_segment_valid((const SegLoadRaster*)buf, count, nsegs, dvalid, ctx->num_sms, s));
+    std::vector<uint32_t> valid((size_t)nsegs);
+    CU(ctx, cudaMemcpyAsync(valid.data(), dvalid, (size_t)nsegs * 4, cudaMemcpyDeviceToHost, s));
+    CU(ctx, cudaStreamSynchronize(s));
+    const int SR = batch_strip_segment_rows(), SC = batch_strip_segment_cols();
+    loads->assign((size_t)nsegs, 0.0);
+    std::vector<uint64_t> ids((size_t)nsegs);
+    for (int k = 0; k < count; k++) {
+        const int64_t rows = rs[k].rows, cols = rs[k].cols;
+        for (int64_t l = 0; l < seg_start[k + 1] - seg_start[k]; l++) {
+            const int64_t g = seg_start[k] + l;
+            const int64_t x0 = (l % nstrips[k]) * SC, y0 = (l / nstrips[k]) * SR;
+            const int64_t cells = (std::min<int64_t>(y0 + SR, rows) - y0) * (std::min<int64_t>(x0 + SC, cols) - x0);
+            (*loads)[g] = (double)valid[g] * o.valid_load + (double)(cells - (int64_t)valid[g]) * o.nodata_load;
+            ids[g] = ((uint64_t)k << 40) | (uint64_t)l;
+        }
+    }
+    std::vector<int64_t> pos((size_t)nsegs);
+    for (int64_t g = 0; g < nsegs; g++) pos[g] = g;
+    std::stable_sort(pos.begin(), pos.end(), [&](int64_t a, int64_t b) { return (*loads)[a] > (*loads)[b]; });
+    queue->resize((size_t)nsegs);
+    std::vector<double> sorted((size_t)nsegs);
+    for (int64_t i = 0; i < nsegs; i++) {
+        (*queue)[i] = ids[pos[i]];
+        sorted[i] = (*loads)[pos[i]];
+    }
+    loads->swap(sorted);
+    return PARGO_OK;
+}
+
 pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* slopes,
                                   pargo_raster* d8s, const pargo_nbr* nbr, int method, int units, int dir_type,
                                   void* stream) {
+    return pargo_batch_slope_d8_ex(ctx, count, dems, slopes, d8s, nbr, method, units, dir_type, nullptr, stream);
+}
+
+pargo_status pargo_batch_queue(pargo_ctx* ctx, int count, const pargo_raster* dems, const pargo_batch_opts* opts,
+                               int64_t cap, int64_t* n_out, int32_t* raster, int64_t* segment, double* load,
+                               void* stream) {
+    if (!ctx) return PARGO_ERR_INVALID_ARG;
+    ctx->err.clear();
+    if (count < 0 || (count > 0 && !dems) || cap < 0) return fail(ctx, PARGO_ERR_INVALID_ARG, "batch queue: bad args");
+    const pargo_batch_opts o = batch_defaults(opts);
+    pargo_status st;
+    if ((st = check_batch_opts(ctx, o)) != PARGO_OK) return st;
+    for (int i = 0; i < count; i++) {
+        if ((st = check_raster(ctx, &dems[i], "batch dem")) != PARGO_OK) return st;
+        if ((st = check_dims(ctx, &dems[i])) != PARGO_OK) return st;
+        if (dems[i].dtype != PARGO_F32 || dems[i].location != PARGO_DEVICE)
+            return fail(ctx, PARGO_ERR_INVALID_ARG, "batch dem %d: must be F32 on the device", i);
+    }
+    std::vector<int> korder(count);
+    for (int i = 0; i < count; i++) korder[i] = i;
+    std::stable_sort(korder.begin(), korder.end(), [&](int a, int b) {
+        return dems[a].rows * dems[a].cols > dems[b].rows * dems[b].cols;
+    });
+    std::vector<int64_t> seg_start(count + 1);
+    std::vector<int> nstrips(count);
+    int64_t nsegs = 0;
+    for (int k = 0; k < count; k++) {
+        seg_start[k] = nsegs;
+        nsegs += batch_strip_segments(dems[korder[k]].rows, dems[korder[k]].cols, &nstrips[k]);
+    }
+    seg_start[count] = nsegs;
+    if (n_out) *n_out = nsegs;
+    cudaStream_t s = (cudaStream_t)stream;
+    CU(ctx, cudaSetDevice(ctx->device));
+    std::vector<uint64_t> q;
+    std::vector<double> ld;
+    if (o.order == PARGO_BATCH_BY_INTENSITY && count > 0) {
+        if ((st = batch_intensity_queue(ctx, count, dems, korder, seg_start, nstrips, nsegs, o, s, &q, &ld)) !=
+            PARGO_OK)
+            return st;
+    } else {
+        for (int k = 0; k < count; k++)
+            for (int64_t l = 0; l < seg_start[k + 1] - seg_start[k]; l++) q.push_back(((uint64_t)k << 40) | l);
+        ld.assign(q.size(), 0.0);
+    }
+    for (int64_t i = 0; i < std::min<int64_t>(cap, nsegs); i++) {
+        const int k = (int)(q[i] >> 40);
+        if (raster) raster[i] = korder[k];
+        if (segment) segment[i] = (int64_t)(q[i] & ((1ULL << 40) - 1));
+        if (load) load[i] = ld[i];
+    }
+    return PARGO_OK;
+}
+
+pargo_status pargo_batch_slope_d8_ex(pargo_ctx* ctx, int count, const pargo_raster* dems, pargo_raster* slopes,
+                                     pargo_raster* d8s, const pargo_nbr* nbr, int method, int units, int dir_type,
+                                     const pargo_batch_opts* opts, void* stream) {
     if (!ctx) return PARGO_ERR_INVALID_ARG;
     ctx->err.clear();
     if (count < 0 || (count > 0 && !dems)) return fail(ctx, PARGO_ERR_INVALID_ARG, "batch: bad count or dems");
     if (!slopes && !d8s) return fail(ctx, PARGO_ERR_INVALID_ARG, "batch: no output requested");
     if (count == 0) return PARGO_OK;
     pargo_status st;
+    const pargo_batch_opts bo = batch_defaults(opts);
+    if ((st = check_batch_opts(ctx, bo)) != PARGO_OK) return st;
     if ((st = check_nbr(ctx, nbr)) != PARGO_OK) return st;
     if (slopes && (method < 0 || method > 6)) return fail(ctx, PARGO_ERR_INVALID_ARG, "unknown slope method %d", method);
     bool all_tma = true;
@@ -1579,6 +1853,7 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
     // Device tables (cached while the batch description is unchanged).
     std::string key((const char*)params.data(), params.size() * sizeof(FocalParams));
     key.append((const char*)dems, (size_t)count * sizeof(pargo_raster));
+    key.append((const char*)&bo, sizeof(bo));
     cudaError_t e;
     CUtensorMap* dmaps = (CUtensorMap*)slot(ctx, kSlotBatchMaps, (size_t)count * sizeof(CUtensorMap), &e);
     FocalParams* dparams = (FocalParams*)slot(ctx, kSlotBatchParams, (size_t)count * sizeof(FocalParams), &e);
@@ -1613,6 +1888,22 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
             CU(ctx, cudaMemcpy(dsmaps, smaps.data(), smaps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
             CU(ctx, cudaMemcpy(dseg, seg_start.data(), (count + 1) * 8, cudaMemcpyHostToDevice));
             CU(ctx, cudaMemcpy(dns, nstrips.data(), count * sizeof(int), cudaMemcpyHostToDevice));
+            // The queue: segments by compute intensity, heaviest first.  The
+            // estimate is taken when a batch description is first seen and is
+            // kept with the other tables; it orders the work only, so the
+            // outputs never depend on it.
+            ctx->batch_ordered = false;
+            if (bo.order == PARGO_BATCH_BY_INTENSITY) {
+                std::vector<uint64_t> q;
+                std::vector<double> ld;
+                if ((st = batch_intensity_queue(ctx, count, dems, order, seg_start, nstrips, nsegs, bo, s, &q, &ld)) !=
+                    PARGO_OK)
+                    return st;
+                uint64_t* dq = (uint64_t*)slot(ctx, kSlotBatchOrder, (size_t)nsegs * 8, &e);
+                if (!dq) return cuda_fail(ctx, e, "batch queue");
+                CU(ctx, cudaMemcpy(dq, q.data(), (size_t)nsegs * 8, cudaMemcpyHostToDevice));
+                ctx->batch_ordered = true;
+            }
         }
         std::vector<CUtensorMap> maps(all_tma ? count : 0);
         if (all_tma)
@@ -1630,7 +1921,9 @@ pargo_status pargo_batch_slope_d8(pargo_ctx* ctx, int count, const pargo_raster*
     }
     CU(ctx, cudaMemsetAsync(&ctx->d_counters[0], 0, sizeof(unsigned long long), s));
     if (strip)
-        CU(ctx, launch_batch_strip(dsmaps, dparams, ddems, dseg, dns, count, nsegs, slopes ? 1 : 0, d8s ? 1 : 0,
+        CU(ctx, launch_batch_strip(dsmaps, dparams, ddems, dseg, dns,
+                                   ctx->batch_ordered ? (const uint64_t*)ctx->slots[kSlotBatchOrder].p : nullptr,
+                                   count, nsegs, slopes ? 1 : 0, d8s ? 1 : 0,
                                    &ctx->d_counters[4], dslow, &ctx->d_counters[0], ctx->d_error, ctx->num_sms, s));
     else if (all_tma)
         CU(ctx, launch_batch_tma(dmaps, dparams, dstart, dntx, count, total, slopes ? 1 : 0, d8s ? 1 : 0, claim,

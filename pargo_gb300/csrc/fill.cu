@@ -556,7 +556,80 @@ __global__ void fill_finish_kernel(const FillParams p, const OutView out, unsign
     if (raised && (threadIdx.x & 31) == 0 && cnt) atomicAdd(raised, cnt);
 }
 
+// ---- batched form: many rasters packed into one mosaic ------------------
+// Every raster of a batch is copied into its own rectangle of one mosaic
+// DEM; the raster's ring and its nodata cells become the mosaic's nodata, as
+// does every mosaic cell outside the rasters.  A ring cell's level is nodata
+// in the reference (rasterLayer copyLayerInfo) whatever its DEM value, so two
+// rasters side by side meet at two rows (or columns) of nodata levels: no
+// level of one is ever a neighbour of a level of the other, and the mosaic's
+// fixpoint is every raster's own fixpoint.  One persistent relaxation then
+// serves the whole batch.
+
+__global__ void fill_mosaic_clear_kernel(void* mosaic, int64_t n, int f64, double nd) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (f64) reinterpret_cast<double*>(mosaic)[i] = nd;
+        else reinterpret_cast<float*>(mosaic)[i] = (float)nd;
+    }
+}
+
+// blockIdx.y = raster; the block's threads stride over the raster's cells.
+__global__ void fill_mosaic_pack_kernel(const FillBatchItem* items, void* mosaic, int64_t mstride, int f64, double nd) {
+    const FillBatchItem it = items[blockIdx.y];
+    const int64_t n = it.rows * it.cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / it.cols, c = i - r * it.cols;
+        const char* row = reinterpret_cast<const char*>(it.dem) + r * it.pitch;
+        const bool ring = r == 0 || c == 0 || r == it.rows - 1 || c == it.cols - 1;
+        const int64_t m = (it.oy + r) * mstride + it.ox + c;
+        if (f64) {
+            const double z = reinterpret_cast<const double*>(row)[c];
+            reinterpret_cast<double*>(mosaic)[m] = (ring || it.nd6d.has(z)) ? nd : z;
+        } else {
+            const float z = reinterpret_cast<const float*>(row)[c];
+            reinterpret_cast<float*>(mosaic)[m] = (ring || it.nd6f.has(z)) ? (float)nd : z;
+        }
+    }
+}
+
+// The levels of each raster's rectangle into its own output (nodata levels:
+// the output's nodata), and the count of raised cells over the batch.
+__global__ void fill_mosaic_finish_kernel(const FillParams p, const FillBatchItem* items, unsigned long long* raised) {
+    const FillBatchItem it = items[blockIdx.y];
+    const int64_t n = it.rows * it.cols;
+    unsigned long long cnt = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / it.cols, c = i - r * it.cols;
+        const double w = p.w[(it.oy + r) * p.w_stride + it.ox + c];
+        const bool nd = isinf(w);
+        if (!nd && w > dem_at(p, it.oy + r, it.ox + c)) cnt++;
+        put_value(it.out, r, c, nd ? it.out.nodata : w);
+    }
+    cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
+    if (raised && (threadIdx.x & 31) == 0 && cnt) atomicAdd(raised, cnt);
+}
+
 }  // namespace
+
+cudaError_t fill_mosaic_pack(const FillBatchItem* items, int count, int64_t max_cells, void* mosaic, int64_t mrows,
+                             int64_t mstride, int f64, double nd, cudaStream_t st) {
+    const int64_t n = mrows * mstride;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 8192) blocks = 8192;
+    fill_mosaic_clear_kernel<<<(unsigned)blocks, 256, 0, st>>>(mosaic, n, f64, nd);
+    int64_t bx = (max_cells + 255) / 256;
+    if (bx > 64) bx = 64;
+    fill_mosaic_pack_kernel<<<dim3((unsigned)bx, (unsigned)count), 256, 0, st>>>(items, mosaic, mstride, f64, nd);
+    return cudaGetLastError();
+}
+
+cudaError_t fill_mosaic_finish(const FillParams& p, const FillBatchItem* items, int count, int64_t max_cells,
+                               unsigned long long* raised, cudaStream_t st) {
+    int64_t bx = (max_cells + 255) / 256;
+    if (bx > 64) bx = 64;
+    fill_mosaic_finish_kernel<<<dim3((unsigned)bx, (unsigned)count), 256, 0, st>>>(p, items, raised);
+    return cudaGetLastError();
+}
 
 int fill_tile_rows() { return kT; }
 int fill_tile_cols() { return kT; }

@@ -905,6 +905,7 @@ struct BatchStripTables {
     const InView* dems;
     const int64_t* seg_start;  // count + 1
     const int* nstrips;
+    const uint64_t* order;     // queue position -> raster << 40 | segment of the raster; null: raster by raster
     int count;
     int64_t nsegs;
     unsigned long long* claim;
@@ -948,12 +949,21 @@ __global__ void __launch_bounds__(kSWarps * 32, 5) batch_strip_kernel(const Batc
         int x0, y0, item, rows;
     };
     auto origin = [&](int64_t g) {
-        int lo = 0, hi = t.count - 1;  // the last raster whose first segment is <= g
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (t.seg_start[mid] <= g) lo = mid; else hi = mid - 1;
+        int lo = 0;
+        uint32_t local;
+        if (t.order) {  // the queue ordered by the segments' compute intensity
+            const uint64_t v = t.order[g];
+            lo = (int)(v >> 40);
+            local = (uint32_t)(v & ((1ULL << 40) - 1));
+        } else {
+            int hi = t.count - 1;  // the last raster whose first segment is <= g
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (t.seg_start[mid] <= g) lo = mid; else hi = mid - 1;
+            }
+            local = (uint32_t)(g - t.seg_start[lo]);
         }
-        const uint32_t local = (uint32_t)(g - t.seg_start[lo]), ns = (uint32_t)t.nstrips[lo];
+        const uint32_t ns = (uint32_t)t.nstrips[lo];
         return Origin{(int)((local % ns) * kTW), (int)((local / ns) * kSegRows), lo, (int)t.params[lo].rows};
     };
     auto issue_prime = [&](const Origin& o, int buf) {
@@ -1283,6 +1293,51 @@ cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params,
     return cudaGetLastError();
 }
 
+// Compute intensity of the batch's strip segments (a kTW-column strip by
+// kSegRows rows of one raster): the intensity-ratio estimate of the load
+// estimator (gpro/transformation.h:155-197: valid_load per cell whose
+// |v - nodata| > Eps, nodata_load per other cell), here counted per segment.
+// One warp per segment, 4 columns per lane; out[g] = the valid cells of
+// segment g (the host turns counts into loads and orders the queue).
+__global__ void __launch_bounds__(256) batch_segment_valid_kernel(const SegLoadRaster* rs, int count, int64_t nsegs,
+                                                                  uint32_t* out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t g = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); g < nsegs; g += warps) {
+        int lo = 0, hi = count - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (rs[mid].seg_start <= g) lo = mid; else hi = mid - 1;
+        }
+        const SegLoadRaster r = rs[lo];
+        const int64_t local = g - r.seg_start;
+        const int64_t x0 = (local % r.nstrips) * kTW, y0 = (local / r.nstrips) * kSegRows;
+        const int64_t y1 = min(y0 + kSegRows, r.rows);
+        const int64_t xa = x0 + 4 * lane;
+        uint32_t valid = 0;
+        for (int64_t y = y0; y < y1; y++) {
+            const float* row = reinterpret_cast<const float*>(r.dem.base + y * r.dem.pitch);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                if (xa + j < r.cols) valid += r.nd.has(row[xa + j]) ? 0u : 1u;
+        }
+        valid = __reduce_add_sync(0xffffffffu, valid);
+        if (lane == 0) out[g] = valid;
+    }
+}
+
+cudaError_t launch_batch_segment_valid(const SegLoadRaster* rs, int count, int64_t nsegs, uint32_t* out, int num_sms,
+                                       cudaStream_t s) {
+    if (nsegs == 0) return cudaSuccess;
+    int64_t blocks = (nsegs + 7) / 8;
+    if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
+    batch_segment_valid_kernel<<<(unsigned)blocks, 256, 0, s>>>(rs, count, nsegs, out);
+    return cudaGetLastError();
+}
+
+int batch_strip_segment_rows() { return kSegRows; }
+int batch_strip_segment_cols() { return kTW; }
+
 // Batched strip walk over `count` rasters: maps[2k] / maps[2k+1] are raster
 // k's stage (kBoxW x focal_strip_stage_rows()) and priming (kBoxW x 2) tensor
 // maps; seg_start[k] its first segment (batch_strip_segments() per raster);
@@ -1294,12 +1349,13 @@ int64_t batch_strip_segments(int64_t rows, int64_t cols, int* nstrips) {
 }
 
 cudaError_t launch_batch_strip(const CUtensorMap* maps, const FocalParams* params, const InView* dems,
-                               const int64_t* seg_start, const int* nstrips, int count, int64_t nsegs, int do_slope,
-                               int do_d8, unsigned long long* counters, uint64_t* slow_items,
-                               unsigned long long* fallbacks, int* error_flag, int num_sms, cudaStream_t s) {
+                               const int64_t* seg_start, const int* nstrips, const uint64_t* order, int count,
+                               int64_t nsegs, int do_slope, int do_d8, unsigned long long* counters,
+                               uint64_t* slow_items, unsigned long long* fallbacks, int* error_flag, int num_sms,
+                               cudaStream_t s) {
     if (nsegs == 0) return cudaSuccess;
-    const BatchStripTables t{maps, params, dems, seg_start, nstrips, count, nsegs, counters, counters + 1, slow_items,
-                             error_flag};
+    const BatchStripTables t{maps, params, dems, seg_start, nstrips, order, count, nsegs, counters, counters + 1,
+                             slow_items, error_flag};
     const size_t smem = (size_t)kSWarps * kSWarpBytes;
     auto kern = do_slope ? (do_d8 ? batch_strip_kernel<true, true> : batch_strip_kernel<true, false>)
                          : batch_strip_kernel<false, true>;

@@ -76,10 +76,23 @@ cudaError_t launch_batch_tma(const CUtensorMap* maps, const FocalParams* params,
                              unsigned long long* claim, unsigned long long* fallbacks, int* error_flag, int num_sms,
                              cudaStream_t s);
 int64_t batch_strip_segments(int64_t rows, int64_t cols, int* nstrips);
+int batch_strip_segment_rows();
+int batch_strip_segment_cols();
 cudaError_t launch_batch_strip(const CUtensorMap* maps, const FocalParams* params, const InView* dems,
-                               const int64_t* seg_start, const int* nstrips, int count, int64_t nsegs, int do_slope,
-                               int do_d8, unsigned long long* counters, uint64_t* slow_items,
-                               unsigned long long* fallbacks, int* error_flag, int num_sms, cudaStream_t s);
+                               const int64_t* seg_start, const int* nstrips, const uint64_t* order, int count,
+                               int64_t nsegs, int do_slope, int do_d8, unsigned long long* counters,
+                               uint64_t* slow_items, unsigned long long* fallbacks, int* error_flag, int num_sms,
+                               cudaStream_t s);
+// One raster of a batch, for the segments' compute-intensity count.
+struct SegLoadRaster {
+    InView dem;             // float32
+    int64_t rows, cols;
+    Band<float> nd;         // |v - nodata| <= Eps 1e-7: a nodata cell of the intensity estimate
+    int64_t seg_start;      // its first segment
+    int nstrips;
+};
+cudaError_t launch_batch_segment_valid(const SegLoadRaster* rs, int count, int64_t nsegs, uint32_t* out, int num_sms,
+                                       cudaStream_t s);
 cudaError_t launch_batch_generic(const FocalParams* params, const InView* dems, const int64_t* cell_start, int count,
                                  int64_t total_cells, unsigned long long* fallbacks, int num_sms, cudaStream_t s);
 
@@ -137,6 +150,20 @@ cudaError_t fill_init(const FillParams& p, const FillScratch& s, cudaStream_t st
 cudaError_t fill_round(const FillParams& p, const FillScratch& s, int parity, int num_sms, cudaStream_t st);
 cudaError_t fill_persistent(const FillParams& p, const FillScratch& s, long long patience, int num_sms, cudaStream_t st);
 cudaError_t fill_finish(const FillParams& p, const OutView& out, unsigned long long* raised, cudaStream_t st);
+// Batched fill: each raster's place in one mosaic DEM, and its output.
+struct FillBatchItem {
+    const void* dem;        // the raster's DEM (float32, or float64 for a float64 batch)
+    int64_t pitch;          // bytes
+    int64_t rows, cols;
+    int64_t oy, ox;         // its cell (0, 0) in the mosaic
+    Band<float> nd6f;       // its own nodata band (Eps 1e-6)
+    Band<double> nd6d;
+    OutView out;            // its filled output
+};
+cudaError_t fill_mosaic_pack(const FillBatchItem* items, int count, int64_t max_cells, void* mosaic, int64_t mrows,
+                             int64_t mstride, int f64, double nd, cudaStream_t st);
+cudaError_t fill_mosaic_finish(const FillParams& p, const FillBatchItem* items, int count, int64_t max_cells,
+                               unsigned long long* raised, cudaStream_t st);
 int fill_tile_rows();
 int fill_tile_cols();
 

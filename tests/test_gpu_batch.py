@@ -67,3 +67,57 @@ def test_batch_strip_walk_with_nodata_and_edge_sizes(outputs, ctx, oracle_lib):
             assert ok, (k, mx)
         if want_c:
             assert bits_equal(d8_as_f64(host(bc[k]), -128), oracle_lib.d8(dem, -9999.0)), k
+
+
+def _np_queue(dems, nodata_load, valid_load, seg_rows=48, seg_cols=128):
+    """The queue by intensity, restated: segments numbered raster by raster
+    (largest raster first), loads counted with |v - nodata| > 1e-7 as valid,
+    then a stable sort heaviest first."""
+    korder = sorted(range(len(dems)), key=lambda i: -dems[i].size)
+    items = []
+    for k in korder:
+        d = dems[k].astype(np.float64)
+        valid = np.abs(d - (-9999.0)) > 1e-7
+        R, C = d.shape
+        ns = (C + seg_cols - 1) // seg_cols
+        nb = (R + seg_rows - 1) // seg_rows
+        for l in range(ns * nb):
+            x0, y0 = (l % ns) * seg_cols, (l // ns) * seg_rows
+            v = valid[y0:y0 + seg_rows, x0:x0 + seg_cols]
+            items.append((k, l, float(v.sum()) * valid_load + float(v.size - v.sum()) * nodata_load))
+    order = sorted(range(len(items)), key=lambda i: -items[i][2])   # Python's sort is stable
+    return [items[i] for i in order]
+
+
+@pytest.mark.parametrize("loads", [(0.0, 1.0), (3.0, 1.0)])
+def test_batch_queue_by_intensity_matches_restatement(loads, ctx):
+    """The device-counted segment loads and the queue order equal a numpy
+    restatement of the intensity-ratio estimate on DEMs with nodata blobs."""
+    shapes = [(300, 700), (97, 130), (1024, 129), (48, 128), (49, 257), (500, 500)]
+    dems = [synth.hydro_dem(r, c, seed=400 + k, blob_fraction=0.15) for k, (r, c) in enumerate(shapes)]
+    dd = [dev(d, 16) for d in dems]
+    ras, seg, ld = ctx.batch_queue([abi.raster(d, -9999.0) for d in dd], nodata_load=loads[0], valid_load=loads[1])
+    want = _np_queue(dems, *loads)
+    assert len(ras) == len(want)
+    assert np.array_equal(ld, np.array([w[2] for w in want]))
+    assert np.array_equal(ras, np.array([w[0] for w in want]))
+    assert np.array_equal(seg, np.array([w[1] for w in want]))
+    assert (np.diff(ld) <= 0).all()
+    r2, s2, l2 = ctx.batch_queue([abi.raster(d, -9999.0) for d in dd], order=abi.BATCH_BY_SIZE)
+    korder = sorted(range(len(dems)), key=lambda i: -dems[i].size)
+    assert list(dict.fromkeys(r2.tolist())) == korder       # raster by raster, largest first
+
+
+@pytest.mark.parametrize("order,loads", [(0, (0.0, 1.0)), (0, (5.0, 1.0)), (1, (0.0, 1.0))])
+def test_batch_outputs_do_not_depend_on_the_queue_order(order, loads, ctx, oracle_lib):
+    shapes = _batch(14, 500, 0.1)
+    dems = [synth.hydro_dem(r, c, seed=s, blob_fraction=0.12) for (s, r, c, h) in shapes]
+    dd = [dev(d, 16) for d in dems]
+    bs = [empty_dev(d.shape, np.float32, 16) for d in dems]
+    bc = [empty_dev(d.shape, np.int8, 16) for d in dems]
+    ctx.batch_slope_d8([abi.raster(d, -9999.0, 30.0) for d in dd], [abi.raster(s, -9999.0) for s in bs],
+                       [abi.raster(c, -128) for c in bc], order=order, nodata_load=loads[0], valid_load=loads[1])
+    for k, dem in enumerate(dems):
+        ok, mx, _ = slope_close(host(bs[k]), oracle_lib.slope(dem, -9999.0, 30.0))
+        assert ok, (k, mx)
+        assert bits_equal(d8_as_f64(host(bc[k]), -128), oracle_lib.d8(dem, -9999.0)), k
