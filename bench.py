@@ -371,7 +371,9 @@ def run_slope(args, ws, rank, local, side):
                      # DRAM read + write of one launch, scaled by cells from the 8192^2 ncu capture of the
                      # same kernel (the traffic grows with the cell count)
                      "traffic": round((STRIP_DRAM_BYTES_PER_CELL if strip else FOCAL_DRAM_BYTES_PER_CELL) * cells),
-                     "traffic_source": "ncu 8192^2 capture scaled per cell", "variant": best, "variant_ms": tune_ms},
+                     "traffic_source": "ncu 8192^2 capture scaled per cell",
+                     "variant": abi.focal_variant_names()[int(forced) if forced else best],
+                     "variant_ms": dict(zip(abi.focal_variant_names(), tune_ms))},
         # the strip walk is a walk launch and a fix-up launch per step; the tiled kernel one
         "gpu_launches": args.steps * (2 if strip else 1), "clocks": clk,
     }

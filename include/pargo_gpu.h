@@ -148,15 +148,33 @@ pargo_status pargo_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* d8,
 pargo_status pargo_slope_d8(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* slope, pargo_raster* d8,
                             const pargo_nbr* nbr, int method, int units, int dir_type, void* stream);
 
-/* Autotuner of the fused slope+D8 kernel: times each tile-shape / occupancy
- * variant `reps` times on `dem` (an F32 device raster with 16-byte aligned
- * rows), keeps the fastest for rasters of the same size class (power of two of
- * the cell count) in this context, and reports it in *best and the per-variant
- * milliseconds in times_ms[0 .. max_times-1] (either may be NULL).  The
- * environment variable PARGO_FOCAL_VARIANT, when set, overrides the choice.
- * No reference counterpart. */
+/* Autotuner of the fused slope+D8 kernel (no reference counterpart).  It times
+ * each kernel variant `reps` times on `dem` (an F32 device raster with
+ * 16-byte aligned rows) and keeps the fastest for rasters of the same size
+ * class (power of two of the cell count).  The variants span the tiled
+ * kernel's tile rows (cells per thread) and CTAs per SM, and the strip
+ * walk's rows per TMA stage, stages per segment (segment height) and CTAs
+ * per SM; the halo every variant loads is the stencil's MBR
+ * (gpro/neighborhood.h:423-467: one cell for the 3x3 window).  *best gets the
+ * chosen variant and times_ms[0 .. max_times-1] the per-variant milliseconds
+ * (either may be NULL).  The choice is kept in the context and persisted in a
+ * JSON cache keyed by (operation, device, size class) that pargo_create
+ * reads, so later contexts -- an application's main, say -- run the tuned
+ * kernel: the file is $PARGO_TUNE_CACHE (set but empty: no cache), else
+ * $XDG_CACHE_HOME/pargo_gb300/tune.json, else ~/.cache/pargo_gb300/tune.json.
+ * PARGO_FOCAL_VARIANT in the environment overrides every choice.  Every
+ * variant computes the same bytes. */
 pargo_status pargo_tune_focal(pargo_ctx* ctx, const pargo_raster* dem, int reps, int* best, float* times_ms,
                               int max_times);
+
+/* The focal kernel variants: their number, the name of variant v ("tile-r32-b5":
+ * 32-row tiles at 5 CTAs per SM; "strip-s6x8-b5": 6-row stages, 8 stages per
+ * segment, 5 CTAs per SM; NULL when v is out of range), and the variant a
+ * context runs for a fused slope + D8 of `cells` cells (PARGO_FOCAL_VARIANT,
+ * else the tuned or cached choice for the size class, else the size default). */
+int pargo_focal_num_variants(void);
+const char* pargo_focal_variant_name(int v);
+int pargo_focal_variant(const pargo_ctx* ctx, int64_t cells);
 
 /* Planchon-Darboux pit removal: the fixpoint the reference's Gauss-Seidel
  * sweeps reach (any visiting order reaches the same one).  dem: F32 or F64;
@@ -264,20 +282,21 @@ pargo_status pargo_load_decompose(pargo_ctx* ctx, const pargo_raster* load, int 
 /* Batched fused slope + D8 over `count` independent rasters in one persistent
  * launch; slopes / d8s may be NULL (no such output) and all rasters must be on
  * the device.  The launch's warps claim work items -- 128-column by 48-row
- * segments of every raster -- from one device queue.  The queue is ordered
- * heaviest first by the load estimator's intensity-ratio estimate
+ * segments of every raster -- from one device queue.  The queue holds the
+ * rasters heaviest first by the load estimator's intensity-ratio estimate
  * (Transformation::Operator, gpro/transformation.h:155-197: valid_load per
- * cell with |v - nodata| > 1e-7, nodata_load per other cell), counted per
- * segment on the device the first time a batch description (buffers, shapes,
- * options) is seen and kept with the batch's other device tables; the order
- * balances the work only and never changes an output.  pargo_batch_slope_d8
+ * cell with |v - nodata| > 1e-7, nodata_load per other cell), each raster's
+ * segments together; the estimate is counted per segment on the device the
+ * first time a batch description (buffers, shapes, options) is seen and kept
+ * with the batch's other device tables.  The order balances the work only and
+ * never changes an output.  pargo_batch_slope_d8
  * uses the defaults: by intensity, nodata_load 0, valid_load 1 (the
  * reference's "-nodataLoad 0 -validLoad 1", apps/spatial/reclassify/
  * pRelclassify.cpp:22).  Configurations outside the strip walk (slope methods
  * other than Horn, degrees, dirType 256, unaligned rows) run a tiled launch
  * whose queue is ordered by raster size. */
 typedef enum pargo_batch_order {
-    PARGO_BATCH_BY_INTENSITY = 0, /* segments by estimated load, heaviest first */
+    PARGO_BATCH_BY_INTENSITY = 0, /* rasters by estimated load, heaviest first */
     PARGO_BATCH_BY_SIZE = 1       /* raster by raster, largest raster first */
 } pargo_batch_order;
 

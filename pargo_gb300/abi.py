@@ -105,6 +105,11 @@ def lib():
         L.pargo_sca_noalloc.restype = st
         L.pargo_tune_focal.argtypes = [vp, R, i, P(i), P(ctypes.c_float), i]
         L.pargo_tune_focal.restype = st
+        L.pargo_focal_num_variants.restype = i
+        L.pargo_focal_variant_name.argtypes = [i]
+        L.pargo_focal_variant_name.restype = ctypes.c_char_p
+        L.pargo_focal_variant.argtypes = [vp, ctypes.c_int64]
+        L.pargo_focal_variant.restype = i
         L.pargo_last_d8_fallbacks.argtypes = [vp]
         L.pargo_last_d8_fallbacks.restype = ctypes.c_int64
         for name in ("pargo_create", "pargo_destroy", "pargo_nbr_parse", "pargo_slope", "pargo_d8", "pargo_slope_d8",
@@ -117,6 +122,12 @@ def lib():
             getattr(L, name).restype = st
         _lib = L
     return _lib
+
+
+def focal_variant_names():
+    """Names of the fused slope+D8 kernel variants, by index."""
+    L = lib()
+    return [L.pargo_focal_variant_name(v).decode() for v in range(L.pargo_focal_num_variants())]
 
 
 def compute_load_dims(rows, cols, grain):
@@ -214,9 +225,14 @@ class Context:
     def tune_focal(self, dem, reps=5):
         """Autotune the fused slope+D8 kernel on a device DEM; returns (best, ms per variant)."""
         best = ctypes.c_int(0)
-        times = (ctypes.c_float * 16)()
-        self._check(lib().pargo_tune_focal(self._p, ctypes.byref(dem), reps, ctypes.byref(best), times, 16))
-        return best.value, [round(t, 4) for t in times if t > 0]
+        n = lib().pargo_focal_num_variants()
+        times = (ctypes.c_float * n)()
+        self._check(lib().pargo_tune_focal(self._p, ctypes.byref(dem), reps, ctypes.byref(best), times, n))
+        return best.value, [round(t, 4) for t in times]
+
+    def focal_variant(self, cells):
+        """The kernel variant this context runs for a fused slope + D8 of `cells` cells."""
+        return lib().pargo_focal_variant(self._p, cells)
 
     def slope(self, dem, slope, method=SLOPE_FD, units=RATIO, nbr=None, stream=None):
         self._check(lib().pargo_slope(self._p, ctypes.byref(dem), ctypes.byref(slope), self._nbr(nbr), method, units,

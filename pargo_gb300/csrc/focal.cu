@@ -548,14 +548,32 @@ __global__ void __launch_bounds__(256) batch_generic_kernel(const FocalParams* p
 // general path often (the raster's left and right edges) do not stretch the
 // launch.  The row loop is unrolled by three with the registers' roles
 // rotated (above / centre / below), so no register is copied from row to row.
-constexpr int kSR = 6;                                      // rows per stage (a multiple of 3)
-constexpr int kSegStages = 8;                               // stages per segment
-constexpr int kSegRows = kSR * kSegStages;                  // output rows per segment
-constexpr int kSStageBytes = kBoxW * kSR * 4;               // 3264
-constexpr int kSStageStride = (kSStageBytes + 127) / 128 * 128;
-constexpr int kSPrimeBytes = kBoxW * 2 * 4;                 // 1088
-constexpr int kSPrimeStride = (kSPrimeBytes + 127) / 128 * 128;
-constexpr int kSWarpBytes = 2 * kSStageStride + 2 * kSPrimeStride;
+// Strip geometry, a tuning parameter: SR rows per TMA stage (a multiple of 3:
+// the row loop rotates three register roles; at most 32: one bit per row of
+// a stage), STAGES stages per segment.
+template <int SR_, int STAGES_>
+struct StripGeom {
+    static_assert(SR_ % 3 == 0 && SR_ <= 30 && STAGES_ >= 2, "strip geometry");
+    static constexpr int kSR = SR_;                                   // rows per stage
+    static constexpr int kStages = STAGES_;                           // stages per segment
+    static constexpr int kSegRows = SR_ * STAGES_;                    // output rows per segment
+    static constexpr int kStageBytes = kBoxW * SR_ * 4;
+    static constexpr int kStageStride = (kStageBytes + 127) / 128 * 128;
+    static constexpr int kPrimeBytes = kBoxW * 2 * 4;                 // 1088
+    static constexpr int kPrimeStride = (kPrimeBytes + 127) / 128 * 128;
+    static constexpr int kWarpBytes = 2 * kStageStride + 2 * kPrimeStride;
+};
+// The batched walk's geometry (and the single walk's default): 6-row stages,
+// 8 stages, 48-row segments.
+using StripDefault = StripGeom<6, 8>;
+constexpr int kSR = StripDefault::kSR;
+constexpr int kSegStages = StripDefault::kStages;
+constexpr int kSegRows = StripDefault::kSegRows;
+constexpr int kSStageBytes = StripDefault::kStageBytes;  // 3264
+constexpr int kSStageStride = StripDefault::kStageStride;
+constexpr int kSPrimeBytes = StripDefault::kPrimeBytes;
+constexpr int kSPrimeStride = StripDefault::kPrimeStride;
+constexpr int kSWarpBytes = StripDefault::kWarpBytes;
 constexpr int kSWarps = 4;
 
 __device__ __forceinline__ float fmax3f(float a, float b, float c) {
@@ -719,9 +737,10 @@ __device__ __noinline__ void strip_flush(uint32_t pend, int y_last, int64_t gx0,
 // hold a value in the nodata band.  A band below zero (the usual negative
 // nodata) needs only the minimum: a stage with values below the band is
 // flagged too, which only sends it through the per-row tests.
+template <int SR = kSR>
 __device__ __forceinline__ bool stage_lane_maybe_nodata(const float* st, const Band<float>& b) {
     const float4* s4 = reinterpret_cast<const float4*>(st);
-    constexpr int kQuads = kSR * kBoxW / 4;
+    constexpr int kQuads = SR * kBoxW / 4;
     float mn = INFINITY, mx = -INFINITY;
     if (b.hi < 0.0f) {
 #pragma unroll
@@ -746,18 +765,19 @@ __device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity) {
     return __all_sync(0xffffffffu, ok);
 }
 
-template <bool SLOPE, bool D8, int MINB>
+template <bool SLOPE, bool D8, int MINB, int SR, int STAGES>
 __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const __grid_constant__ CUtensorMap map_stage,
                                                                        const __grid_constant__ CUtensorMap map_prime,
                                                                        const __grid_constant__ FocalParams p,
                                                                        int64_t nstrips, int64_t nsegs,
                                                                        unsigned long long* claim, SlowList slow) {
+    using G = StripGeom<SR, STAGES>;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t bars[kSWarps][4];  // stage 0, stage 1, prime 0, prime 1
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    unsigned char* wbase = smem + warp * kSWarpBytes;
-    auto stage = [&](int b) { return reinterpret_cast<float*>(wbase + b * kSStageStride); };
-    auto prime = [&](int b) { return reinterpret_cast<float*>(wbase + 2 * kSStageStride + b * kSPrimeStride); };
+    unsigned char* wbase = smem + warp * G::kWarpBytes;
+    auto stage = [&](int b) { return reinterpret_cast<float*>(wbase + b * G::kStageStride); };
+    auto prime = [&](int b) { return reinterpret_cast<float*>(wbase + 2 * G::kStageStride + b * G::kPrimeStride); };
     uint64_t* bar = bars[warp];
     if (lane == 0) {
         tma_prefetch_desc(&map_stage);
@@ -780,20 +800,20 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
     const uint32_t ns32 = (uint32_t)nstrips;
     auto origin = [&](int64_t seg) {
         const uint32_t sg = (uint32_t)seg;
-        return Origin{(int)((sg % ns32) * kTW), (int)((sg / ns32) * kSegRows)};
+        return Origin{(int)((sg % ns32) * kTW), (int)((sg / ns32) * G::kSegRows)};
     };
     auto issue_prime = [&](const Origin& o, int buf) {
         if (lane == 0) {
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bar[2 + buf], kSPrimeBytes);
+            mbar_arrive_expect_tx(&bar[2 + buf], G::kPrimeBytes);
             tma_load_2d(prime(buf), &map_prime, o.x0 - 4, o.y0 - 1, &bar[2 + buf]);
         }
     };
     auto issue_stage = [&](const Origin& o, int k, int buf) {
         if (lane == 0) {
-            const int yb = min(o.y0 + 1 + k * kSR, (int)box_y_max);  // rows past the raster: never stored
+            const int yb = min(o.y0 + 1 + k * G::kSR, (int)box_y_max);  // rows past the raster: never stored
             fence_proxy_async_smem();
-            mbar_arrive_expect_tx(&bar[buf], kSStageBytes);
+            mbar_arrive_expect_tx(&bar[buf], G::kStageBytes);
             tma_load_2d(stage(buf), &map_stage, o.x0 - 4, yb, &bar[buf]);
         }
     };
@@ -829,7 +849,7 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
         s_load_row(prime(pb) + kBoxW, lane, B, p.nd6f);
         s_pair(A, B, PAB);
 #pragma unroll 1
-        for (int k = 0; k < kSegStages; k++) {
+        for (int k = 0; k < G::kStages; k++) {
             const int buf = k & 1;
             if (!warp_wait(&bar[buf], (sphase >> buf) & 1u)) {
                 if (lane == 0 && p.error_flag) atomicExch(p.error_flag, 1);
@@ -838,12 +858,12 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
             sphase ^= 1u << buf;
             const int64_t spp = SLOPE ? p.slope.pitch : 0, dpp = D8 ? p.d8.pitch : 0;
             uint32_t pend = 0;
-            const int ys = (int)y0 + k * kSR;
-            const bool inside = (ys >= 1) & (ys + kSR - 1 <= rows - 2);
+            const int ys = (int)y0 + k * G::kSR;
+            const bool inside = (ys >= 1) & (ys + G::kSR - 1 <= rows - 2);
             // one vote: the stage's values and the two rows above it
-            if (__any_sync(0xffffffffu, stage_lane_maybe_nodata(stage(buf), p.nd6f) | A.nd | B.nd) | !inside) {
+            if (__any_sync(0xffffffffu, stage_lane_maybe_nodata<SR>(stage(buf), p.nd6f) | A.nd | B.nd) | !inside) {
 #pragma unroll 1
-                for (int t = 0; t < kSR; t += 3) {
+                for (int t = 0; t < G::kSR; t += 3) {
                     const float* st = stage(buf) + t * kBoxW;
                     const int y = ys + t;
                     strip_step<SLOPE, D8, false>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
@@ -857,7 +877,7 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
                 }
             } else {  // inside the ring, no nodata in any row it reads: the rows skip the tests
 #pragma unroll 1
-                for (int t = 0; t < kSR; t += 3) {
+                for (int t = 0; t < G::kSR; t += 3) {
                     const float* st = stage(buf) + t * kBoxW;
                     const int y = ys + t;
                     strip_step<SLOPE, D8, true>(st, A, B, C, PAB, PBC, y, rows, gx0, lane_int, k_fd, p.nd6f, sp, dp,
@@ -870,20 +890,20 @@ __global__ void __launch_bounds__(kSWarps * 32, MINB) focal_strip_kernel(const _
                     dp += 3 * dpp;
                 }
             }
-            if (pend) strip_flush(pend, ys + kSR - 1, gx0, slow);
+            if (pend) strip_flush(pend, ys + G::kSR - 1, gx0, slow);
             __syncwarp();
             // refill this buffer with the item two ahead
-            if (k + 2 < kSegStages) {
+            if (k + 2 < G::kStages) {
                 issue_stage(co, k + 2, buf);
             } else {
-                if (k + 2 == kSegStages) {
+                if (k + 2 == G::kStages) {
                     nxt = claim_seg();
                     if (nxt < nsegs) {
                         no = origin(nxt);
                         issue_prime(no, pb ^ 1);
                     }
                 }
-                if (nxt < nsegs) issue_stage(no, k + 2 - kSegStages, buf);
+                if (nxt < nsegs) issue_stage(no, k + 2 - G::kStages, buf);
             }
         }
         if (nxt >= nsegs) break;
@@ -1150,18 +1170,40 @@ __global__ void __launch_bounds__(128) strip_fixup_kernel(const InView dem, cons
 
 }  // namespace
 
-// Kernel variants the autotuner chooses among (tile rows = 4 x ROWS).
+// Kernel variants the autotuner searches.  Tiled kernel: tile rows (4 x
+// ROWS; each thread computes ROWS rows of 4 cells, 4 x ROWS cells) and CTAs
+// per SM.  Strip walk: rows per TMA stage, stages per segment (the segment
+// height is their product) and CTAs per SM; the strip width is the warp's 32
+// lanes x 4 cells (one float4 per lane and row).  Every variant computes the
+// same bytes.  A variant is named for its parameters; the names key the
+// persisted tuning cache, so a rebuilt table still resolves a cached choice.
 struct Variant {
-    int rows, unroll, minb;
+    char kind;       // 't' tiled, 's' strip walk
+    int rows, stages, minb;
+    const char* name;
 };
-static const Variant kVariants[] = {{8, 1, 5}, {6, 1, 6}, {6, 1, 7}, {4, 1, 8}, {8, 1, 6}};
+static const Variant kVariants[] = {
+    {'t', 8, 0, 5, "tile-r32-b5"},     {'t', 6, 0, 6, "tile-r24-b6"},     {'t', 6, 0, 7, "tile-r24-b7"},
+    {'t', 4, 0, 8, "tile-r16-b8"},     {'t', 8, 0, 6, "tile-r32-b6"},     {'s', 6, 8, 5, "strip-s6x8-b5"},
+    {'s', 6, 8, 6, "strip-s6x8-b6"},   {'s', 3, 16, 5, "strip-s3x16-b5"}, {'s', 6, 4, 5, "strip-s6x4-b5"},
+    {'s', 6, 16, 5, "strip-s6x16-b5"}, {'s', 9, 6, 5, "strip-s9x6-b5"},   {'s', 12, 4, 4, "strip-s12x4-b4"},
+};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+constexpr int kNumTiled = 5;          // variants 0 .. 4 are tiled
+constexpr int kDefaultStrip = 5;      // strip-s6x8-b5
 
-// Variants kNumVariants and kNumVariants + 1 are the strip walk
-// (launch_focal_strip) at 5 and 6 CTAs per SM.
-int focal_num_variants() { return kNumVariants + 2; }
-bool focal_variant_is_strip(int v) { return v == kNumVariants || v == kNumVariants + 1; }
-int focal_variant_rows(int v) { return kWarps * kVariants[(v >= 0 && v < kNumVariants) ? v : 0].rows; }
+int focal_num_variants() { return kNumVariants; }
+int focal_default_strip_variant() { return kDefaultStrip; }
+bool focal_variant_is_strip(int v) { return v >= kNumTiled && v < kNumVariants; }
+int focal_variant_rows(int v) { return kWarps * kVariants[(v >= 0 && v < kNumTiled) ? v : 0].rows; }
+const char* focal_variant_name(int v) { return (v >= 0 && v < kNumVariants) ? kVariants[v].name : nullptr; }
+// Stage rows of strip variant v for these outputs: the stage geometries other
+// than the default are built for the fused slope + D8 (the tuned operation);
+// single-output calls run them at the default geometry.
+int focal_strip_stage_rows(int v, int do_slope, int do_d8) {
+    if (!focal_variant_is_strip(v) || !(do_slope && do_d8)) return kSR;
+    return kVariants[v].rows;
+}
 size_t focal_tma_smem_bytes() { return 2 * Shape<kBatchRows>::kStageStride; }
 int focal_tma_tile_rows() { return Shape<kBatchRows>::kTH; }
 int focal_tma_tile_cols() { return kTW; }
@@ -1200,17 +1242,16 @@ static cudaError_t launch_variants(const CUtensorMap* map, const FocalParams& p,
     }
 }
 
-int focal_strip_stage_rows() { return kSR; }
-
-template <bool SLOPE, bool D8, int MINB>
+template <bool SLOPE, bool D8, int MINB, int SR = kSR, int STAGES = kSegStages>
 static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
                                 const FocalParams& p, unsigned long long* counters, uint32_t* slow_items, int num_sms,
                                 cudaStream_t s) {
-    const int64_t nstrips = (p.cols + kTW - 1) / kTW, nbands = (p.rows + kSegRows - 1) / kSegRows;
+    using G = StripGeom<SR, STAGES>;
+    const int64_t nstrips = (p.cols + kTW - 1) / kTW, nbands = (p.rows + G::kSegRows - 1) / G::kSegRows;
     const int64_t nsegs = nstrips * nbands;
     if (nsegs == 0) return cudaSuccess;
-    const size_t smem = (size_t)kSWarps * kSWarpBytes;
-    auto kern = focal_strip_kernel<SLOPE, D8, MINB>;
+    const size_t smem = (size_t)kSWarps * G::kWarpBytes;
+    auto kern = focal_strip_kernel<SLOPE, D8, MINB, SR, STAGES>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0;
@@ -1230,7 +1271,8 @@ static cudaError_t launch_strip(const CUtensorMap* map_stage, const CUtensorMap*
 
 size_t focal_strip_slow_bytes(int64_t rows, int64_t cols) { return (size_t)(rows * ((cols + 3) / 4)) * 4; }
 
-// Strip-walk form: `map_stage` has a (kBoxW, focal_strip_stage_rows()) box and
+// Strip-walk form: `map_stage` has a (kBoxW, focal_strip_stage_rows(variant,
+// ...)) box and
 // `map_prime` a (kBoxW, 2) box over the same float32 DEM `dem`; `counters`
 // points to two device counters (segment claims, slow items) and
 // `slow_items` to focal_strip_slow_bytes() of scratch.
@@ -1253,8 +1295,17 @@ cudaError_t launch_focal_strip(const CUtensorMap* map_stage, const CUtensorMap* 
     FocalParams q = p;
     q.fast_out = fast_out;
     q.fd = p.sk.method == PARGO_SLOPE_FD || !p.do_slope;
-    if (variant == kNumVariants + 1)
-        return launch_strip_minb<6>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+    if (q.do_slope && q.do_d8) {
+        switch (variant) {  // the stage geometries (map_stage's box: focal_strip_stage_rows())
+            case 7: return launch_strip<true, true, 5, 3, 16>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+            case 8: return launch_strip<true, true, 5, 6, 4>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+            case 9: return launch_strip<true, true, 5, 6, 16>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+            case 10: return launch_strip<true, true, 5, 9, 6>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+            case 11: return launch_strip<true, true, 4, 12, 4>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
+            default: break;
+        }
+    }
+    if (variant == 6) return launch_strip_minb<6>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
     return launch_strip_minb<5>(map_stage, map_prime, dem, q, counters, slow_items, num_sms, s);
 }
 

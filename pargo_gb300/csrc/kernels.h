@@ -67,7 +67,9 @@ int focal_tma_box_rows();
 cudaError_t launch_focal_strip(const CUtensorMap* map_stage, const CUtensorMap* map_prime, const InView& dem,
                                const FocalParams& p, int fast_out, int variant, unsigned long long* counters,
                                uint32_t* slow_items, int num_sms, cudaStream_t s);
-int focal_strip_stage_rows();
+int focal_strip_stage_rows(int variant, int do_slope, int do_d8);
+int focal_default_strip_variant();
+const char* focal_variant_name(int variant);
 size_t focal_strip_slow_bytes(int64_t rows, int64_t cols);
 
 // Batched slope+D8 (focal.cu): device tables of per-raster descriptors/params.

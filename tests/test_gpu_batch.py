@@ -70,23 +70,26 @@ def test_batch_strip_walk_with_nodata_and_edge_sizes(outputs, ctx, oracle_lib):
 
 
 def _np_queue(dems, nodata_load, valid_load, seg_rows=48, seg_cols=128):
-    """The queue by intensity, restated: segments numbered raster by raster
-    (largest raster first), loads counted with |v - nodata| > 1e-7 as valid,
-    then a stable sort heaviest first."""
-    korder = sorted(range(len(dems)), key=lambda i: -dems[i].size)
-    items = []
+    """The queue by intensity, restated: segment loads counted with
+    |v - nodata| > 1e-7 as valid, summed per raster, rasters heaviest first
+    (a stable sort of the rasters by size, largest first), each raster's
+    segments in order."""
+    korder = sorted(range(len(dems)), key=lambda i: -dems[i].size)   # Python's sort is stable
+    per = []
     for k in korder:
         d = dems[k].astype(np.float64)
         valid = np.abs(d - (-9999.0)) > 1e-7
         R, C = d.shape
         ns = (C + seg_cols - 1) // seg_cols
         nb = (R + seg_rows - 1) // seg_rows
+        items = []
         for l in range(ns * nb):
             x0, y0 = (l % ns) * seg_cols, (l // ns) * seg_rows
             v = valid[y0:y0 + seg_rows, x0:x0 + seg_cols]
             items.append((k, l, float(v.sum()) * valid_load + float(v.size - v.sum()) * nodata_load))
-    order = sorted(range(len(items)), key=lambda i: -items[i][2])   # Python's sort is stable
-    return [items[i] for i in order]
+        per.append(items)
+    order = sorted(range(len(per)), key=lambda j: -sum(it[2] for it in per[j]))
+    return [it for j in order for it in per[j]]
 
 
 @pytest.mark.parametrize("loads", [(0.0, 1.0), (3.0, 1.0)])
@@ -102,7 +105,8 @@ def test_batch_queue_by_intensity_matches_restatement(loads, ctx):
     assert np.array_equal(ld, np.array([w[2] for w in want]))
     assert np.array_equal(ras, np.array([w[0] for w in want]))
     assert np.array_equal(seg, np.array([w[1] for w in want]))
-    assert (np.diff(ld) <= 0).all()
+    rl = [ld[ras == k].sum() for k in list(dict.fromkeys(ras.tolist()))]
+    assert (np.diff(rl) <= 0).all()                            # rasters heaviest first
     r2, s2, l2 = ctx.batch_queue([abi.raster(d, -9999.0) for d in dd], order=abi.BATCH_BY_SIZE)
     korder = sorted(range(len(dems)), key=lambda i: -dems[i].size)
     assert list(dict.fromkeys(r2.tolist())) == korder       # raster by raster, largest first
