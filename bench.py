@@ -460,7 +460,7 @@ def run_batch(args, ws, rank, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (D8 decisions certified, FP64 fallback)",
         "data": "synthetic", "batched_vs_plain_speedup": round(ms_p / ms_b, 3), "plain_ms_per_step": round(ms_p, 4),
         "batched_outputs_identical_to_plain": identical,
-        "queue": {"order": "segments by compute intensity (valid 1, nodata 0), heaviest first",
+        "queue": {"order": "rasters by compute intensity (valid 1, nodata 0), heaviest first, each raster's segments together",
                   "first_call_ms_with_estimate": round(first_call_ms, 3),
                   "ms_per_step_ordered_by_raster_size": round(ms_size, 4)},
         "config": {"workload": "batch512: 512 fBm rasters, seeds 100-611, sides log-uniform [256, 4096], "

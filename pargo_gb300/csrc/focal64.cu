@@ -120,9 +120,19 @@ __device__ __forceinline__ int load_keys(const double* s, int ty, int lane, long
 // correct rounding; above, the error is at most 2^-23 |d| (the low half's
 // rounding, 2^8, is below 2^-24 |d|), which keeps the certified D8 bound
 // |x - r| <= 2^-22 |x| with the diagonal's extra roundings.
+// The conversions run on the FP32 and integer pipes: an integer x < 2^23 is
+// exactly the float 2^23 + x (x in the significand) minus 2^23, so the high
+// half (< 2^22: |d| < 2^54) converts exactly, and the low half's two 16-bit
+// halves convert exactly and are joined by one fma -- the single correct
+// rounding of the low half, the same bits as __uint2float_rn gives.  The
+// hardware conversion instructions ran on the FP64 pipe here (a narrow pipe
+// on this part; 50% busy on the 2048^2 profile with ~5% of cells on FP64).
+__device__ __forceinline__ float u23f(unsigned x) { return __int_as_float(0x4B000000u | x) - 8388608.0f; }
 __device__ __forceinline__ float i64f(long long d) {
     const unsigned long long a = (unsigned long long)(d < 0 ? -d : d);
-    const float f = __fmaf_rn(__uint2float_rn((unsigned int)(a >> 32)), 4294967296.0f, __uint2float_rn((unsigned int)a));
+    const unsigned lo = (unsigned)a, hi = (unsigned)(a >> 32);
+    const float lof = __fmaf_rn(u23f(lo >> 16), 65536.0f, u23f(lo & 0xFFFFu));
+    const float f = __fmaf_rn(u23f(hi), 4294967296.0f, lof);
     return d < 0 ? -f : f;
 }
 
