@@ -978,8 +978,6 @@ pargo_status fill_core(pargo_ctx* ctx, const Staged& sdem, const pargo_raster* d
     p.init_level = o.init_level;
     p.tiles_y = (rows + T - 1) / T;
     p.tiles_x = (cols + T - 1) / T;
-    p.defer = 0;
-    if (const char* dv = getenv("PARGO_FILL_DEFER")) p.defer = atoi(dv);  // EXPERIMENT
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     if (ntiles >= INT32_MAX) return fail(ctx, PARGO_ERR_INVALID_ARG, "fill: raster too large");
     cudaError_t e;

@@ -232,61 +232,6 @@ __device__ int32_t ring_pop(const FillScratch& s, long long patience) {
 // before a neighbour's write is always followed by one that reads after it.
 constexpr int32_t kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3;
 
-// A popped tile back to the ring's tail, still queued and still counted as
-// pending (it never left the queue as far as the count is concerned).
-__device__ void ring_repush(const FillScratch& s, int32_t t, long long patience) {
-    const unsigned long long pos = atomicAdd(&s.q[kQTail], 1ULL);
-    int32_t* slot = &s.ring[pos % (unsigned long long)s.ring_cap];
-    const long long t0 = clock64();
-    unsigned ns = 32;
-    while (atomicCAS(slot, -1, t) != -1) {
-        if (vload64(&s.q[kQError]) != 0) return;
-        if (clock64() - t0 > patience) {
-            atomicCAS(&s.q[kQError], 0ULL, (unsigned long long)kQErrPush);
-            return;
-        }
-        __nanosleep(ns);
-        if (ns < 1024) ns *= 2;
-    }
-}
-
-// Whether one of tile t's eight neighbours has a visitor right now.  Two
-// neighbouring tiles relaxed at once each read the other's border before the
-// other's writes and request each other again; a visitor that pops such a
-// tile puts it back (up to FillParams::defer times in a row) and takes the
-// next one.
-__device__ __forceinline__ bool neighbour_running(const FillScratch& s, const FillParams& p, int32_t t) {
-    const int64_t ty = t / p.tiles_x, tx = t % p.tiles_x;
-    bool busy = false;
-#pragma unroll
-    for (int a = -1; a <= 1; a++)
-#pragma unroll
-        for (int b = -1; b <= 1; b++) {
-            if ((a | b) == 0) continue;
-            const int64_t y = ty + a, x = tx + b;
-            if (y < 0 || x < 0 || y >= p.tiles_y || x >= p.tiles_x) continue;
-            busy |= *((volatile int32_t*)&s.queued[y * p.tiles_x + x]) >= kRunning;
-        }
-    return busy;
-}
-
-__device__ void request_tile(const FillScratch& s, int32_t t, long long patience) {
-    int32_t st = kIdle;  // the common state: the first CAS either queues the tile or returns its state
-    for (int guard = 0; guard < 64; guard++) {  // each failed CAS means another thread moved the state
-        int32_t want;
-        if (st == kIdle) want = kQueued;
-        else if (st == kRunning) want = kRunningDirty;
-        else return;  // already queued, or will be queued by its visitor
-        const int32_t old = atomicCAS(&s.queued[t], st, want);
-        if (old == st) {
-            if (want == kQueued) ring_push(s, t, patience);
-            return;
-        }
-        st = old;
-    }
-    atomicCAS(&s.q[kQError], 0ULL, (unsigned long long)kQErrState);
-}
-
 // Record, in tile (ty, tx)'s halo-change words, cells of its halo that this
 // visit changed (word k, bits); ignored outside the raster's tiles.
 __device__ __forceinline__ void mark_halo(const FillScratch& s, const FillParams& p, int64_t ty, int64_t tx, int k,
@@ -350,10 +295,6 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
             if (!chase) {
                 if (PERSIST) {
                     claim = ring_pop(s, patience);
-                    for (int d = 0; d < p.defer && claim >= 0 && neighbour_running(s, p, claim); d++) {
-                        ring_repush(s, claim, patience);
-                        claim = ring_pop(s, patience);
-                    }
                 } else {
                     const int32_t k = atomicAdd(&s.counts[2], 1);
                     claim = k < ncur ? cur[k] : -1;

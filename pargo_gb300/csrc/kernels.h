@@ -127,7 +127,6 @@ struct FillParams {
     double* w;              // working levels, rows x w_stride doubles, +inf marks nodata levels
     int64_t w_stride;       // elements per row of w (a multiple of 2: 16-byte rows for TMA)
     int64_t tiles_y, tiles_x;
-    int defer;              // persistent form: times a popped tile with a running neighbour goes back to the ring
 };
 struct FillScratch {
     int32_t* list_a;        // tile worklists (capacity tiles_y * tiles_x)
