@@ -232,6 +232,23 @@ __device__ int32_t ring_pop(const FillScratch& s, long long patience) {
 // before a neighbour's write is always followed by one that reads after it.
 constexpr int32_t kIdle = 0, kQueued = 1, kRunning = 2, kRunningDirty = 3;
 
+__device__ void request_tile(const FillScratch& s, int32_t t, long long patience) {
+    int32_t st = kIdle;  // the common state: the first CAS either queues the tile or returns its state
+    for (int guard = 0; guard < 64; guard++) {  // each failed CAS means another thread moved the state
+        int32_t want;
+        if (st == kIdle) want = kQueued;
+        else if (st == kRunning) want = kRunningDirty;
+        else return;  // already queued, or will be queued by its visitor
+        const int32_t old = atomicCAS(&s.queued[t], st, want);
+        if (old == st) {
+            if (want == kQueued) ring_push(s, t, patience);
+            return;
+        }
+        st = old;
+    }
+    atomicCAS(&s.q[kQError], 0ULL, (unsigned long long)kQErrState);
+}
+
 // Record, in tile (ty, tx)'s halo-change words, cells of its halo that this
 // visit changed (word k, bits); ignored outside the raster's tiles.
 __device__ __forceinline__ void mark_halo(const FillScratch& s, const FillParams& p, int64_t ty, int64_t tx, int k,
