@@ -43,6 +43,7 @@ namespace {
 constexpr int kT = kScaTile;       // tile side
 constexpr int kH = kT + 4;         // codes with a 2-cell halo
 constexpr int kCells = kT * kT;
+constexpr int kThreads = 256;
 constexpr int8_t kNodata = -1, kNoFlow = -2;
 
 __device__ __forceinline__ int8_t decode8(const ScaParams& p, int64_t r, int64_t c) {
@@ -76,38 +77,31 @@ __device__ __forceinline__ int slot_of(int lr, int lc, int th, int tw) {
     return -1;
 }
 
-// Shared state of one tile.  The in-tile flow forest is summed by the Euler
-// tour technique: every non-root cell v contributes two tour elements,
-// down(v) = 2v (weight w(v)) and up(v) = 2v + 1 (weight 0); the tour of a
-// tree visits down(v), the tours of v's children, up(v).  Suffix sums along
-// the tours by pointer jumping (log2 of the tour length rounds, each a
-// read phase and a write phase between barriers) give every subtree sum as
-// R(down(v)) - R(up(v)), so no thread walks a chain: a filled lake makes
-// in-tile flow paths thousands of cells long, and walking them one thread per
-// chain made the tile passes latency bound.  A weight packs two counts:
-// the cell's own count 1 + inflow (low field) and whether it is "bad" (high
-// field), so one ranking gives the subtree sum and the subtree OR of "bad".
-// Roots are found by pointer jumping on the parents (log2(cells) rounds); a
-// cell whose chain reaches no root lies on or above a cycle and is not
-// completed.
+// Shared state of one tile.  In-degrees (at most 8) and flags are bytes
+// packed four to a word: a walker decrements a degree by an atomic subtract
+// on the word (a byte is at least 1 when decremented, so nothing borrows from
+// its neighbours) and sets flags by atomic OR.  Flag bits: 1 valid work cell,
+// 2 "bad" (a non-source inflow follows it in raster order), 4 completed,
+// 8 in-tile leaf, 16 some cell of its subtree is bad.  In-tile sums fit 32
+// bits in the first pass; the final pass adds inflows from other tiles.
 template <bool FINAL>
 struct TileSmem {
-    // packed tour weights: first pass 16 + 16 bits, final pass 48 + 16 bits
-    using Val = typename std::conditional<FINAL, unsigned long long, unsigned int>::type;
-    static constexpr int kBadShift = FINAL ? 48 : 16;
-    int8_t cd[kH * kH];                  // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
-    uint8_t src[(kT + 2) * (kT + 2)];    // the tile and a one-cell ring: reference in-degree is zero
-    uint8_t flags[kCells];               // 1 valid work cell, 2 bad, 4 completed, 16 an unpulled inflow from another tile
-    int16_t lpar[kCells];                // in-tile parent, -1 none, -2 outside the tile
-    int16_t root[kCells];                // pointer jumping towards the chain's last cell
-    int16_t next[2 * kCells];            // tour successor, -1 at the end
-    Val val[2 * kCells];                 // tour weights, then suffix sums
-    unsigned long long cnt[3];           // valid, completed, ring inflows
+    using Acc = typename std::conditional<FINAL, unsigned long long, unsigned int>::type;
+    int8_t cd[kH * kH];          // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
+    int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
+    uint32_t degw[kCells / 4];   // in-tile children not yet folded in, a byte per cell
+    Acc acc[kCells];
+    uint32_t flagw[kCells / 4];  // a byte of flags per cell
+    unsigned long long cnt[3];   // valid, completed, ring inflows
+    __device__ __forceinline__ unsigned flag(int i) const { return (flagw[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
+    __device__ __forceinline__ unsigned flag_sync(int i) { return (atomicOr(&flagw[i >> 2], 0u) >> (8 * (i & 3))) & 0xFFu; }
+    __device__ __forceinline__ void set_flag(int i, unsigned bits) { atomicOr(&flagw[i >> 2], bits << (8 * (i & 3))); }
+    // true when this call folded in the last child
+    __device__ __forceinline__ bool dec_degree(int i) {
+        const unsigned sh = 8 * (i & 3);
+        return ((atomicSub(&degw[i >> 2], 1u << sh) >> sh) & 0xFFu) == 1u;
+    }
 };
-
-constexpr int kTourThreads = 512;
-constexpr int kCellsPerThread = kCells / kTourThreads;  // 8
-constexpr int kElemsPerThread = 2 * kCellsPerThread;    // 16
 
 // Whether the neighbour at (a, b) of the cell at codes position (ca, cb)
 // flows into it: its code names the cell and the cell does not name it back.
@@ -118,27 +112,21 @@ __device__ __forceinline__ bool flows_in(const S_t& S, int ca, int cb, int a, in
     return q == 8 - k && S.cd[ca * kH + cb] != k;
 }
 
-// First in-tile child of v after window position `after` (-1: from the
-// start), or -1: the neighbours whose in-tile parent is v, in window order.
+// Reference in-degree of the cell at codes position (ca, cb) is zero.
 template <class S_t>
-__device__ __forceinline__ int child_after(const S_t& S, int v, int after, int th, int tw) {
-    const int vr = v / kT, vc = v % kT;
-#pragma unroll 1
-    for (int k = after + 1; k < 9; k++) {
-        if (k == 4) continue;
-        const int qr = vr + k / 3 - 1, qc = vc + k % 3 - 1;
-        if (qr < 0 || qc < 0 || qr >= th || qc >= tw) continue;
-        const int q = qr * kT + qc;
-        if (S.lpar[q] == v) return q;
-    }
-    return -1;
+__device__ __forceinline__ bool is_source(const S_t& S, int ca, int cb) {
+#pragma unroll
+    for (int a = -1; a <= 1; a++)
+#pragma unroll
+        for (int b = -1; b <= 1; b++)
+            if ((a || b) && flows_in(S, ca, cb, a, b)) return false;
+    return true;
 }
 
 template <bool FINAL>
-__global__ void __launch_bounds__(kTourThreads, 2) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
+__global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
     extern __shared__ __align__(16) unsigned char sca_smem[];
     using Smem = TileSmem<FINAL>;
-    using Val = typename Smem::Val;
     Smem& S = *reinterpret_cast<Smem*>(sca_smem);
     const int tid = threadIdx.x;
     const int64_t ntiles = T.tiles_x * T.tiles_y;
@@ -154,26 +142,16 @@ __global__ void __launch_bounds__(kTourThreads, 2) sca_tile_kernel(const ScaPara
             T.tin[node] = 0;
             T.tinb[node] = 0;
         }
-        for (int i = tid; i < kH * kH; i += kTourThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
+        for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
         __syncthreads();
-        // Reference sources (in-degree zero) over the tile and a one-cell ring.
-        for (int i = tid; i < (kT + 2) * (kT + 2); i += kTourThreads) {
-            const int ca = i / (kT + 2) + 1, cb = i % (kT + 2) + 1;
-            bool src = true;
-#pragma unroll
-            for (int a = -1; a <= 1; a++)
-#pragma unroll
-                for (int b = -1; b <= 1; b++)
-                    if ((a || b) && flows_in(S, ca, cb, a, b)) src = false;
-            S.src[i] = src ? 1 : 0;
-        }
-        // The in-tile forest: parents, flags.
+        // The in-tile forest.
         unsigned long long nvalid = 0, nring = 0;
-        for (int i = tid; i < kCells; i += kTourThreads) {
+        for (int i = tid; i < kCells; i += kThreads) {
             const int lr = i / kT, lc = i % kT;
             const int64_t r = r0 + lr, c = c0 + lc;
             const int ca = lr + 2, cb = lc + 2;
             int16_t lp = -1;
+            int deg = 0;
             uint8_t f = 0;
             if (lr < th && lc < tw && in_work(p, r, c) && S.cd[ca * kH + cb] != kNodata) {
                 f = 1;
@@ -187,151 +165,110 @@ __global__ void __launch_bounds__(kTourThreads, 2) sca_tile_kernel(const ScaPara
                         lp = (tr >= 0 && tc >= 0 && tr < th && tc < tw) ? (int16_t)(tr * kT + tc) : (int16_t)-2;
                     }
                 }
-                // an inflow from the ring is never released; a non-source child
-                // that follows the cell in raster order is not pulled by the
-                // single sweep ("bad")
-#pragma unroll
+                // children: in-tile ones count towards the walk; an inflow from
+                // the ring is never released; a non-source child that follows
+                // the cell in raster order is not pulled by the single sweep.
+#pragma unroll 1
                 for (int a = -1; a <= 1; a++)
-#pragma unroll
+#pragma unroll 1
                     for (int b = -1; b <= 1; b++) {
                         if (!(a || b) || !flows_in(S, ca, cb, a, b)) continue;
                         if (!in_work(p, r + a, c + b)) {
                             nring++;
                             continue;
                         }
-                        if ((a > 0 || (a == 0 && b > 0)) && !S.src[(lr + 1 + a) * (kT + 2) + (lc + 1 + b)]) f |= 2;
+                        const int qr = lr + a, qc = lc + b;
+                        if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
+                        if ((a > 0 || (a == 0 && b > 0)) && !is_source(S, ca + a, cb + b)) f |= 2;
                     }
-                if (FINAL) {
-                    const int sl = slot_of(lr, lc, th, tw);
-                    if (sl >= 0 && T.tinb[t * kScaSlots + sl]) f |= 16;  // an inflow from another tile was not pulled
-                }
             }
             S.lpar[i] = lp;
-            S.root[i] = lp >= 0 ? lp : (int16_t)i;
-            S.flags[i] = f;
+            reinterpret_cast<uint8_t*>(S.degw)[i] = (uint8_t)deg;
+            reinterpret_cast<uint8_t*>(S.flagw)[i] = (f && deg == 0) ? (uint8_t)(f | 8) : f;  // leaves fixed before any walk
+            unsigned long long w = 0;
+            uint32_t wb = 0;
+            if (FINAL && f) {
+                const int sl = slot_of(lr, lc, th, tw);
+                if (sl >= 0) {
+                    w = T.tin[t * kScaSlots + sl];
+                    wb = T.tinb[t * kScaSlots + sl];
+                }
+            }
+            S.acc[i] = (typename Smem::Acc)w;  // external inflow (final pass) plus, later, the in-tile children
+            if (wb) reinterpret_cast<uint8_t*>(S.flagw)[i] |= 16;  // an inflow from another tile was not pulled
         }
         atomicAdd(&S.cnt[0], nvalid);
         if (nring) atomicAdd(&S.cnt[2], nring);
         __syncthreads();
-        // Tour successors and weights.
-        for (int v = tid; v < kCells; v += kTourThreads) {
-            const int lp = S.lpar[v];
-            Val wd = 0;
-            int16_t nd = -1, nu = -1;
-            if (lp >= 0) {  // a non-root valid cell (only valid cells have parents)
-                const unsigned f = S.flags[v];
-                unsigned long long own = 1;
-                if (FINAL) {
-                    const int sl = slot_of(v / kT, v % kT, th, tw);
-                    if (sl >= 0) own += T.tin[t * kScaSlots + sl];
-                }
-                wd = (Val)own | ((Val)((f & 18u) ? 1u : 0u) << Smem::kBadShift);
-                const int fc = child_after(S, v, -1, th, tw);
-                nd = fc >= 0 ? (int16_t)(2 * fc) : (int16_t)(2 * v + 1);
-                const int kpos = ((v / kT) - (lp / kT) + 1) * 3 + ((v % kT) - (lp % kT) + 1);  // v in lp's window
-                const int ns = child_after(S, lp, kpos, th, tw);
-                nu = ns >= 0 ? (int16_t)(2 * ns) : (S.lpar[lp] >= 0 ? (int16_t)(2 * lp + 1) : (int16_t)-1);
-            }
-            S.val[2 * v] = wd;
-            S.val[2 * v + 1] = 0;
-            S.next[2 * v] = nd;
-            S.next[2 * v + 1] = nu;
-        }
-        __syncthreads();
-        // Suffix sums along the tours (Wyllie's pointer jumping).
-#pragma unroll 1
-        for (int round = 0; round < 14; round++) {
-            Val nv[kElemsPerThread];
-            int16_t nn[kElemsPerThread];
-            bool more = false;
-#pragma unroll
-            for (int j = 0; j < kElemsPerThread; j++) {
-                const int e = tid + j * kTourThreads;
-                const int n = S.next[e];
-                nv[j] = S.val[e];
-                nn[j] = (int16_t)n;
-                if (n >= 0) {
-                    nv[j] += S.val[n];
-                    nn[j] = S.next[n];
-                    more = true;
-                }
-            }
-            if (!__syncthreads_or(more)) break;
-#pragma unroll
-            for (int j = 0; j < kElemsPerThread; j++) {
-                const int e = tid + j * kTourThreads;
-                S.val[e] = nv[j];
-                S.next[e] = nn[j];
-            }
-            __syncthreads();
-        }
-        // Roots: pointer jumping on the parents (a chain without a cycle
-        // reaches its root within kCells - 1 steps: 12 doublings).
-#pragma unroll 1
-        for (int round = 0; round < 12; round++) {
-            int16_t nr[kCellsPerThread];
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; j++) nr[j] = S.root[S.root[tid + j * kTourThreads]];
-            __syncthreads();
-#pragma unroll
-            for (int j = 0; j < kCellsPerThread; j++) S.root[tid + j * kTourThreads] = nr[j];
-            __syncthreads();
-        }
-        // Subtree sums; completion; outputs of the pass.
+        // Topological walk from the in-tile leaves.
         unsigned long long ndone = 0;
-        for (int v = tid; v < kCells; v += kTourThreads) {
-            const unsigned f = S.flags[v];
-            if (!(f & 1u)) continue;
-            const bool done = S.lpar[S.root[v]] < 0;  // its chain ends at a root
-            Val tot;
-            if (S.lpar[v] >= 0) {
-                tot = S.val[2 * v] - S.val[2 * v + 1];
-            } else {  // a root: its own weight and every down edge of its tree
-                unsigned long long own = 1;
-                if (FINAL) {
-                    const int sl = slot_of(v / kT, v % kT, th, tw);
-                    if (sl >= 0) own += T.tin[t * kScaSlots + sl];
-                }
-                tot = (Val)own | ((Val)((f & 18u) ? 1u : 0u) << Smem::kBadShift);
-                const int fc = child_after(S, v, -1, th, tw);
-                if (fc >= 0) tot += S.val[2 * fc];
+        for (int i = tid; i < kCells; i += kThreads) {
+            if (!(S.flag(i) & 8)) continue;
+            int cur = i;
+            for (;;) {
+                const unsigned long long tot = 1 + (unsigned long long)atomicAdd(&S.acc[cur], (typename Smem::Acc)0);
+                const unsigned fl = S.flag_sync(cur);
+                const bool bad = (fl & 2) || (fl & 16);
+                S.acc[cur] = (typename Smem::Acc)tot;
+                S.set_flag(cur, 4u | (bad ? 16u : 0u));
+                ndone++;
+                const int par = S.lpar[cur];
+                if (par < 0) break;
+                atomicAdd(&S.acc[par], (typename Smem::Acc)tot);
+                if (bad) S.set_flag(par, 16u);
+                __threadfence_block();
+                if (!S.dec_degree(par)) break;
+                __threadfence_block();
+                cur = par;
             }
-            const unsigned long long sum = (unsigned long long)(tot & (((Val)1 << Smem::kBadShift) - 1));
-            const unsigned bad = (tot >> Smem::kBadShift) != 0 ? 1u : 0u;
-            if (done) ndone++;
-            if (FINAL) {
-                const int64_t g = (r0 + v / kT) * p.cols + (c0 + v % kT);
-                s.conv[g] = done ? sum : 0ULL;
-                s.ship[g] = done ? (unsigned long long)bad : 0ULL;
-            } else if (done) {
-                const int lr = v / kT, lc = v % kT;
+        }
+        atomicAdd(&S.cnt[1], ndone);
+        __syncthreads();
+        if (!FINAL) {
+            // Border cells: the exit each in-tile path reaches; exits record
+            // their in-tile totals and the entry they feed.
+            for (int i = tid; i < kCells; i += kThreads) {
+                const int lr = i / kT, lc = i % kT;
+                if (lr >= th || lc >= tw) continue;
                 const int sl = slot_of(lr, lc, th, tw);
-                if (sl >= 0) {
-                    // a border cell: the exit its path reaches; an exit: where its flow enters
-                    const int64_t node = t * kScaSlots + sl;
-                    const int rt = S.root[v];
-                    if (S.lpar[rt] == -2) T.exit_of[node] = (int32_t)(t * kScaSlots + slot_of(rt / kT, rt % kT, th, tw));
-                    if (S.lpar[v] == -2) {
+                if (sl < 0) continue;
+                const int64_t node = t * kScaSlots + sl;
+                int32_t ex = -1, ys = -1;
+                if (S.flag(i) & 4) {  // completed: its path is acyclic
+                    int cur = i;
+                    for (int step = 0; step < kCells && S.lpar[cur] >= 0; step++) cur = S.lpar[cur];
+                    if (S.lpar[cur] == -2) {
+                        const int er = cur / kT, ec = cur % kT;
+                        ex = (int32_t)(t * kScaSlots + slot_of(er, ec, th, tw));
+                    }
+                    if (S.lpar[i] == -2) {  // this cell is an exit: where its flow enters
                         const int8_t k = S.cd[(lr + 2) * kH + (lc + 2)];
                         const int64_t yr = r0 + lr + k / 3 - 1, yc = c0 + lc + k % 3 - 1;
                         const int64_t yt = (yr / kT) * T.tiles_x + (yc / kT);
                         const int yth = (int)min((int64_t)kT, p.rows - (yr / kT) * kT);
                         const int ytw = (int)min((int64_t)kT, p.cols - (yc / kT) * kT);
-                        T.yslot[node] = (int32_t)(yt * kScaSlots + slot_of((int)(yr % kT), (int)(yc % kT), yth, ytw));
-                        T.tot[node] = sum;
-                        T.totb[node] = bad;
+                        ys = (int32_t)(yt * kScaSlots + slot_of((int)(yr % kT), (int)(yc % kT), yth, ytw));
+                        T.tot[node] = S.acc[i];
+                        T.totb[node] = (S.flag(i) >> 4) & 1u;
                     }
                 }
+                T.exit_of[node] = ex;
+                T.yslot[node] = ys;
             }
-        }
-        atomicAdd(&S.cnt[1], ndone);
-        __syncthreads();
-        if (tid == 0) {
-            if (FINAL) {
+            if (tid == 0 && S.cnt[2]) atomicAdd(&s.counters[6], S.cnt[2]);
+        } else {
+            for (int i = tid; i < kCells; i += kThreads) {
+                const int lr = i / kT, lc = i % kT;
+                if (lr >= th || lc >= tw) continue;
+                const int64_t g = (r0 + lr) * p.cols + (c0 + lc);
+                const unsigned fl = S.flag(i);
+                const bool ok = (fl & 5) == 5;
+                s.conv[g] = ok ? (unsigned long long)S.acc[i] : 0ULL;
+                s.ship[g] = ok ? (unsigned long long)((fl >> 4) & 1u) : 0ULL;
+            }
+            if (tid == 0) {
                 atomicAdd(&s.counters[1], S.cnt[0]);
                 atomicAdd(&s.counters[0], S.cnt[1]);
-            } else if (S.cnt[2]) {
-                atomicAdd(&s.counters[6], S.cnt[2]);
             }
         }
         __syncthreads();
@@ -475,17 +412,17 @@ cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTile
     int dev = 0, sms = 0, per0 = 0, per1 = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sca_tile_kernel<false>, kTourThreads, smem0)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, sca_tile_kernel<false>, kThreads, smem0)) !=
         cudaSuccess)
         return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, sca_tile_kernel<true>, kTourThreads, smem1)) !=
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, sca_tile_kernel<true>, kThreads, smem1)) !=
         cudaSuccess)
         return e;
     const int64_t ntiles = T.tiles_x * T.tiles_y;
     int64_t grid0 = (int64_t)sms * (per0 > 0 ? per0 : 1), grid1 = (int64_t)sms * (per1 > 0 ? per1 : 1);
     if (grid0 > ntiles) grid0 = ntiles;
     if (grid1 > ntiles) grid1 = ntiles;
-    sca_tile_kernel<false><<<(unsigned)grid0, kTourThreads, smem0, st>>>(p, s, T);
+    sca_tile_kernel<false><<<(unsigned)grid0, kThreads, smem0, st>>>(p, s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const int64_t nodes = ntiles * kScaSlots;
     int64_t nb = (nodes + 255) / 256;
@@ -496,7 +433,7 @@ cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTile
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sca_exit_walk_kernel<<<(unsigned)nb, 256, 0, st>>>(s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    sca_tile_kernel<true><<<(unsigned)grid1, kTourThreads, smem1, st>>>(p, s, T);
+    sca_tile_kernel<true><<<(unsigned)grid1, kThreads, smem1, st>>>(p, s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     int64_t blocks = (n + 255) / 256;
     if (blocks > 8192) blocks = 8192;
