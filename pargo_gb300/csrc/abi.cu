@@ -1572,8 +1572,9 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     CU(ctx, launch_sca_mfd_init(p, ctx->num_sms, s));
     int32_t* hc = (int32_t*)pinned(ctx, 128, &e);
     if (!hc) return cuda_fail(ctx, e, "pinned counters");
-    // Every round in one cooperative launch (a grid barrier between rounds);
-    // where a cooperative launch is not available, rounds as CUDA graphs.
+    // One persistent launch in which threads walk the flow DAG (a cell is
+    // processed by the thread that released its last inflow); where that
+    // launch cannot run, frontier rounds as CUDA graphs.
     if (launch_sca_mfd_persistent(p, ctx->num_sms, s) == cudaSuccess) {
         CU(ctx, launch_sca_mfd_output(p, ctx->num_sms, s));
         if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
@@ -1586,7 +1587,7 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
             return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: %llu of %llu valid cells processed (cycle)", ht[1], ht[0]);
         return PARGO_OK;
     }
-    cudaGetLastError();  // clear the refused cooperative launch
+    cudaGetLastError();  // clear the refused launch
     // Frontier rounds, 32 per CUDA graph (an even number: list A is current
     // again after each graph), until both lists are empty.
     constexpr int kRounds = 32;

@@ -248,17 +248,18 @@ struct ScaMfdParams {
     double* sca;
     int32_t* list_a;
     int32_t* list_b;
-    int32_t* list_c;               // the persistent form's third frontier list
-    int32_t* counts;               // [0] length of list_a, [1] of list_b, [2] finished blocks, [3] of list_c
+    int32_t* list_c;               // spare list
+    int32_t* counts;               // [0] length of list_a, [1] of list_b, [2] finished blocks / list_b claims, [3] list_a claims
     unsigned long long* totals;    // [0] valid cells, [1] processed cells, [2] nodata cells with weights
-    unsigned int* barrier;         // [0] arrivals, [1] generation (persistent form)
-    int* error_flag;               // a bounded wait of the persistent form gave up
+    unsigned int* barrier;         // [0] pending ready cells (walk form)
+    int* error_flag;               // a bounded wait of the walk form gave up
 };
 cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t st);
 cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms, cudaStream_t st);
 cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st);
-// All rounds in one cooperative launch (grid barrier between rounds); returns
-// cudaErrorCooperativeLaunchTooLarge and the like when it cannot run, so the
+// The walk form: one persistent launch (every block resident) in which a
+// thread goes on with the cell its processing made ready; returns an error
+// (and launches nothing) when the kernel cannot be made resident, so the
 // caller can take the per-round launches instead.
 cudaError_t launch_sca_mfd_persistent(const ScaMfdParams& p, int num_sms, cudaStream_t st);
 

@@ -186,7 +186,9 @@ __device__ __forceinline__ double weight_at(const InView& v, int64_t r, int64_t 
 // flags) are issued before the first is used, and the counter decrements go
 // out together -- a level costs a few memory round trips, not one per
 // neighbour.  The sum is still taken in the reference's window order.
-__device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, int32_t* next, int32_t* next_count) {
+// Returns the layers q whose receiving cell this call made ready (its last
+// inflow): bit q.
+__device__ __forceinline__ unsigned sca_mfd_process(const ScaMfdParams& p, int64_t i) {
     const int64_t r = i / p.cols, c = i % p.cols;
     double wq[8], sq[8];
     bool pq[8];
@@ -222,6 +224,7 @@ __device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, i
         const int pos = pos_of_layer(q);
         fd[q] = p.flags[i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1)];
     }
+    __threadfence();  // this cell's sum and flag before the counters that release its receivers
     int left[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
@@ -230,11 +233,24 @@ __device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, i
         const bool go = po[q] && dr >= 1 && dc >= 1 && dr <= p.rows - 2 && dc <= p.cols - 2 && (fd[q] & kValid);
         left[q] = go ? atomicSub(&p.cnt[dr * p.cols + dc], 1) : 0;
     }
+    unsigned ready = 0;
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        if (left[q] != 1) continue;
-        const int pos = pos_of_layer(q);
-        next[atomicAdd(next_count, 1)] = (int32_t)(i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1));
+    for (int q = 0; q < 8; q++) ready |= (left[q] == 1 ? 1u : 0u) << q;
+    return ready;
+}
+
+// the cell of layer q's receiver
+__device__ __forceinline__ int64_t receiver(const ScaMfdParams& p, int64_t i, int q) {
+    const int pos = pos_of_layer(q);
+    return i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1);
+}
+
+__device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, int32_t* next, int32_t* next_count) {
+    unsigned ready = sca_mfd_process(p, i);
+    while (ready) {
+        const int q = __ffs(ready) - 1;
+        ready &= ready - 1;
+        next[atomicAdd(next_count, 1)] = (int32_t)receiver(p, i, q);
     }
 }
 
@@ -267,63 +283,89 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdPar
     }
 }
 
-constexpr long long kBarrierBudget = 4000000000LL;  // ~2 s of SM clocks without the barrier opening
+constexpr long long kWaitBudget = 4000000000LL;  // ~2 s of SM clocks without a queued cell arriving
 
-// Grid-wide barrier of the cooperative launch: arrivals counted, the last
-// arriver opens the next generation.  Bounded: a block that waits longer than
-// the budget reports false (and sets the error flag) instead of spinning on.
-__device__ bool grid_barrier(const ScaMfdParams& p) {
-    __shared__ bool ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned int* gen = &p.barrier[1];
-        const unsigned int g = *gen;
-        __threadfence();
-        ok = true;
-        if (atomicAdd(&p.barrier[0], 1u) == gridDim.x - 1) {
-            p.barrier[0] = 0;
-            __threadfence();
-            atomicAdd(&p.barrier[1], 1u);
-        } else {
-            const long long t0 = clock64();
-            while (*gen == g) {
-                if (clock64() - t0 > kBarrierBudget || *((volatile int*)p.error_flag) != 0) {
-                    ok = false;
-                    atomicExch(p.error_flag, 1);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return ok;
+// Walk form, one persistent launch with every block resident.  A thread takes
+// a ready cell (the first frontier, then cells queued by other threads),
+// processes it, and goes on at once with a receiver this made ready -- its
+// last inflow is then final -- queuing any further ready receivers; a
+// thread's walk follows the flow down the DAG, so no round waits on the
+// slowest cell of a level.  Each cell is processed once, after all its
+// inflows (their counters), so the sums are those of the rounds.
+//   counts[0]  cells of the first frontier (list_a), from the init kernel
+//   counts[3]  claimed from list_a
+//   counts[1]  queued in list_b (each cell at most once: room for every cell)
+//   counts[2]  claimed from list_b
+//   barrier[0] pending: ready cells not yet finished, raised before a cell is
+//              queued and lowered when a walk ends -- zero exactly when every
+//              ready cell is done.
+// list_b starts filled with -1; a claimed position is waited on until its
+// cell is written (bounded: the error flag ends the launch).
+__global__ void sca_mfd_walk_setup_kernel(const ScaMfdParams p) {
+    p.barrier[0] = (unsigned int)p.counts[0];
+    p.counts[1] = 0;
+    p.counts[2] = 0;
+    p.counts[3] = 0;
 }
 
-// Every round in one launch: round k processes list k mod 3, queues into
-// list k+1 mod 3 and empties list k+2 mod 3 (processed in round k-1, filled
-// again in round k+1), so one grid barrier separates rounds.
-__global__ void __launch_bounds__(512) sca_mfd_persistent_kernel(const ScaMfdParams p) {
-    auto list = [&](int i) { return i == 0 ? p.list_a : (i == 1 ? p.list_b : p.list_c); };
-    auto count = [&](int i) { return i == 0 ? &p.counts[0] : (i == 1 ? &p.counts[1] : &p.counts[3]); };
-    unsigned long long done_cells = 0;
-    for (int k = 0;; k++) {
-        const int cur = k % 3, nxt = (k + 1) % 3, old = (k + 2) % 3;
-        const int32_t ncur = *((volatile int32_t*)count(cur));
-        const int32_t* cl = list(cur);
-        int32_t* nl = list(nxt);
-        int32_t* nc = count(nxt);
-        for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < ncur;
-             idx += (int64_t)gridDim.x * blockDim.x) {
-            sca_mfd_cell(p, cl[idx], nl, nc);
-            done_cells++;
+__device__ int64_t walk_claim(const ScaMfdParams& p, int64_t n) {
+    const int32_t a = atomicAdd(&p.counts[3], 1);
+    if (a < *((volatile int32_t*)&p.counts[0])) return p.list_a[a];
+    const int32_t b = atomicAdd(&p.counts[2], 1);
+    const long long t0 = clock64();
+    unsigned ns = 32;
+    for (;;) {
+        if (b < n) {
+            const int32_t v = *((volatile int32_t*)&p.list_b[b]);
+            if (v >= 0) return v;
         }
-        if (blockIdx.x == 0 && threadIdx.x == 0) *count(old) = 0;
-        if (!grid_barrier(p)) break;
-        if (*((volatile int32_t*)nc) == 0) break;  // the same value in every block
+        if (*((volatile unsigned int*)&p.barrier[0]) == 0) return -1;  // every ready cell done
+        if (*((volatile int*)p.error_flag) != 0) return -1;
+        if (clock64() - t0 > kWaitBudget) {
+            atomicExch(p.error_flag, 1);
+            return -1;
+        }
+        __nanosleep(ns);
+        if (ns < 1024) ns *= 2;
     }
-    if (done_cells) atomicAdd(&p.totals[1], done_cells);
+}
+
+__global__ void __launch_bounds__(kThreads) sca_mfd_walk_kernel(const ScaMfdParams p) {
+    const int64_t n = p.rows * p.cols;
+    unsigned long long done_cells = 0;
+    for (;;) {
+        int64_t cell = walk_claim(p, n);
+        if (cell < 0) break;
+        while (cell >= 0) {
+            __threadfence();  // the released inflows' sums and flags are visible
+            unsigned ready = sca_mfd_process(p, cell);
+            done_cells++;
+            const int nr = __popc(ready);
+            int64_t next = -1;
+            if (nr) {
+                const int q0 = __ffs(ready) - 1;
+                next = receiver(p, cell, q0);
+                ready &= ready - 1;
+                if (nr > 1) {
+                    __threadfence();  // what released these cells is visible to whoever takes them
+                    atomicAdd(&p.barrier[0], (unsigned int)(nr - 1));  // raised before the cells are queued
+                    const int32_t pos = atomicAdd(&p.counts[1], nr - 1);
+                    int k = 0;
+                    while (ready) {
+                        const int q = __ffs(ready) - 1;
+                        ready &= ready - 1;
+                        if (pos + k < n) atomicExch(&p.list_b[pos + k], (int32_t)receiver(p, cell, q));
+                        k++;
+                    }
+                }
+            } else {
+                atomicAdd(&p.barrier[0], 0xFFFFFFFFu);  // this walk ends: one pending cell fewer
+            }
+            cell = next;
+        }
+    }
+    const unsigned dc = __reduce_add_sync(__activemask(), (unsigned)done_cells);
+    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1 && dc) atomicAdd(&p.totals[1], (unsigned long long)dc);
 }
 
 __global__ void __launch_bounds__(kThreads) sca_mfd_output_kernel(const ScaMfdParams p) {
@@ -364,15 +406,17 @@ cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms,
 
 cudaError_t launch_sca_mfd_persistent(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sca_mfd_persistent_kernel, 512, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sca_mfd_walk_kernel, kThreads, 0);
     if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorCooperativeLaunchTooLarge;
-    if (per_sm > 2) per_sm = 2;  // fewer arrivals per barrier
-    if ((e = cudaMemsetAsync(p.barrier, 0, 2 * sizeof(unsigned int), st)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(&p.counts[3], 0, sizeof(int32_t), st)) != cudaSuccess) return e;
-    void* args[] = {(void*)&p};
-    return cudaLaunchCooperativeKernel((const void*)sca_mfd_persistent_kernel, dim3((unsigned)(num_sms * per_sm)),
-                                       dim3(512), args, 0, st);
+    if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+    const int64_t n = p.rows * p.cols;
+    if ((e = cudaMemsetAsync(p.list_b, 0xFF, (size_t)n * sizeof(int32_t), st)) != cudaSuccess) return e;
+    sca_mfd_walk_setup_kernel<<<1, 1, 0, st>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // every block resident: a thread waiting for a queued cell never waits on
+    // a block that has not started
+    sca_mfd_walk_kernel<<<(unsigned)(num_sms * per_sm), kThreads, 0, st>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
