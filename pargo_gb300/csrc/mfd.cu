@@ -16,8 +16,9 @@
 // adds sca(n) w(n -> cell) for each inflow n whose degree is 0 at that moment
 // -- a source, or an earlier cell that pulled all its own inflows ("done").
 // Here the same sums are evaluated in topological order: a cell is processed
-// once every inflow from a valid work cell is processed (frontier rounds with
-// in-degree counters); it then adds, in the reference's window order and in
+// once every inflow from a valid work cell is processed (in-degree counters;
+// the thread that releases a cell's last inflow processes it next, see the
+// walk form below); it then adds, in the reference's window order and in
 // FP64 with separately rounded products and sums, the inflows the sweep pulls
 // (source, or earlier in raster order and done), so with the same weights the
 // result equals the reference's bit for bit.  Inflows from cells that are
