@@ -24,8 +24,6 @@
 // result equals the reference's bit for bit.  Inflows from cells that are
 // never processed (the ring, nodata) are never pulled.
 
-#include <cuda/atomic>
-
 #include "common.cuh"
 #include "kernels.h"
 
@@ -227,20 +225,14 @@ __device__ __forceinline__ unsigned sca_mfd_process(const ScaMfdParams& p, int64
         const int pos = pos_of_layer(q);
         fd[q] = p.flags[i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1)];
     }
-    // The counter decrements release this cell's sum and flag (acq_rel: the
-    // decrement that empties a counter also acquires what every earlier
-    // inflow released, so its thread may process that receiver next).
+    __threadfence();  // this cell's sum and flag before the counters that release its receivers
     int left[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) {
         const int pos = pos_of_layer(q);
         const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
         const bool go = po[q] && dr >= 1 && dc >= 1 && dr <= p.rows - 2 && dc <= p.cols - 2 && (fd[q] & kValid);
-        left[q] = 0;
-        if (go) {
-            cuda::atomic_ref<int32_t, cuda::thread_scope_device> cnt(p.cnt[dr * p.cols + dc]);
-            left[q] = cnt.fetch_sub(1, cuda::memory_order_acq_rel);
-        }
+        left[q] = go ? atomicSub(&p.cnt[dr * p.cols + dc], 1) : 0;
     }
     unsigned ready = 0;
 #pragma unroll
@@ -325,8 +317,7 @@ __device__ int64_t walk_claim(const ScaMfdParams& p, int64_t n) {
     unsigned ns = 32;
     for (;;) {
         if (b < n) {
-            const int32_t v = cuda::atomic_ref<int32_t, cuda::thread_scope_device>(p.list_b[b]).load(
-                cuda::memory_order_acquire);
+            const int32_t v = *((volatile int32_t*)&p.list_b[b]);
             if (v >= 0) return v;
         }
         if (*((volatile unsigned int*)&p.barrier[0]) == 0) return -1;  // every ready cell done
@@ -347,6 +338,7 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_walk_kernel(const ScaMfdPara
         int64_t cell = walk_claim(p, n);
         if (cell < 0) break;
         while (cell >= 0) {
+            __threadfence();  // the released inflows' sums and flags are visible
             unsigned ready = sca_mfd_process(p, cell);
             done_cells++;
             const int nr = __popc(ready);
@@ -356,16 +348,14 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_walk_kernel(const ScaMfdPara
                 next = receiver(p, cell, q0);
                 ready &= ready - 1;
                 if (nr > 1) {
+                    __threadfence();  // what released these cells is visible to whoever takes them
                     atomicAdd(&p.barrier[0], (unsigned int)(nr - 1));  // raised before the cells are queued
                     const int32_t pos = atomicAdd(&p.counts[1], nr - 1);
                     int k = 0;
                     while (ready) {
                         const int q = __ffs(ready) - 1;
                         ready &= ready - 1;
-                        // a release store: the taker's acquire load sees what released the cell
-                        if (pos + k < n)
-                            cuda::atomic_ref<int32_t, cuda::thread_scope_device>(p.list_b[pos + k])
-                                .store((int32_t)receiver(p, cell, q), cuda::memory_order_release);
+                        if (pos + k < n) atomicExch(&p.list_b[pos + k], (int32_t)receiver(p, cell, q));
                         k++;
                     }
                 }
