@@ -48,6 +48,9 @@ FALLBACK_HBM_GBS = 6800.0
 # from its ncu capture on 8192^2 (301.3 MB + 289.3 MB over 67108864 cells)
 FOCAL_DRAM_BYTES_PER_CELL = (301.330688e6 + 289.264128e6) / 67108864   # tiled kernel, 8192^2 ncu capture
 STRIP_DRAM_BYTES_PER_CELL = (289.425152e6 + 284.340224e6) / 67108864   # strip walk, 8192^2 ncu capture
+# dram__bytes_read.sum + dram__bytes_write.sum of one batch_strip_kernel launch
+# on the batch512 workload (one-pass ncu capture of that launch)
+BATCH_STRIP_DRAM_BYTES_512 = 4283454464 + 4787671296
 # dram__bytes_read.sum + dram__bytes_write.sum of one fill_tiles_kernel<true>
 # launch on the default 8192^2 workload (one-pass ncu capture of that launch)
 FILL_DRAM_BYTES_8192 = 2444316416 + 757925632
@@ -467,7 +470,10 @@ def run_batch(args, ws, rank, local):
                                "Hurst U(0.6, 0.9), %d cells" % cells,
                    "l2": "inputs larger than L2 (%.1f GB per step)" % (cells * 9 / 1e9)},
         "roofline": {"bound": "hbm", "kernel": "batch_strip_kernel (+ batch_strip_fixup_kernel)", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind, "traffic": None},
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind,
+                     "traffic": BATCH_STRIP_DRAM_BYTES_512,
+                     "traffic_source": "ncu capture of one batch_strip_kernel launch of this workload",
+                     "algorithmic_bytes": cells * 9},
         "gpu_launches": 2 * args.steps, "plain_gpu_launches": args.steps * 512, "clocks": clk,
     }
 
