@@ -34,6 +34,7 @@ struct pargo_ctx {
     cudaStream_t own = nullptr;  // stream for captured fill rounds
     cudaEvent_t ev_a = nullptr, ev_b = nullptr;  // stream hand-off
     cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;  // timing of the fill rounds
+    cudaEvent_t ev_band[8] = {nullptr};  // pipeline: row bands computed, their host copies may start
     // grow-only device scratch slots
     struct Slot {
         void* p = nullptr;
@@ -333,6 +334,15 @@ pargo_status stage_out(pargo_ctx* ctx, pargo_raster* r, int slot_id, Staged* s) 
     if (!d) return cuda_fail(ctx, e, "staging output");
     s->out = OutView{d, dp, r->dtype, r->nodata};
     s->dpitch = dp;
+    return PARGO_OK;
+}
+
+// Rows [r0, r1) of a staged host output back to the host.
+pargo_status unstage_rows(pargo_ctx* ctx, const Staged& s, int64_t r0, int64_t r1, cudaStream_t st) {
+    if (!s.host || r1 <= r0) return PARGO_OK;
+    const pargo_raster* r = s.user;
+    CU(ctx, cudaMemcpy2DAsync((char*)r->data + r0 * pitch_of(r), pitch_of(r), s.out.base + r0 * s.dpitch, s.dpitch,
+                              row_bytes(r), r1 - r0, cudaMemcpyDeviceToHost, st));
     return PARGO_OK;
 }
 
@@ -813,6 +823,8 @@ pargo_status pargo_destroy(pargo_ctx* ctx) {
     if (ctx->ev_b) cudaEventDestroy(ctx->ev_b);
     if (ctx->ev_t0) cudaEventDestroy(ctx->ev_t0);
     if (ctx->ev_t1) cudaEventDestroy(ctx->ev_t1);
+    for (cudaEvent_t& ev : ctx->ev_band)
+        if (ev) cudaEventDestroy(ev);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
     return PARGO_OK;
@@ -1438,7 +1450,30 @@ pargo_status pargo_hydro_pipeline(pargo_ctx* ctx, const pargo_raster* dem, pargo
         if ((st = make_tma_map(ctx, &map, p.w, p.rows, p.cols, q.wpitch, focal64_tile_rows() + 2, focal64_box_cols(),
                                true)) != PARGO_OK)
             return st;
-        CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s));
+        if (!sca && (sw.host || ss.host || sd.host)) {
+            // Host outputs: the raster in row bands, each band's copies to the
+            // host on the context's own stream as soon as the band is written,
+            // so they overlap the following bands' kernel.
+            constexpr int kBands = 8;
+            const int64_t tr = focal64_tile_rows();
+            const int64_t band = ((p.rows + kBands - 1) / kBands + tr - 1) / tr * tr;
+            int b = 0;
+            for (int64_t r0 = 0; r0 < p.rows; r0 += band, b++) {
+                const int64_t r1 = std::min(p.rows, r0 + band);
+                CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s, r0, r1));
+                if (!ctx->ev_band[b]) CU(ctx, cudaEventCreateWithFlags(&ctx->ev_band[b], cudaEventDisableTiming));
+                CU(ctx, cudaEventRecord(ctx->ev_band[b], s));
+                CU(ctx, cudaStreamWaitEvent(ctx->own, ctx->ev_band[b], 0));
+                if (wdem && (st = unstage_rows(ctx, sw, r0, r1, ctx->own)) != PARGO_OK) return st;
+                if (slope && (st = unstage_rows(ctx, ss, r0, r1, ctx->own)) != PARGO_OK) return st;
+                if (d8 && (st = unstage_rows(ctx, sd, r0, r1, ctx->own)) != PARGO_OK) return st;
+            }
+            CU(ctx, cudaEventRecord(ctx->ev_b, ctx->own));
+            CU(ctx, cudaStreamWaitEvent(s, ctx->ev_b, 0));
+            sw.host = ss.host = sd.host = false;  // copied back already
+        } else {
+            CU(ctx, launch_focal64_tma(&map, q, ctx->num_sms, s));
+        }
     }
     if (sca) {
         ScaParams q{};

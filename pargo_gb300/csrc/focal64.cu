@@ -19,6 +19,8 @@
 
 #include <string.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 #include "tma.cuh"
@@ -314,7 +316,8 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
 
 __global__ void __launch_bounds__(kThreads, 4) focal64_tma_kernel(const __grid_constant__ CUtensorMap map,
                                                                   const __grid_constant__ Focal64Params P,
-                                                                  int64_t ntx, int64_t ntiles, int klo, int khi) {
+                                                                  int64_t ntx, int64_t t_begin, int64_t ntiles,
+                                                                  int klo, int khi) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar[2];
     const int tid = threadIdx.x;
@@ -325,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, 4) focal64_tma_kernel(const __grid_c
         mbar_fence_init();
     }
     __syncthreads();
-    int64_t t = blockIdx.x;
+    int64_t t = t_begin + blockIdx.x;  // tiles t_begin .. ntiles-1
     if (tid == 0 && t < ntiles) {
         mbar_arrive_expect_tx(&bar[0], kStageBytes);
         tma_load_2d(smem, &map, (int32_t)((t % ntx) * kTW - 2), (int32_t)((t / ntx) * kTH - 1), &bar[0]);
@@ -370,10 +373,14 @@ int key_hi(double x) {
 int focal64_tile_rows() { return kTH; }
 int focal64_box_cols() { return kBoxW; }
 
-cudaError_t launch_focal64_tma(const CUtensorMap* map, const Focal64Params& p, int num_sms, cudaStream_t s) {
+cudaError_t launch_focal64_tma(const CUtensorMap* map, const Focal64Params& p, int num_sms, cudaStream_t s,
+                               int64_t row_begin, int64_t row_end) {
     const int64_t ntx = (p.f.cols + kTW - 1) / kTW, nty = (p.f.rows + kTH - 1) / kTH;
-    const int64_t ntiles = ntx * nty;
-    if (ntiles == 0) return cudaSuccess;
+    // tile rows covering output rows [row_begin, row_end); row_begin is a multiple of kTH
+    const int64_t ty0 = row_begin / kTH;
+    const int64_t ty1 = row_end < 0 ? nty : std::min(nty, (row_end + kTH - 1) / kTH);
+    const int64_t t_begin = ty0 * ntx, ntiles = ty1 * ntx;
+    if (ntiles <= t_begin) return cudaSuccess;
     const size_t smem = 2 * kStageStride;
     cudaError_t e = cudaFuncSetAttribute(focal64_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -382,14 +389,14 @@ cudaError_t launch_focal64_tma(const CUtensorMap* map, const Focal64Params& p, i
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     int64_t grid = (int64_t)num_sms * per_sm;
-    if (grid > ntiles) grid = ntiles;
+    if (grid > ntiles - t_begin) grid = ntiles - t_begin;
     // band of the levels' nodata as high-word keys (conservative superset)
     int klo = key_hi(p.f.nd6d.lo), khi = key_hi(p.f.nd6d.hi);
     if (!(p.f.nd6d.lo <= p.f.nd6d.hi)) {
         klo = 1;
         khi = 0;  // empty band
     }
-    focal64_tma_kernel<<<(unsigned)grid, kThreads, smem, s>>>(*map, p, ntx, ntiles, klo, khi);
+    focal64_tma_kernel<<<(unsigned)grid, kThreads, smem, s>>>(*map, p, ntx, t_begin, ntiles, klo, khi);
     return cudaGetLastError();
 }
 

@@ -111,7 +111,10 @@ struct Focal64Params {
     int64_t dem_pitch;
     int dem_f64;
 };
-cudaError_t launch_focal64_tma(const CUtensorMap* map, const Focal64Params& p, int num_sms, cudaStream_t s);
+// Output rows [row_begin, row_end) (row_end < 0: to the last row); row_begin
+// must be a multiple of focal64_tile_rows().
+cudaError_t launch_focal64_tma(const CUtensorMap* map, const Focal64Params& p, int num_sms, cudaStream_t s,
+                               int64_t row_begin = 0, int64_t row_end = -1);
 int focal64_tile_rows();
 int focal64_box_cols();
 
