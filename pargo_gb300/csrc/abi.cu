@@ -2280,7 +2280,19 @@ static pargo_status grad_impl(pargo_ctx* ctx, const pargo_raster* z, const pargo
     p.gz = (float*)sg.out.base;
     p.gz_pitch = sg.out.pitch;
     p.loss = dloss;
-    CU(ctx, launch_slope_loss_grad(p, mode, s));
+    p.error_flag = ctx->d_error;
+    if (tma_ok(p.z) && (mode != 0 || tma_ok(p.zref))) {
+        CUtensorMap mz, mr;
+        if ((st = make_tma_map(ctx, &mz, p.z.base, p.rows, p.cols, p.z.pitch, grad_box_rows(), grad_box_cols())) !=
+            PARGO_OK)
+            return st;
+        if (mode == 0 && (st = make_tma_map(ctx, &mr, p.zref.base, p.rows, p.cols, p.zref.pitch, grad_box_rows(),
+                                            grad_box_cols())) != PARGO_OK)
+            return st;
+        CU(ctx, launch_slope_loss_grad_tma(&mz, &mr, p, mode, s));
+    } else {
+        CU(ctx, launch_slope_loss_grad(p, mode, s));
+    }
     if ((st = unstage_out(ctx, sg, s)) != PARGO_OK) return st;
     const bool sync = sz.host || so.host || sg.host || loss;
     if (loss) {

@@ -24,6 +24,7 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace pargo {
 
@@ -154,12 +155,151 @@ __global__ void __launch_bounds__(kThreads) slope_grad_kernel(const GradParams p
     }
 }
 
+// TMA-staged form of the same computation, for 16-byte aligned float32
+// inputs: one thread loads the block's z (and z_ref) with its two-cell halo
+// as a 2-D box (72 x 36 floats from column x0 - 4: the box's x coordinate
+// stays 16-byte aligned), the block turns nodata into NaN in place four
+// values at a time, and the A/B and gather phases run as above on the boxes.
+// The per-element address arithmetic and bounds checks of the staging (a
+// quarter of the kernel's instructions; it is issue bound) go away.  Cells
+// outside the raster load as 0 instead of NaN: only ring cells and cells
+// beyond the raster have them in their windows, and those have no slope.
+constexpr int kTBW = kBW + 8;                 // box columns: x0-4 .. x0+67
+constexpr int kTBH = kZH;                     // box rows: y0-2 .. y0+33
+constexpr int kBoxFloats = kTBW * kTBH;
+constexpr int kBoxBytes = kBoxFloats * 4;     // 10368: a multiple of 128
+constexpr long long kWaitBudget = 4000000000LL;
+
+__global__ void __launch_bounds__(kThreads) slope_grad_tma_kernel(const __grid_constant__ CUtensorMap mz,
+                                                                  const __grid_constant__ CUtensorMap mr,
+                                                                  const GradParams p, int mode, int64_t nbx) {
+    extern __shared__ __align__(1024) unsigned char grad_smem[];
+    float* bz = reinterpret_cast<float*>(grad_smem);
+    float* br = bz + kBoxFloats;
+    __shared__ float sa[kAH][kAW + 1];
+    __shared__ float sb[kAH][kAW + 1];
+    __shared__ double red[kThreads / 32];
+    __shared__ __align__(8) uint64_t bar;
+    const int tid = threadIdx.x;
+    const int64_t by = blockIdx.x / nbx, bx = blockIdx.x % nbx;
+    const int64_t y0 = by * kBH, x0 = bx * kBW;
+    const float kNaN = __int_as_float(0x7FC00000);
+    if (tid == 0) {
+        tma_prefetch_desc(&mz);
+        mbar_init(&bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0) {
+        mbar_arrive_expect_tx(&bar, mode == 0 ? 2 * kBoxBytes : kBoxBytes);
+        tma_load_2d(bz, &mz, (int32_t)(x0 - 4), (int32_t)(y0 - 2), &bar);
+        if (mode == 0) tma_load_2d(br, &mr, (int32_t)(x0 - 4), (int32_t)(y0 - 2), &bar);
+    }
+    if (!mbar_wait_bounded(&bar, 0, kWaitBudget)) {
+        if (tid == 0 && p.error_flag) atomicExch(p.error_flag, 1);
+        return;
+    }
+    // nodata (Eps 1e-7) as NaN, four values at a time
+    {
+        float4* z4 = reinterpret_cast<float4*>(bz);
+        const int n4 = (mode == 0 ? 2 : 1) * kBoxFloats / 4;  // br follows bz
+        for (int i = tid; i < n4; i += kThreads) {
+            float4 v = z4[i];
+            v.x = p.nd7f.has(v.x) ? kNaN : v.x;
+            v.y = p.nd7f.has(v.y) ? kNaN : v.y;
+            v.z = p.nd7f.has(v.z) ? kNaN : v.z;
+            v.w = p.nd7f.has(v.w) ? kNaN : v.w;
+            z4[i] = v;
+        }
+    }
+    __syncthreads();
+    float lsum = 0.0f;
+    for (int i = tid; i < kAH * kAW; i += kThreads) {
+        const int a = i / kAW, b = i % kAW;  // cell (y0 - 1 + a, x0 - 1 + b); its window starts at box (a, b + 2)
+        const int64_t r = y0 - 1 + a, c = x0 - 1 + b;
+        float A = 0.0f, B = 0.0f;
+        const bool inner = r >= 1 && c >= 1 && r <= p.rows - 2 && c <= p.cols - 2;
+        const float* wz = bz + a * kTBW + b + 2;
+        float nx, ny;
+        numerators(wz, kTBW, nx, ny);
+        const float q = __fmaf_rn(nx, nx, __fmul_rn(ny, ny));
+        if (inner && wz[kTBW + 1] == wz[kTBW + 1] && q == q) {  // centre and neighbours valid
+            const float s = horn_slope(nx, ny, p.k_fd);
+            float g = 0.0f;
+            bool have = true;
+            if (mode == 0) {
+                const float* wr = br + a * kTBW + b + 2;
+                float mx, my;
+                numerators(wr, kTBW, mx, my);
+                const float sref = horn_slope(mx, my, p.k_fd);
+                have = wr[kTBW + 1] == wr[kTBW + 1] && sref == sref;
+                if (have) {
+                    const float d = s - sref;
+                    g = 2.0f * d;
+                    if (a >= 1 && b >= 1 && a <= kBH && b <= kBW) lsum += d * d;
+                }
+            } else {
+                g = load_f32(p.gslope, r, c);
+            }
+            if (have && q > 0.0f) {  // subgradient 0 at zero slope
+                const float f = g * p.k_fd * rsqrtf(q);
+                A = f * nx;
+                B = f * ny;
+            }
+        }
+        sa[a][b] = A;
+        sb[a][b] = B;
+    }
+    __syncthreads();
+    for (int i = tid; i < kBH * kBW; i += kThreads) {
+        const int a = i / kBW, b = i % kBW;
+        const int64_t r = y0 + a, c = x0 + b;
+        if (r >= p.rows || c >= p.cols) continue;
+        const float* A0 = &sa[a][b];
+        const float* B0 = &sb[a][b];
+        constexpr int L = kAW + 1;
+        const float ga = (-A0[2 * L + 2] + A0[2 * L]) + 2.0f * (-A0[L + 2] + A0[L]) + (-A0[2] + A0[0]);
+        const float gb = (B0[2 * L + 2] + 2.0f * B0[2 * L + 1] + B0[2 * L]) - (B0[2] + 2.0f * B0[1] + B0[0]);
+        reinterpret_cast<float*>(reinterpret_cast<char*>(p.gz) + r * p.gz_pitch)[c] = ga + gb;
+    }
+    if (mode == 0 && p.loss) {
+        float v = lsum;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) red[tid >> 5] = (double)v;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kThreads / 32; w++) t += red[w];
+            if (t != 0.0) atomicAdd(p.loss, t);
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_slope_loss_grad(const GradParams& p, int mode, cudaStream_t st) {
     const int64_t nby = (p.rows + kBH - 1) / kBH, nbx = (p.cols + kBW - 1) / kBW;
     if (nby * nbx == 0) return cudaSuccess;
     slope_grad_kernel<<<(unsigned)(nby * nbx), kThreads, 0, st>>>(p, mode, nbx);
+    return cudaGetLastError();
+}
+
+}  // namespace pargo
+
+namespace pargo {
+
+int grad_box_rows() { return kTBH; }
+int grad_box_cols() { return kTBW; }
+
+cudaError_t launch_slope_loss_grad_tma(const CUtensorMap* mz, const CUtensorMap* mr, const GradParams& p, int mode,
+                                       cudaStream_t st) {
+    const int64_t nby = (p.rows + kBH - 1) / kBH, nbx = (p.cols + kBW - 1) / kBW;
+    if (nby * nbx == 0) return cudaSuccess;
+    const size_t smem = 2 * (size_t)kBoxBytes;
+    cudaError_t e = cudaFuncSetAttribute(slope_grad_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    slope_grad_tma_kernel<<<(unsigned)(nby * nbx), kThreads, smem, st>>>(*mz, mode == 0 ? *mr : *mz, p, mode, nbx);
     return cudaGetLastError();
 }
 

@@ -276,7 +276,14 @@ struct GradParams {
     int64_t gz_pitch;
     OutView slope;
     double* loss;           // device accumulator (may be null)
+    int* error_flag;        // a bounded wait for the staged boxes gave up (TMA form)
 };
 cudaError_t launch_slope_loss_grad(const GradParams& p, int mode, cudaStream_t st);
+// TMA form: mz (and, for mode 0, mr) are tensor maps of z (z_ref) with a
+// grad_box_cols() x grad_box_rows() box; inputs float32, 16-byte aligned rows.
+int grad_box_rows();
+int grad_box_cols();
+cudaError_t launch_slope_loss_grad_tma(const CUtensorMap* mz, const CUtensorMap* mr, const GradParams& p, int mode,
+                                       cudaStream_t st);
 
 }  // namespace pargo
