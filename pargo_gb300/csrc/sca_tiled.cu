@@ -206,9 +206,13 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
             if (!(S.flag(i) & 8)) continue;
             int cur = i;
             for (;;) {
-                const unsigned long long tot = 1 + (unsigned long long)atomicAdd(&S.acc[cur], (typename Smem::Acc)0);
-                const unsigned fl = S.flag_sync(cur);
-                const bool bad = (fl & 2) || (fl & 16);
+                // Every child of cur added its total and flag before the
+                // fenced decrement that released cur, and nothing writes them
+                // any more: plain (volatile) reads see the final values.
+                const unsigned long long tot =
+                    1 + (unsigned long long)((volatile typename Smem::Acc*)S.acc)[cur];
+                const unsigned fl = (((volatile uint32_t*)S.flagw)[cur >> 2] >> (8 * (cur & 3))) & 0xFFu;
+                const bool bad = (fl & 18u) != 0;
                 S.acc[cur] = (typename Smem::Acc)tot;
                 S.set_flag(cur, 4u | (bad ? 16u : 0u));
                 ndone++;
@@ -225,6 +229,22 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
         atomicAdd(&S.cnt[1], ndone);
         __syncthreads();
         if (!FINAL) {
+            // Parents become the path's last cell by pointer jumping (a
+            // parent pointer is replaced by its parent's while that is a
+            // cell): 12 rounds cover any acyclic path of a 64 x 64 tile, and
+            // a pointer is an ancestor of its cell at every moment, so the
+            // rounds need no read/write separation.  The last cell keeps its
+            // own -1 or -2.  lpar is rebuilt by the final pass.
+#pragma unroll 1
+            for (int round = 0; round < 12; round++) {
+                for (int i = tid; i < kCells; i += kThreads) {
+                    const int q = S.lpar[i];
+                    if (q < 0) continue;
+                    const int q2 = ((volatile int16_t*)S.lpar)[q];
+                    if (q2 >= 0) S.lpar[i] = (int16_t)q2;
+                }
+                __syncthreads();
+            }
             // Border cells: the exit each in-tile path reaches; exits record
             // their in-tile totals and the entry they feed.
             for (int i = tid; i < kCells; i += kThreads) {
@@ -235,8 +255,7 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 const int64_t node = t * kScaSlots + sl;
                 int32_t ex = -1, ys = -1;
                 if (S.flag(i) & 4) {  // completed: its path is acyclic
-                    int cur = i;
-                    for (int step = 0; step < kCells && S.lpar[cur] >= 0; step++) cur = S.lpar[cur];
+                    const int cur = S.lpar[i] >= 0 ? S.lpar[i] : i;  // the path's last cell (pointers jumped above)
                     if (S.lpar[cur] == -2) {
                         const int er = cur / kT, ec = cur % kT;
                         ex = (int32_t)(t * kScaSlots + slot_of(er, ec, th, tw));
