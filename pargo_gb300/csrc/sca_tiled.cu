@@ -218,19 +218,6 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 ndone++;
                 const int par = S.lpar[cur];
                 if (par < 0) break;
-                // cur is par's last child still to fold in when par's count
-                // reads 1 (counts only fall, and cur has not counted itself
-                // off): no other thread touches par any more, so the walk goes
-                // on without the atomics -- down a chain of single children,
-                // the common case in filled lakes, each step is plain.
-                const unsigned dg = (((volatile uint32_t*)S.degw)[par >> 2] >> (8 * (par & 3))) & 0xFFu;
-                if (dg == 1u) {
-                    __threadfence_block();  // the other children's totals, added before their decrements
-                    S.acc[par] = (typename Smem::Acc)(((volatile typename Smem::Acc*)S.acc)[par] + tot);
-                    if (bad) S.set_flag(par, 16u);
-                    cur = par;
-                    continue;
-                }
                 atomicAdd(&S.acc[par], (typename Smem::Acc)tot);
                 if (bad) S.set_flag(par, 16u);
                 __threadfence_block();
