@@ -85,13 +85,27 @@ __device__ __forceinline__ int64_t add_gap(int64_t k, double gap) {
     return dkey(__dadd_rn(dval(k), gap));
 }
 
-// DEM value (float32 or float64 input) and its nodata test (Eps 1e-6).
-__device__ __forceinline__ double dem_at(const FillParams& p, int64_t r, int64_t c) {
+// The DEM value at (r, c) as an order-preserving key of its double value,
+// and its nodata test (Eps 1e-6) -- both from the bits: a float DEM widened
+// to double and compared in double would cost conversions and compares on
+// the FP64 pipe (a narrow pipe on this part) for every cell a visit loads.
+__device__ __forceinline__ int64_t dem_key(const FillParams& p, int64_t r, int64_t c) {
     const char* row = reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch;
-    return p.dem_f64 ? reinterpret_cast<const double*>(row)[c] : (double)reinterpret_cast<const float*>(row)[c];
+    return p.dem_f64 ? dkey(reinterpret_cast<const double*>(row)[c]) : fkey64(reinterpret_cast<const float*>(row)[c]);
 }
-__device__ __forceinline__ bool dem_nodata(const FillParams& p, double z) {
-    return p.dem_f64 ? p.nd6d.has(z) : p.nd6f.has((float)z);
+__device__ __forceinline__ bool dem_is_nodata(const FillParams& p, int64_t r, int64_t c) {
+    const char* row = reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch;
+    if (!p.dem_f64) return p.nd6f.has(reinterpret_cast<const float*>(row)[c]);
+    const int64_t k = dkey(reinterpret_cast<const double*>(row)[c]);
+    return k >= dkey(p.nd6d.lo) && k <= dkey(p.nd6d.hi);  // an empty band has lo > hi: its keys too
+}
+
+// A level into a filled-DEM output, nodata levels (+inf) as the output's
+// nodata; float output rounded on the integer pipes.
+__device__ __forceinline__ void put_level(const OutView& o, int64_t r, int64_t c, double w, bool nd, float nd_f) {
+    char* row = o.base + r * o.pitch;
+    if (o.dtype == PARGO_F32) reinterpret_cast<float*>(row)[c] = nd ? nd_f : dbl2flt_rn(w);
+    else put_value(o, r, c, nd ? o.nodata : w);
 }
 
 // Tile bookkeeping: every ring slot empty, every tile idle with no halo
@@ -125,19 +139,19 @@ __global__ void fill_init_kernel(const FillParams p, FillScratch s) {
             double w = INFINITY;
             const bool inner = r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
             if (inner) {
-                const double z = dem_at(p, r, c);
-                if (!dem_nodata(p, z)) {
+                if (!dem_is_nodata(p, r, c)) {
+                    const int64_t kz = dem_key(p, r, c);
                     w = p.init_level;
-                    if (p.init_level > z) {
+                    if (dkey(p.init_level) > kz) {
                         bool outlet = false;
                         for (int a = -1; a <= 1; a++)
                             for (int b = -1; b <= 1; b++) {
                                 const int64_t rr = r + a, cc = c + b;
                                 const bool ring = rr <= 0 || cc <= 0 || rr >= p.rows - 1 || cc >= p.cols - 1;
-                                if (ring || dem_nodata(p, dem_at(p, rr, cc))) outlet = true;
+                                if (ring || dem_is_nodata(p, rr, cc)) outlet = true;
                             }
                         if (outlet) {
-                            w = z;
+                            w = dval(kz);  // the DEM value itself, as a double
                             s.halo_chg[((r / kT) * p.tiles_x + c / kT) * 5 + 4] = kHaloAll;
                         }
                     }
@@ -353,18 +367,18 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
                 if (i < kH * kH) lv[(i / kH) * kLS + i % kH] = dkey(wv[q]);
             }
             // DEM keys; kKeyInf where a level never moves (the raster's ring, beyond the raster)
-            double zv[kZPer];
+            int64_t zk[kZPer];
 #pragma unroll
             for (int q = 0; q < kZPer; q++) {
                 const int i = tid + q * kThreads;
                 const int64_t gr = y0 + 1 + i / kT, gc = x0 + 1 + i % kT;
-                zv[q] = INFINITY;
-                if (gr > 0 && gc > 0 && gr < p.rows - 1 && gc < p.cols - 1) zv[q] = dem_at(p, gr, gc);
+                zk[q] = kKeyInf;
+                if (gr > 0 && gc > 0 && gr < p.rows - 1 && gc < p.cols - 1) zk[q] = dem_key(p, gr, gc);
             }
 #pragma unroll
             for (int q = 0; q < kZPer; q++) {
                 const int i = tid + q * kThreads;
-                zs[(i / kT) * kZS + i % kT] = dkey(zv[q]);
+                zs[(i / kT) * kZS + i % kT] = zk[q];
             }
         } else if (tid < 4 * kH - 4) {
             // The same tile again: only its halo can have moved (this CTA
@@ -542,14 +556,19 @@ __global__ void __launch_bounds__(kThreads, 8) fill_tiles_kernel(const FillParam
     }
 }
 
+__device__ __forceinline__ bool level_is_inf(double w) {
+    return (__double_as_longlong(w) & 0x7FFFFFFFFFFFFFFFLL) == 0x7FF0000000000000LL;
+}
+
 __global__ void fill_finish_kernel(const FillParams p, const OutView out, unsigned long long* raised) {
+    const float nd_f = (float)out.nodata;
     unsigned long long cnt = 0;
     for (int64_t r = blockIdx.y; r < p.rows; r += gridDim.y) {
         for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < p.cols; c += (int64_t)gridDim.x * blockDim.x) {
             const double w = p.w[r * p.w_stride + c];
-            const bool nd = isinf(w);
-            if (!nd && w > dem_at(p, r, c)) cnt++;
-            put_value(out, r, c, nd ? out.nodata : w);
+            const bool nd = level_is_inf(w);
+            if (!nd && dkey(w) > dem_key(p, r, c)) cnt++;
+            put_level(out, r, c, w, nd, nd_f);
         }
     }
     cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
@@ -601,9 +620,9 @@ __global__ void fill_mosaic_finish_kernel(const FillParams p, const FillBatchIte
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t r = i / it.cols, c = i - r * it.cols;
         const double w = p.w[(it.oy + r) * p.w_stride + it.ox + c];
-        const bool nd = isinf(w);
-        if (!nd && w > dem_at(p, it.oy + r, it.ox + c)) cnt++;
-        put_value(it.out, r, c, nd ? it.out.nodata : w);
+        const bool nd = level_is_inf(w);
+        if (!nd && dkey(w) > dem_key(p, it.oy + r, it.ox + c)) cnt++;
+        put_level(it.out, r, c, w, nd, (float)it.out.nodata);
     }
     cnt = __reduce_add_sync(0xffffffffu, (unsigned)cnt);
     if (raised && (threadIdx.x & 31) == 0 && cnt) atomicAdd(raised, cnt);
