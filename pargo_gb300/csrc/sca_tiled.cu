@@ -77,30 +77,39 @@ __device__ __forceinline__ int slot_of(int lr, int lc, int th, int tw) {
     return -1;
 }
 
-// Shared state of one tile.  In-degrees (at most 8) and flags are bytes
-// packed four to a word: a walker decrements a degree by an atomic subtract
-// on the word (a byte is at least 1 when decremented, so nothing borrows from
-// its neighbours) and sets flags by atomic OR.  Flag bits: 1 valid work cell,
-// 2 "bad" (a non-source inflow follows it in raster order), 4 completed,
-// 8 in-tile leaf, 16 some cell of its subtree is bad.  In-tile sums fit 32
-// bits in the first pass; the final pass adds inflows from other tiles.
+// Shared state of one tile.  Each cell's accumulator word packs, from the
+// top: a 4-bit count of in-tile children not yet folded in, a 4-bit count of
+// folded children whose subtree holds a "bad" cell, and the sum of the folded
+// subtree sizes (plus, in the final pass, the inflow from other tiles).  A
+// child folds itself into its parent with one atomic add (its size, one more
+// bad child if its subtree is bad, one child fewer) and the return value
+// tells it whether it was the last child; the last one continues the walk
+// from the value it computed, so no walk step waits for another read.  A
+// completed cell's word is rewritten as 0xF in the count field (no real count
+// reaches 15: a cell has at most 8 children), its subtree-bad bit and its
+// subtree size.  First pass: 32-bit words (4 + 4 + 24 bits; an in-tile sum is
+// at most 4096); final pass: 64-bit (4 + 4 + 56).  Static flags are bytes
+// packed four to a word, written before the walk: 1 valid work cell, 2 "bad"
+// (a non-source inflow follows it in raster order), 8 in-tile leaf, 16 an
+// inflow from another tile was not pulled.
 template <bool FINAL>
 struct TileSmem {
     using Acc = typename std::conditional<FINAL, unsigned long long, unsigned int>::type;
+    static constexpr int kDegShift = FINAL ? 60 : 28;
+    static constexpr int kBadShift = FINAL ? 56 : 24;
+    static constexpr Acc kSum = ((Acc)1 << kBadShift) - 1;
+    static constexpr Acc kOne = (Acc)1 << kDegShift;   // one child in the count field
+    static constexpr Acc kBadOne = (Acc)1 << kBadShift;
+    static constexpr Acc kDone = (Acc)0xF << kDegShift;
     int8_t cd[kH * kH];          // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
     int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
-    uint32_t degw[kCells / 4];   // in-tile children not yet folded in, a byte per cell
     Acc acc[kCells];
-    uint32_t flagw[kCells / 4];  // a byte of flags per cell
+    uint32_t flagw[kCells / 4];  // a byte of static flags per cell
     unsigned long long cnt[3];   // valid, completed, ring inflows
     __device__ __forceinline__ unsigned flag(int i) const { return (flagw[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
-    __device__ __forceinline__ unsigned flag_sync(int i) { return (atomicOr(&flagw[i >> 2], 0u) >> (8 * (i & 3))) & 0xFFu; }
-    __device__ __forceinline__ void set_flag(int i, unsigned bits) { atomicOr(&flagw[i >> 2], bits << (8 * (i & 3))); }
-    // true when this call folded in the last child
-    __device__ __forceinline__ bool dec_degree(int i) {
-        const unsigned sh = 8 * (i & 3);
-        return ((atomicSub(&degw[i >> 2], 1u << sh) >> sh) & 0xFFu) == 1u;
-    }
+    __device__ __forceinline__ bool done(int i) const { return (acc[i] & kDone) == kDone; }
+    __device__ __forceinline__ Acc total(int i) const { return acc[i] & kSum; }
+    __device__ __forceinline__ unsigned sub_bad(int i) const { return (unsigned)((acc[i] >> kBadShift) & 1u); }
 };
 
 // Whether the neighbour at (a, b) of the cell at codes position (ca, cb)
@@ -183,8 +192,6 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                     }
             }
             S.lpar[i] = lp;
-            reinterpret_cast<uint8_t*>(S.degw)[i] = (uint8_t)deg;
-            reinterpret_cast<uint8_t*>(S.flagw)[i] = (f && deg == 0) ? (uint8_t)(f | 8) : f;  // leaves fixed before any walk
             unsigned long long w = 0;
             uint32_t wb = 0;
             if (FINAL && f) {
@@ -194,35 +201,35 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                     wb = T.tinb[t * kScaSlots + sl];
                 }
             }
-            S.acc[i] = (typename Smem::Acc)w;  // external inflow (final pass) plus, later, the in-tile children
-            if (wb) reinterpret_cast<uint8_t*>(S.flagw)[i] |= 16;  // an inflow from another tile was not pulled
+            // leaves fixed before any walk; an inflow from another tile that was not pulled
+            reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0) | (wb ? 16 : 0));
+            // the in-tile children to come, and the external inflow (final pass)
+            S.acc[i] = (typename Smem::Acc)deg * Smem::kOne + (typename Smem::Acc)w;
         }
         atomicAdd(&S.cnt[0], nvalid);
         if (nring) atomicAdd(&S.cnt[2], nring);
         __syncthreads();
-        // Topological walk from the in-tile leaves.
+        // Topological walk from the in-tile leaves: a walker holds the value
+        // of its cell's word once every child has folded in (a leaf's word is
+        // final from the start; anything else's is the last child's return
+        // value plus its own add), so a step is one atomic on the parent.
+        using Acc = typename Smem::Acc;
         unsigned long long ndone = 0;
         for (int i = tid; i < kCells; i += kThreads) {
             if (!(S.flag(i) & 8)) continue;
             int cur = i;
+            Acc v = S.acc[i];
             for (;;) {
-                // Every child of cur added its total and flag before the
-                // fenced decrement that released cur, and nothing writes them
-                // any more: plain (volatile) reads see the final values.
-                const unsigned long long tot =
-                    1 + (unsigned long long)((volatile typename Smem::Acc*)S.acc)[cur];
-                const unsigned fl = (((volatile uint32_t*)S.flagw)[cur >> 2] >> (8 * (cur & 3))) & 0xFFu;
-                const bool bad = (fl & 18u) != 0;
-                S.acc[cur] = (typename Smem::Acc)tot;
-                S.set_flag(cur, 4u | (bad ? 16u : 0u));
+                const Acc tot = 1 + (v & Smem::kSum);
+                const bool bad = (S.flag(cur) & 18u) != 0 || ((v >> Smem::kBadShift) & 0xFu) != 0;
+                S.acc[cur] = Smem::kDone | (bad ? Smem::kBadOne : (Acc)0) | tot;  // nothing else writes it now
                 ndone++;
                 const int par = S.lpar[cur];
                 if (par < 0) break;
-                atomicAdd(&S.acc[par], (typename Smem::Acc)tot);
-                if (bad) S.set_flag(par, 16u);
-                __threadfence_block();
-                if (!S.dec_degree(par)) break;
-                __threadfence_block();
+                const Acc delta = tot + (bad ? Smem::kBadOne : (Acc)0) - Smem::kOne;  // the count field is >= 1
+                const Acc old = atomicAdd(&S.acc[par], delta);
+                if (((old >> Smem::kDegShift) & 0xFu) != 1u) break;  // another child is still to come
+                v = old + delta;
                 cur = par;
             }
         }
@@ -254,7 +261,7 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 if (sl < 0) continue;
                 const int64_t node = t * kScaSlots + sl;
                 int32_t ex = -1, ys = -1;
-                if (S.flag(i) & 4) {  // completed: its path is acyclic
+                if (S.done(i)) {  // completed: its path is acyclic
                     const int cur = S.lpar[i] >= 0 ? S.lpar[i] : i;  // the path's last cell (pointers jumped above)
                     if (S.lpar[cur] == -2) {
                         const int er = cur / kT, ec = cur % kT;
@@ -267,8 +274,8 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                         const int yth = (int)min((int64_t)kT, p.rows - (yr / kT) * kT);
                         const int ytw = (int)min((int64_t)kT, p.cols - (yc / kT) * kT);
                         ys = (int32_t)(yt * kScaSlots + slot_of((int)(yr % kT), (int)(yc % kT), yth, ytw));
-                        T.tot[node] = S.acc[i];
-                        T.totb[node] = (S.flag(i) >> 4) & 1u;
+                        T.tot[node] = S.total(i);
+                        T.totb[node] = S.sub_bad(i);
                     }
                 }
                 T.exit_of[node] = ex;
@@ -280,10 +287,9 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 const int lr = i / kT, lc = i % kT;
                 if (lr >= th || lc >= tw) continue;
                 const int64_t g = (r0 + lr) * p.cols + (c0 + lc);
-                const unsigned fl = S.flag(i);
-                const bool ok = (fl & 5) == 5;
-                s.conv[g] = ok ? (unsigned long long)S.acc[i] : 0ULL;
-                s.ship[g] = ok ? (unsigned long long)((fl >> 4) & 1u) : 0ULL;
+                const bool ok = (S.flag(i) & 1u) && S.done(i);
+                s.conv[g] = ok ? (unsigned long long)S.total(i) : 0ULL;
+                s.ship[g] = ok ? (unsigned long long)S.sub_bad(i) : 0ULL;
             }
             if (tid == 0) {
                 atomicAdd(&s.counters[1], S.cnt[0]);
