@@ -42,6 +42,7 @@ namespace {
 
 constexpr int kT = kScaTile;       // tile side
 constexpr int kH = kT + 4;         // codes with a 2-cell halo
+constexpr int kM = kT + 2;         // inflow masks with a 1-cell halo
 constexpr int kCells = kT * kT;
 constexpr int kThreads = 256;
 constexpr int8_t kNodata = -1, kNoFlow = -2;
@@ -102,6 +103,7 @@ struct TileSmem {
     static constexpr Acc kBadOne = (Acc)1 << kBadShift;
     static constexpr Acc kDone = (Acc)0xF << kDegShift;
     int8_t cd[kH * kH];          // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
+    uint8_t im[kM * kM];         // inflow masks of the tile and a 1-cell ring, (a, b) = (r - r0 + 1, c - c0 + 1)
     int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
     Acc acc[kCells];
     uint32_t flagw[kCells / 4];  // a byte of static flags per cell
@@ -120,6 +122,10 @@ __device__ __forceinline__ bool flows_in(const S_t& S, int ca, int cb, int a, in
     const int8_t q = S.cd[(ca + a) * kH + (cb + b)];
     return q == 8 - k && S.cd[ca * kH + cb] != k;
 }
+
+// Bit of the neighbour at offset (a, b) in an inflow mask (window index k =
+// (a + 1) * 3 + b + 1 without the centre).
+__device__ __forceinline__ int mask_bit(int k) { return k < 4 ? k : k - 1; }
 
 // Reference in-degree of the cell at codes position (ca, cb) is zero.
 template <class S_t>
@@ -153,6 +159,22 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
         }
         for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
         __syncthreads();
+        // Inflow masks of the tile and its 1-cell ring: bit mask_bit(k) set
+        // when the neighbour at window index k flows into the cell (its code
+        // names the cell, and the cell does not name it back).
+        for (int i = tid; i < kM * kM; i += kThreads) {
+            const int ca = i / kM + 1, cb = i % kM + 1;  // codes position
+            const int8_t own = S.cd[ca * kH + cb];
+            unsigned m = 0;
+#pragma unroll
+            for (int k = 0; k < 9; k++) {
+                if (k == 4) continue;
+                const int8_t q = S.cd[(ca + k / 3 - 1) * kH + (cb + k % 3 - 1)];
+                if (q == 8 - k && own != k) m |= 1u << mask_bit(k);
+            }
+            S.im[i] = (uint8_t)m;
+        }
+        __syncthreads();
         // The in-tile forest.
         unsigned long long nvalid = 0, nring = 0;
         for (int i = tid; i < kCells; i += kThreads) {
@@ -177,19 +199,20 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 // children: in-tile ones count towards the walk; an inflow from
                 // the ring is never released; a non-source child that follows
                 // the cell in raster order is not pulled by the single sweep.
-#pragma unroll 1
-                for (int a = -1; a <= 1; a++)
-#pragma unroll 1
-                    for (int b = -1; b <= 1; b++) {
-                        if (!(a || b) || !flows_in(S, ca, cb, a, b)) continue;
-                        if (!in_work(p, r + a, c + b)) {
-                            nring++;
-                            continue;
-                        }
-                        const int qr = lr + a, qc = lc + b;
-                        if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
-                        if ((a > 0 || (a == 0 && b > 0)) && !is_source(S, ca + a, cb + b)) f |= 2;
+                unsigned m = S.im[(lr + 1) * kM + lc + 1];
+                while (m) {
+                    const int bit = __ffs(m) - 1;
+                    m &= m - 1;
+                    const int kk = bit < 4 ? bit : bit + 1;
+                    const int a = kk / 3 - 1, b = kk % 3 - 1;
+                    if (!in_work(p, r + a, c + b)) {
+                        nring++;
+                        continue;
                     }
+                    const int qr = lr + a, qc = lc + b;
+                    if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
+                    if ((a > 0 || (a == 0 && b > 0)) && S.im[(qr + 1) * kM + qc + 1] != 0) f |= 2;
+                }
             }
             S.lpar[i] = lp;
             unsigned long long w = 0;
@@ -244,13 +267,17 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
             // own -1 or -2.  lpar is rebuilt by the final pass.
 #pragma unroll 1
             for (int round = 0; round < 12; round++) {
+                int moved = 0;
                 for (int i = tid; i < kCells; i += kThreads) {
                     const int q = S.lpar[i];
                     if (q < 0) continue;
                     const int q2 = ((volatile int16_t*)S.lpar)[q];
-                    if (q2 >= 0) S.lpar[i] = (int16_t)q2;
+                    if (q2 >= 0) {
+                        S.lpar[i] = (int16_t)q2;
+                        moved = 1;
+                    }
                 }
-                __syncthreads();
+                if (!__syncthreads_or(moved)) break;  // every pointer is at its path's last cell
             }
             // Border cells: the exit each in-tile path reaches; exits record
             // their in-tile totals and the entry they feed.
@@ -283,13 +310,27 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
             }
             if (tid == 0 && S.cnt[2]) atomicAdd(&s.counters[6], S.cnt[2]);
         } else {
+            // Converged contract: the output itself (a valid cell's count, 0
+            // where a cycle left it uncompleted; nodata elsewhere), plus the
+            // counts of the cells around the raster's last work cell for its
+            // nodata quirk.  Shipped contract: counts and flags for the
+            // output pass, which needs neighbours in other tiles.
+            const int64_t lastr = p.rows - 2, lastc = p.cols - 2;
             for (int i = tid; i < kCells; i += kThreads) {
                 const int lr = i / kT, lc = i % kT;
                 if (lr >= th || lc >= tw) continue;
-                const int64_t g = (r0 + lr) * p.cols + (c0 + lc);
-                const bool ok = (S.flag(i) & 1u) && S.done(i);
-                s.conv[g] = ok ? (unsigned long long)S.total(i) : 0ULL;
-                s.ship[g] = ok ? (unsigned long long)S.sub_bad(i) : 0ULL;
+                const int64_t r = r0 + lr, c = c0 + lc;
+                const int64_t g = r * p.cols + c;
+                const bool valid = (S.flag(i) & 1u) != 0;
+                const bool ok = valid && S.done(i);
+                const unsigned long long tot = ok ? (unsigned long long)S.total(i) : 0ULL;
+                if (p.shipped) {
+                    s.conv[g] = tot;
+                    s.ship[g] = ok ? (unsigned long long)S.sub_bad(i) : 0ULL;
+                } else {
+                    put_value(p.out, r, c, valid ? (double)tot : p.out.nodata);
+                    if (r >= lastr - 1 && r <= lastr + 1 && c >= lastc - 1 && c <= lastc + 1) s.conv[g] = tot;
+                }
             }
             if (tid == 0) {
                 atomicAdd(&s.counters[1], S.cnt[0]);
@@ -356,6 +397,24 @@ __global__ void sca_exit_walk_kernel(ScaScratch s, ScaTiles T) {
 }
 
 // Output: converged counts, or the shipped sweep's pulled sums.
+// Converged contract, after the fused output: the raster's last work cell,
+// when its code is nodata, holds nodata plus what flows into it (the
+// reference accumulates into it before it notices the nodata).
+__global__ void sca_last_cell_kernel(const ScaParams p, ScaScratch s) {
+    if (p.rows < 3 || p.cols < 3) return;
+    const int64_t r = p.rows - 2, c = p.cols - 2, i = r * p.cols + c;
+    if (decode8(p, r, c) != kNodata) return;
+    unsigned long long sum = 0;
+    for (int a = -1; a <= 1; a++)
+        for (int b = -1; b <= 1; b++) {
+            if (!(a || b)) continue;
+            const int k = (a + 1) * 3 + (b + 1);
+            if (!in_work(p, r + a, c + b) || decode8(p, r + a, c + b) != 8 - k) continue;
+            sum += s.conv[i + a * p.cols + b];
+        }
+    put_value(p.out, r, c, p.out.nodata + (double)sum);
+}
+
 __global__ void sca_output_kernel(const ScaParams p, ScaScratch s) {
     const int64_t n = p.rows * p.cols;
     const int64_t last = (p.rows - 2) * p.cols + (p.cols - 2);
@@ -460,6 +519,10 @@ cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTile
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     sca_tile_kernel<true><<<(unsigned)grid1, kThreads, smem1, st>>>(p, s, T);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (!p.shipped) {  // the final tile pass wrote the output
+        sca_last_cell_kernel<<<1, 1, 0, st>>>(p, s);
+        return cudaGetLastError();
+    }
     int64_t blocks = (n + 255) / 256;
     if (blocks > 8192) blocks = 8192;
     sca_output_kernel<<<(unsigned)blocks, 256, 0, st>>>(p, s);
