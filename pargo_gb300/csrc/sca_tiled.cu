@@ -47,22 +47,57 @@ constexpr int kCells = kT * kT;
 constexpr int kThreads = 256;
 constexpr int8_t kNodata = -1, kNoFlow = -2;
 
-__device__ __forceinline__ int8_t decode8(const ScaParams& p, int64_t r, int64_t c) {
-    if (r < 0 || c < 0 || r >= p.rows || c >= p.cols) return kNodata;
-    const char* row = p.d8.base + r * p.d8.pitch;
-    double v;
-    switch (p.d8.dtype) {
-        case PARGO_F64: v = reinterpret_cast<const double*>(row)[c]; break;
-        case PARGO_F32: v = (double)reinterpret_cast<const float*>(row)[c]; break;
-        case PARGO_I8: v = (double)reinterpret_cast<const int8_t*>(row)[c]; break;
-        case PARGO_I16: v = (double)reinterpret_cast<const int16_t*>(row)[c]; break;
-        default: v = (double)reinterpret_cast<const int32_t*>(row)[c]; break;
-    }
+// A D8 value as a code: 0-8 but 4, kNoFlow for any other number, kNodata
+// for the nodata value (scaOperator.cpp:48: within Eps for floating input).
+__device__ __forceinline__ int8_t classify8(const ScaParams& p, double v) {
     const bool nd = (p.d8.dtype == PARGO_F64 || p.d8.dtype == PARGO_F32) ? fabs(v - p.nodata) < kEpsHydro
-                                                                        : v == p.nodata;  // scaOperator.cpp:48
+                                                                        : v == p.nodata;
     if (nd) return kNodata;
     const int k = (int)v;
     return ((double)k == v && k >= 0 && k <= 8 && k != 4) ? (int8_t)k : kNoFlow;
+}
+
+template <typename V>
+__device__ __forceinline__ double d8_value(const ScaParams& p, int64_t r, int64_t c) {
+    return (double)reinterpret_cast<const V*>(p.d8.base + r * p.d8.pitch)[c];
+}
+
+__device__ __forceinline__ int8_t decode8(const ScaParams& p, int64_t r, int64_t c) {
+    if (r < 0 || c < 0 || r >= p.rows || c >= p.cols) return kNodata;
+    double v;
+    switch (p.d8.dtype) {
+        case PARGO_F64: v = d8_value<double>(p, r, c); break;
+        case PARGO_F32: v = d8_value<float>(p, r, c); break;
+        case PARGO_I8: v = d8_value<int8_t>(p, r, c); break;
+        case PARGO_I16: v = d8_value<int16_t>(p, r, c); break;
+        default: v = d8_value<int32_t>(p, r, c); break;
+    }
+    return classify8(p, v);
+}
+
+// The int8 codes of the window at (r0, c0) of kH x kH cells into cd, the
+// loads of a thread issued in two groups before their first use.
+__device__ __forceinline__ void load_codes_i8(const ScaParams& p, int64_t r0, int64_t c0, int8_t* cd, int tid) {
+    constexpr int kPer = (kH * kH + 255) / 256;  // 19
+    constexpr int kHalf = (kPer + 1) / 2;          // two groups of loads in flight
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        int v[kHalf];
+#pragma unroll
+        for (int q = 0; q < kHalf; q++) {
+            const int i = tid + (h * kHalf + q) * 256;
+            const int64_t r = r0 + i / kH, c = c0 + i % kH;
+            v[q] = 256;  // outside: not a byte value
+            if (i < kH * kH && r >= 0 && c >= 0 && r < p.rows && c < p.cols)
+                v[q] = reinterpret_cast<const int8_t*>(p.d8.base + r * p.d8.pitch)[c];
+        }
+#pragma unroll
+        for (int q = 0; q < kHalf; q++) {
+            const int i = tid + (h * kHalf + q) * 256;
+            if (i < kH * kH) cd[i] = v[q] == 256 ? kNodata : classify8(p, (double)v[q]);
+        }
+        asm volatile("" ::: "memory");
+    }
 }
 
 __device__ __forceinline__ bool in_work(const ScaParams& p, int64_t r, int64_t c) {
@@ -108,6 +143,7 @@ struct TileSmem {
     Acc acc[kCells];
     uint32_t flagw[kCells / 4];  // a byte of static flags per cell
     unsigned long long cnt[3];   // valid, completed, ring inflows
+    int next;                    // the walk's next cell to look at for a leaf
     __device__ __forceinline__ unsigned flag(int i) const { return (flagw[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
     __device__ __forceinline__ bool done(int i) const { return (acc[i] & kDone) == kDone; }
     __device__ __forceinline__ Acc total(int i) const { return acc[i] & kSum; }
@@ -139,7 +175,7 @@ __device__ __forceinline__ bool is_source(const S_t& S, int ca, int cb) {
 }
 
 template <bool FINAL>
-__global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
+__global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
     extern __shared__ __align__(16) unsigned char sca_smem[];
     using Smem = TileSmem<FINAL>;
     Smem& S = *reinterpret_cast<Smem*>(sca_smem);
@@ -157,7 +193,11 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
             T.tin[node] = 0;
             T.tinb[node] = 0;
         }
-        for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
+        static_assert(kThreads == 256, "load_codes_i8 strides by 256");
+        if (p.d8.dtype == PARGO_I8) load_codes_i8(p, r0 - 2, c0 - 2, S.cd, tid);
+        else
+            for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
+        if (tid == 0) S.next = 0;
         __syncthreads();
         // Inflow masks of the tile and its 1-cell ring: bit mask_bit(k) set
         // when the neighbour at window index k flows into the cell (its code
@@ -236,49 +276,56 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
         // of its cell's word once every child has folded in (a leaf's word is
         // final from the start; anything else's is the last child's return
         // value plus its own add), so a step is one atomic on the parent.
+        // Walkers take leaves from one shared cursor (a warp's lanes that
+        // need one take consecutive cells with a single atomic), so a lane
+        // that ends a chain starts the next leaf while long chains go on.
         using Acc = typename Smem::Acc;
         unsigned long long ndone = 0;
-        for (int i = tid; i < kCells; i += kThreads) {
-            if (!(S.flag(i) & 8)) continue;
-            int cur = i;
-            Acc v = S.acc[i];
+        {
+            const int lane = tid & 31;
+            int cur = -1;
+            Acc v = 0;
             for (;;) {
-                const Acc tot = 1 + (v & Smem::kSum);
-                const bool bad = (S.flag(cur) & 18u) != 0 || ((v >> Smem::kBadShift) & 0xFu) != 0;
-                S.acc[cur] = Smem::kDone | (bad ? Smem::kBadOne : (Acc)0) | tot;  // nothing else writes it now
-                ndone++;
-                const int par = S.lpar[cur];
-                if (par < 0) break;
-                const Acc delta = tot + (bad ? Smem::kBadOne : (Acc)0) - Smem::kOne;  // the count field is >= 1
-                const Acc old = atomicAdd(&S.acc[par], delta);
-                if (((old >> Smem::kDegShift) & 0xFu) != 1u) break;  // another child is still to come
-                v = old + delta;
-                cur = par;
+                const unsigned need = __ballot_sync(0xffffffffu, cur == -1);
+                if (need) {
+                    int base = 0;
+                    if (lane == __ffs(need) - 1) base = atomicAdd(&S.next, __popc(need));
+                    base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+                    if (cur == -1) {
+                        const int i = base + __popc(need & ((1u << lane) - 1));
+                        if (i < kCells && (S.flag(i) & 8)) {
+                            cur = i;
+                            v = S.acc[i];
+                        } else if (i >= kCells) {
+                            cur = -2;  // no leaves left for this lane
+                        }
+                    }
+                }
+                if (!__any_sync(0xffffffffu, cur >= 0) && !__any_sync(0xffffffffu, cur == -1)) break;
+                if (cur >= 0) {
+                    const Acc tot = 1 + (v & Smem::kSum);
+                    const bool bad = (S.flag(cur) & 18u) != 0 || ((v >> Smem::kBadShift) & 0xFu) != 0;
+                    S.acc[cur] = Smem::kDone | (bad ? Smem::kBadOne : (Acc)0) | tot;  // nothing else writes it now
+                    ndone++;
+                    const int par = S.lpar[cur];
+                    if (par < 0) {
+                        cur = -1;
+                    } else {
+                        const Acc delta = tot + (bad ? Smem::kBadOne : (Acc)0) - Smem::kOne;  // the count field is >= 1
+                        const Acc old = atomicAdd(&S.acc[par], delta);
+                        if (((old >> Smem::kDegShift) & 0xFu) != 1u) {
+                            cur = -1;  // another child is still to come
+                        } else {
+                            v = old + delta;
+                            cur = par;
+                        }
+                    }
+                }
             }
         }
         atomicAdd(&S.cnt[1], ndone);
         __syncthreads();
         if (!FINAL) {
-            // Parents become the path's last cell by pointer jumping (a
-            // parent pointer is replaced by its parent's while that is a
-            // cell): 12 rounds cover any acyclic path of a 64 x 64 tile, and
-            // a pointer is an ancestor of its cell at every moment, so the
-            // rounds need no read/write separation.  The last cell keeps its
-            // own -1 or -2.  lpar is rebuilt by the final pass.
-#pragma unroll 1
-            for (int round = 0; round < 12; round++) {
-                int moved = 0;
-                for (int i = tid; i < kCells; i += kThreads) {
-                    const int q = S.lpar[i];
-                    if (q < 0) continue;
-                    const int q2 = ((volatile int16_t*)S.lpar)[q];
-                    if (q2 >= 0) {
-                        S.lpar[i] = (int16_t)q2;
-                        moved = 1;
-                    }
-                }
-                if (!__syncthreads_or(moved)) break;  // every pointer is at its path's last cell
-            }
             // Border cells: the exit each in-tile path reaches; exits record
             // their in-tile totals and the entry they feed.
             for (int i = tid; i < kCells; i += kThreads) {
@@ -289,7 +336,10 @@ __global__ void __launch_bounds__(kThreads) sca_tile_kernel(const ScaParams p, S
                 const int64_t node = t * kScaSlots + sl;
                 int32_t ex = -1, ys = -1;
                 if (S.done(i)) {  // completed: its path is acyclic
-                    const int cur = S.lpar[i] >= 0 ? S.lpar[i] : i;  // the path's last cell (pointers jumped above)
+                    // the path's last cell, followed parent by parent (a
+                    // completed cell's path has no cycle: at most kCells steps)
+                    int cur = i;
+                    for (int guard = 0; guard < kCells && S.lpar[cur] >= 0; guard++) cur = S.lpar[cur];
                     if (S.lpar[cur] == -2) {
                         const int er = cur / kT, ec = cur % kT;
                         ex = (int32_t)(t * kScaSlots + slot_of(er, ec, th, tw));
