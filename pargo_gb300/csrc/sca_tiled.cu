@@ -144,6 +144,7 @@ struct TileSmem {
     uint32_t flagw[kCells / 4];  // a byte of static flags per cell
     unsigned long long cnt[3];   // valid, completed, ring inflows
     int next;                    // the walk's next cell to look at for a leaf
+    int16_t slotcell[FINAL ? kScaSlots : 1];  // final pass: the valid cell at each border slot, -1 none
     __device__ __forceinline__ unsigned flag(int i) const { return (flagw[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
     __device__ __forceinline__ bool done(int i) const { return (acc[i] & kDone) == kDone; }
     __device__ __forceinline__ Acc total(int i) const { return acc[i] & kSum; }
@@ -185,6 +186,15 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const
         const int64_t r0 = (t / T.tiles_x) * kT, c0 = (t % T.tiles_x) * kT;
         const int th = (int)min((int64_t)kT, p.rows - r0), tw = (int)min((int64_t)kT, p.cols - c0);
         if (tid < 3) S.cnt[tid] = 0;
+        // Final pass: the inflows from other tiles, loaded now and added to
+        // their cells after the forest is built.
+        unsigned long long xin = 0;
+        uint32_t xinb = 0;
+        if (FINAL && tid < kScaSlots) {
+            xin = T.tin[t * kScaSlots + tid];
+            xinb = T.tinb[t * kScaSlots + tid];
+            S.slotcell[tid] = -1;
+        }
         if (!FINAL && tid < kScaSlots) {  // every slot starts as "no exit"; the exit forest's accumulators empty
             const int64_t node = t * kScaSlots + tid;
             T.exit_of[node] = -1;
@@ -255,23 +265,26 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const
                 }
             }
             S.lpar[i] = lp;
-            unsigned long long w = 0;
-            uint32_t wb = 0;
             if (FINAL && f) {
                 const int sl = slot_of(lr, lc, th, tw);
-                if (sl >= 0) {
-                    w = T.tin[t * kScaSlots + sl];
-                    wb = T.tinb[t * kScaSlots + sl];
-                }
+                if (sl >= 0) S.slotcell[sl] = (int16_t)i;
             }
-            // leaves fixed before any walk; an inflow from another tile that was not pulled
-            reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0) | (wb ? 16 : 0));
-            // the in-tile children to come, and the external inflow (final pass)
-            S.acc[i] = (typename Smem::Acc)deg * Smem::kOne + (typename Smem::Acc)w;
+            reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));  // leaves fixed before any walk
+            S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;  // the in-tile children to come
         }
         atomicAdd(&S.cnt[0], nvalid);
         if (nring) atomicAdd(&S.cnt[2], nring);
         __syncthreads();
+        if (FINAL) {
+            // the external inflow of each valid border cell, and its flag: an
+            // inflow from another tile that was not pulled
+            const int i = tid < kScaSlots ? S.slotcell[tid] : -1;
+            if (i >= 0) {
+                S.acc[i] += (typename Smem::Acc)xin;
+                if (xinb) atomicOr(&S.flagw[i >> 2], 16u << (8 * (i & 3)));
+            }
+            __syncthreads();
+        }
         // Topological walk from the in-tile leaves: a walker holds the value
         // of its cell's word once every child has folded in (a leaf's word is
         // final from the start; anything else's is the last child's return
@@ -326,6 +339,26 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const
         atomicAdd(&S.cnt[1], ndone);
         __syncthreads();
         if (!FINAL) {
+            // Parents become the path's last cell by pointer jumping (a
+            // parent pointer is replaced by its parent's while that is a
+            // cell): 12 rounds cover any acyclic path of a 64 x 64 tile, and
+            // a pointer is an ancestor of its cell at every moment, so the
+            // rounds need no read/write separation.  The last cell keeps its
+            // own -1 or -2.  lpar is rebuilt by the final pass.
+#pragma unroll 1
+            for (int round = 0; round < 12; round++) {
+                int moved = 0;
+                for (int i = tid; i < kCells; i += kThreads) {
+                    const int q = S.lpar[i];
+                    if (q < 0) continue;
+                    const int q2 = ((volatile int16_t*)S.lpar)[q];
+                    if (q2 >= 0) {
+                        S.lpar[i] = (int16_t)q2;
+                        moved = 1;
+                    }
+                }
+                if (!__syncthreads_or(moved)) break;  // every pointer is at its path's last cell
+            }
             // Border cells: the exit each in-tile path reaches; exits record
             // their in-tile totals and the entry they feed.
             for (int i = tid; i < kCells; i += kThreads) {
@@ -336,10 +369,7 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const
                 const int64_t node = t * kScaSlots + sl;
                 int32_t ex = -1, ys = -1;
                 if (S.done(i)) {  // completed: its path is acyclic
-                    // the path's last cell, followed parent by parent (a
-                    // completed cell's path has no cycle: at most kCells steps)
-                    int cur = i;
-                    for (int guard = 0; guard < kCells && S.lpar[cur] >= 0; guard++) cur = S.lpar[cur];
+                    const int cur = S.lpar[i] >= 0 ? S.lpar[i] : i;  // the path's last cell (pointers jumped above)
                     if (S.lpar[cur] == -2) {
                         const int er = cur / kT, ec = cur % kT;
                         ex = (int32_t)(t * kScaSlots + slot_of(er, ec, th, tw));
