@@ -68,7 +68,7 @@ enum SlotId {
     kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotMfdLayer0,
     kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotStripSlow, kSlotLoadRows,
     kSlotBatchStripMaps, kSlotBatchSegStart, kSlotBatchNstrips, kSlotBatchSlow, kSlotFillMosaic, kSlotFillItems,
-    kSlotBatchSegLoad, kSlotBatchOrder, kSlotCount
+    kSlotBatchSegLoad, kSlotBatchOrder, kSlotScaForest, kSlotCount
 };
 static_assert(kSlotCount <= 48, "context slot table");
 
@@ -1332,6 +1332,8 @@ pargo_status sca_launch(pargo_ctx* ctx, const ScaParams& q, cudaStream_t s, cons
     if (!sc.ship) return cuda_fail(ctx, e, "sca flags");
     sc.counters = (unsigned long long*)slot(ctx, kSlotScaCounters, 8 * sizeof(unsigned long long), &e);
     if (!sc.counters) return cuda_fail(ctx, e, "sca counters");
+    sc.forest = (uint32_t*)slot(ctx, kSlotScaForest, (size_t)n * 4, &e);
+    if (!sc.forest) return cuda_fail(ctx, e, "sca tile forests");
     void* tb = slot(ctx, kSlotScaTiles, sca_tiles_bytes(q.rows, q.cols), &e);
     if (!tb) return cuda_fail(ctx, e, "sca tile forest");
     const ScaTiles T = sca_tiles_layout(tb, q.rows, q.cols);

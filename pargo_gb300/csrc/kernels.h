@@ -186,6 +186,7 @@ struct ScaScratch {
     unsigned long long* ship;  // accumulated pulled counts (shipped contract)
     uint8_t* flags;         // bit0 source, bit1 not-done, bit2 valid, bit3 completed
     unsigned long long* counters;  // [0] completed cells, [1] valid cells, [2] last-cell conv, [3] last-cell ship
+    uint32_t* forest;       // tiled SCA: per cell, the in-tile forest of the first pass for the final one
 };
 cudaError_t sca_run(const ScaParams& p, const ScaScratch& s, cudaStream_t st);
 

@@ -137,8 +137,10 @@ struct TileSmem {
     static constexpr Acc kOne = (Acc)1 << kDegShift;   // one child in the count field
     static constexpr Acc kBadOne = (Acc)1 << kBadShift;
     static constexpr Acc kDone = (Acc)0xF << kDegShift;
-    int8_t cd[kH * kH];          // codes, (a, b) = (r - r0 + 2, c - c0 + 2)
-    uint8_t im[kM * kM];         // inflow masks of the tile and a 1-cell ring, (a, b) = (r - r0 + 1, c - c0 + 1)
+    // first pass only: the codes, (a, b) = (r - r0 + 2, c - c0 + 2), and the
+    // inflow masks of the tile and a 1-cell ring, (a, b) = (r - r0 + 1, c - c0 + 1)
+    int8_t cd[FINAL ? 1 : kH * kH];
+    uint8_t im[FINAL ? 1 : kM * kM];
     int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
     Acc acc[kCells];
     uint32_t flagw[kCells / 4];  // a byte of static flags per cell
@@ -160,6 +162,12 @@ __device__ __forceinline__ bool flows_in(const S_t& S, int ca, int cb, int a, in
     return q == 8 - k && S.cd[ca * kH + cb] != k;
 }
 
+// A cell's in-tile forest as one word: flags (1 valid work cell, 2 "bad"),
+// in-tile children (bits 4-7) and parent + 2 (bits 8-20: -2 .. 4095).
+__device__ __forceinline__ uint32_t pack_forest(unsigned f, int deg, int lp) {
+    return (f & 3u) | ((uint32_t)deg << 4) | ((uint32_t)(lp + 2) << 8);
+}
+
 // Bit of the neighbour at offset (a, b) in an inflow mask (window index k =
 // (a + 1) * 3 + b + 1 without the centre).
 __device__ __forceinline__ int mask_bit(int k) { return k < 4 ? k : k - 1; }
@@ -176,7 +184,7 @@ __device__ __forceinline__ bool is_source(const S_t& S, int ca, int cb) {
 }
 
 template <bool FINAL>
-__global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
+__global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const ScaParams p, ScaScratch s, ScaTiles T) {
     extern __shared__ __align__(16) unsigned char sca_smem[];
     using Smem = TileSmem<FINAL>;
     Smem& S = *reinterpret_cast<Smem*>(sca_smem);
@@ -203,78 +211,106 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 4 : 6) sca_tile_kernel(const
             T.tin[node] = 0;
             T.tinb[node] = 0;
         }
-        static_assert(kThreads == 256, "load_codes_i8 strides by 256");
-        if (p.d8.dtype == PARGO_I8) load_codes_i8(p, r0 - 2, c0 - 2, S.cd, tid);
-        else
-            for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
         if (tid == 0) S.next = 0;
-        __syncthreads();
-        // Inflow masks of the tile and its 1-cell ring: bit mask_bit(k) set
-        // when the neighbour at window index k flows into the cell (its code
-        // names the cell, and the cell does not name it back).
-        for (int i = tid; i < kM * kM; i += kThreads) {
-            const int ca = i / kM + 1, cb = i % kM + 1;  // codes position
-            const int8_t own = S.cd[ca * kH + cb];
-            unsigned m = 0;
+        if constexpr (!FINAL) {
+            static_assert(kThreads == 256, "load_codes_i8 strides by 256");
+            if (p.d8.dtype == PARGO_I8) load_codes_i8(p, r0 - 2, c0 - 2, S.cd, tid);
+            else
+                for (int i = tid; i < kH * kH; i += kThreads) S.cd[i] = decode8(p, r0 - 2 + i / kH, c0 - 2 + i % kH);
+            __syncthreads();
+            // Inflow masks of the tile and its 1-cell ring: bit mask_bit(k) set
+            // when the neighbour at window index k flows into the cell (its code
+            // names the cell, and the cell does not name it back).
+            for (int i = tid; i < kM * kM; i += kThreads) {
+                const int ca = i / kM + 1, cb = i % kM + 1;  // codes position
+                const int8_t own = S.cd[ca * kH + cb];
+                unsigned m = 0;
+    #pragma unroll
+                for (int k = 0; k < 9; k++) {
+                    if (k == 4) continue;
+                    const int8_t q = S.cd[(ca + k / 3 - 1) * kH + (cb + k % 3 - 1)];
+                    if (q == 8 - k && own != k) m |= 1u << mask_bit(k);
+                }
+                S.im[i] = (uint8_t)m;
+            }
+            __syncthreads();
+            // The in-tile forest.
+            unsigned long long nvalid = 0, nring = 0;
+            for (int i = tid; i < kCells; i += kThreads) {
+                const int lr = i / kT, lc = i % kT;
+                const int64_t r = r0 + lr, c = c0 + lc;
+                const int ca = lr + 2, cb = lc + 2;
+                int16_t lp = -1;
+                int deg = 0;
+                uint8_t f = 0;
+                if (lr < th && lc < tw && in_work(p, r, c) && S.cd[ca * kH + cb] != kNodata) {
+                    f = 1;
+                    nvalid++;
+                    const int8_t k = S.cd[ca * kH + cb];
+                    if (k >= 0) {
+                        const int a = k / 3 - 1, b = k % 3 - 1;
+                        const int8_t tk = S.cd[(ca + a) * kH + (cb + b)];
+                        if (in_work(p, r + a, c + b) && tk != kNodata && tk != 8 - k) {
+                            const int tr = lr + a, tc = lc + b;
+                            lp = (tr >= 0 && tc >= 0 && tr < th && tc < tw) ? (int16_t)(tr * kT + tc) : (int16_t)-2;
+                        }
+                    }
+                    // children: in-tile ones count towards the walk; an inflow from
+                    // the ring is never released; a non-source child that follows
+                    // the cell in raster order is not pulled by the single sweep.
+                    unsigned m = S.im[(lr + 1) * kM + lc + 1];
+                    while (m) {
+                        const int bit = __ffs(m) - 1;
+                        m &= m - 1;
+                        const int kk = bit < 4 ? bit : bit + 1;
+                        const int a = kk / 3 - 1, b = kk % 3 - 1;
+                        if (!in_work(p, r + a, c + b)) {
+                            nring++;
+                            continue;
+                        }
+                        const int qr = lr + a, qc = lc + b;
+                        if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
+                        if ((a > 0 || (a == 0 && b > 0)) && S.im[(qr + 1) * kM + qc + 1] != 0) f |= 2;
+                    }
+                }
+                S.lpar[i] = lp;
+                reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));  // leaves fixed before any walk
+                S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;  // the in-tile children to come
+                if (lr < th && lc < tw) s.forest[r * p.cols + c] = pack_forest(f, deg, lp);
+            }
+            atomicAdd(&S.cnt[0], nvalid);
+            if (nring) atomicAdd(&S.cnt[2], nring);
+            __syncthreads();
+        } else {
+            // The forest the first pass built, one word per cell, every load
+            // of a thread issued before the first is unpacked.
+            constexpr int kPer = kCells / kThreads;  // 16
+            uint32_t fw[kPer];
 #pragma unroll
-            for (int k = 0; k < 9; k++) {
-                if (k == 4) continue;
-                const int8_t q = S.cd[(ca + k / 3 - 1) * kH + (cb + k % 3 - 1)];
-                if (q == 8 - k && own != k) m |= 1u << mask_bit(k);
+            for (int q = 0; q < kPer; q++) {
+                const int i = tid + q * kThreads;
+                const int lr = i / kT, lc = i % kT;
+                fw[q] = pack_forest(0, 0, -1);  // outside the raster: no cell
+                if (lr < th && lc < tw) fw[q] = s.forest[(r0 + lr) * p.cols + (c0 + lc)];
             }
-            S.im[i] = (uint8_t)m;
-        }
-        __syncthreads();
-        // The in-tile forest.
-        unsigned long long nvalid = 0, nring = 0;
-        for (int i = tid; i < kCells; i += kThreads) {
-            const int lr = i / kT, lc = i % kT;
-            const int64_t r = r0 + lr, c = c0 + lc;
-            const int ca = lr + 2, cb = lc + 2;
-            int16_t lp = -1;
-            int deg = 0;
-            uint8_t f = 0;
-            if (lr < th && lc < tw && in_work(p, r, c) && S.cd[ca * kH + cb] != kNodata) {
-                f = 1;
-                nvalid++;
-                const int8_t k = S.cd[ca * kH + cb];
-                if (k >= 0) {
-                    const int a = k / 3 - 1, b = k % 3 - 1;
-                    const int8_t tk = S.cd[(ca + a) * kH + (cb + b)];
-                    if (in_work(p, r + a, c + b) && tk != kNodata && tk != 8 - k) {
-                        const int tr = lr + a, tc = lc + b;
-                        lp = (tr >= 0 && tc >= 0 && tr < th && tc < tw) ? (int16_t)(tr * kT + tc) : (int16_t)-2;
-                    }
-                }
-                // children: in-tile ones count towards the walk; an inflow from
-                // the ring is never released; a non-source child that follows
-                // the cell in raster order is not pulled by the single sweep.
-                unsigned m = S.im[(lr + 1) * kM + lc + 1];
-                while (m) {
-                    const int bit = __ffs(m) - 1;
-                    m &= m - 1;
-                    const int kk = bit < 4 ? bit : bit + 1;
-                    const int a = kk / 3 - 1, b = kk % 3 - 1;
-                    if (!in_work(p, r + a, c + b)) {
-                        nring++;
-                        continue;
-                    }
-                    const int qr = lr + a, qc = lc + b;
-                    if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
-                    if ((a > 0 || (a == 0 && b > 0)) && S.im[(qr + 1) * kM + qc + 1] != 0) f |= 2;
+            __syncthreads();  // every slot reset to -1 above before any is claimed below
+            unsigned long long nvalid = 0;
+#pragma unroll
+            for (int q = 0; q < kPer; q++) {
+                const int i = tid + q * kThreads;
+                const unsigned f = fw[q] & 3u, deg = (fw[q] >> 4) & 0xFu;
+                S.lpar[i] = (int16_t)((int)(fw[q] >> 8) - 2);
+                reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));
+                S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;
+                if (f & 1u) {
+                    nvalid++;
+                    const int sl = slot_of(i / kT, i % kT, th, tw);
+                    if (sl >= 0) S.slotcell[sl] = (int16_t)i;
                 }
             }
-            S.lpar[i] = lp;
-            if (FINAL && f) {
-                const int sl = slot_of(lr, lc, th, tw);
-                if (sl >= 0) S.slotcell[sl] = (int16_t)i;
-            }
-            reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));  // leaves fixed before any walk
-            S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;  // the in-tile children to come
+            atomicAdd(&S.cnt[0], nvalid);
+            __syncthreads();
         }
-        atomicAdd(&S.cnt[0], nvalid);
-        if (nring) atomicAdd(&S.cnt[2], nring);
-        __syncthreads();
         if (FINAL) {
             // the external inflow of each valid border cell, and its flag: an
             // inflow from another tile that was not pulled
