@@ -197,11 +197,9 @@ struct ScaTiles {
     int32_t* exit_of;   // border cell -> exit node its in-tile path reaches (-1: ends in the tile)
     int32_t* yslot;     // exit node -> entry node its flow enters (-1: not an exit)
     int32_t* xpar;      // exit node -> exit-forest parent (-1: root)
-    int32_t* xdeg;      // exit-forest in-degree
-    unsigned long long* tot;   // exit: own in-tile total, then the total through it
+    unsigned long long* tot;   // exit: packed count of feeding exits, bad count, and sum (sca_tiled.cu)
     unsigned long long* tin;   // entry: external inflow total
-    uint32_t* totb;     // the same for the "some inflow not pulled" flag
-    uint32_t* tinb;
+    uint32_t* tinb;     // bit 0, entry: some inflow was not pulled (shipped contract); bit 1, exit: a leaf
 };
 constexpr int kScaTile = 64;
 constexpr int kScaSlots = 256;

@@ -162,6 +162,18 @@ __device__ __forceinline__ bool flows_in(const S_t& S, int ca, int cb, int a, in
     return q == 8 - k && S.cd[ca * kH + cb] != k;
 }
 
+// An exit's word in the exit forest: from the top, a 12-bit count of exits
+// still to feed it (at most 5 per border cell of its tile), a 12-bit count
+// of fed exits whose total holds a "bad" cell (its own in-tile subtree's bad
+// bit counts as one), and a 40-bit sum of cells.
+constexpr int kXCountShift = 52, kXBadShift = 40;
+constexpr unsigned long long kXCountMask = 0xFFFULL;
+constexpr unsigned long long kXOne = 1ULL << kXCountShift, kXBadOne = 1ULL << kXBadShift;
+constexpr unsigned long long kXSum = kXBadOne - 1;
+__device__ __forceinline__ unsigned long long xpack(unsigned long long total, unsigned bad) {
+    return total | (bad ? kXBadOne : 0ULL);
+}
+
 // A cell's in-tile forest as one word: flags (1 valid work cell, 2 "bad"),
 // in-tile children (bits 4-7) and parent + 2 (bits 8-20: -2 .. 4095).
 __device__ __forceinline__ uint32_t pack_forest(unsigned f, int deg, int lp) {
@@ -207,7 +219,6 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             const int64_t node = t * kScaSlots + tid;
             T.exit_of[node] = -1;
             T.yslot[node] = -1;
-            T.xdeg[node] = 0;
             T.tin[node] = 0;
             T.tinb[node] = 0;
         }
@@ -317,7 +328,7 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             const int i = tid < kScaSlots ? S.slotcell[tid] : -1;
             if (i >= 0) {
                 S.acc[i] += (typename Smem::Acc)xin;
-                if (xinb) atomicOr(&S.flagw[i >> 2], 16u << (8 * (i & 3)));
+                if (xinb & 1u) atomicOr(&S.flagw[i >> 2], 16u << (8 * (i & 3)));
             }
             __syncthreads();
         }
@@ -417,8 +428,7 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                         const int yth = (int)min((int64_t)kT, p.rows - (yr / kT) * kT);
                         const int ytw = (int)min((int64_t)kT, p.cols - (yc / kT) * kT);
                         ys = (int32_t)(yt * kScaSlots + slot_of((int)(yr % kT), (int)(yc % kT), yth, ytw));
-                        T.tot[node] = S.total(i);
-                        T.totb[node] = S.sub_bad(i);
+                        T.tot[node] = xpack(S.total(i), S.sub_bad(i));
                     }
                 }
                 T.exit_of[node] = ex;
@@ -467,7 +477,7 @@ __global__ void sca_exit_links_kernel(ScaScratch s, ScaTiles T) {
         if (y >= 0) {
             nexit++;
             px = T.exit_of[y];
-            if (px >= 0) atomicAdd(&T.xdeg[px], 1);
+            if (px >= 0) atomicAdd(&T.tot[px], kXOne);
         }
         T.xpar[x] = px;
     }
@@ -475,38 +485,55 @@ __global__ void sca_exit_links_kernel(ScaScratch s, ScaTiles T) {
     if ((threadIdx.x & 31) == 0 && nexit) atomicAdd(&s.counters[4], nexit);
 }
 
-// Exit forest: mark its leaves (bit 1 of totb) once every in-degree is known,
-// so that the walk below starts from them only.
+// Exit forest: mark its leaves (exits that no other exit feeds: a zero count
+// field once every link is in) in bit 1 of tinb, before any walk lowers a
+// count to zero.
 __global__ void sca_exit_leaves_kernel(ScaTiles T) {
     const int64_t n = T.tiles_x * T.tiles_y * kScaSlots;
     for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
-        if (T.yslot[x] >= 0 && T.xdeg[x] == 0) T.totb[x] |= 2u;
+        if (T.yslot[x] >= 0 && (T.tot[x] >> kXCountShift) == 0) T.tinb[x] |= 2u;
 }
 
-// Exit forest: totals by a topological walk from its leaves; each exit feeds
-// its total into the entry it flows into.
+// Exit forest: totals by a topological walk from its leaves; each exit
+// feeds its total into the entry it flows into.  A step is one atomic add on
+// the parent's packed word, whose return value tells the walker whether it
+// was the last child and, if so, the parent's complete sum.  A thread takes
+// the leaves of its grid-stride range one after another.
 __global__ void sca_exit_walk_kernel(ScaScratch s, ScaTiles T) {
     const int64_t n = T.tiles_x * T.tiles_y * kScaSlots;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     unsigned long long ndone = 0;
-    for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-        if (T.yslot[x] < 0 || !(T.totb[x] & 2u)) continue;
-        int64_t cur = x;
-        for (;;) {
-            const unsigned long long tot = atomicAdd(&T.tot[cur], 0ULL);
-            const uint32_t bad = atomicOr(&T.totb[cur], 0u) & 1u;
-            const int32_t y = T.yslot[cur];
-            atomicAdd(&T.tin[y], tot);
-            if (bad) atomicOr(&T.tinb[y], 1u);
-            ndone++;
-            const int32_t px = T.xpar[cur];
-            if (px < 0) break;
-            atomicAdd(&T.tot[px], tot);
-            if (bad) atomicOr(&T.totb[px], 1u);
-            __threadfence();
-            if (atomicSub(&T.xdeg[px], 1) != 1) break;
-            __threadfence();
-            cur = px;
+    int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t cur = -1;
+    unsigned long long v = 0;
+    for (;;) {
+        if (cur < 0) {
+            for (; x < n; x += stride)
+                if (T.yslot[x] >= 0 && (T.tinb[x] & 2u)) break;
+            if (x >= n) break;
+            cur = x;
+            v = T.tot[x];
+            x += stride;
         }
+        const unsigned long long tot = v & kXSum;
+        const bool bad = ((v >> kXBadShift) & kXCountMask) != 0;
+        const int32_t y = T.yslot[cur];
+        atomicAdd(&T.tin[y], tot);
+        if (bad) atomicOr(&T.tinb[y], 1u);  // bit 0: not pulled (bit 1 marks y's own leaf state)
+        ndone++;
+        const int32_t px = T.xpar[cur];
+        if (px < 0) {
+            cur = -1;
+            continue;
+        }
+        const unsigned long long delta = tot + (bad ? kXBadOne : 0ULL) - kXOne;  // the count field is >= 1
+        const unsigned long long old = atomicAdd(&T.tot[px], delta);
+        if ((old >> kXCountShift) != 1ULL) {
+            cur = -1;  // another exit still feeds it
+            continue;
+        }
+        v = old + delta;
+        cur = px;
     }
     ndone = __reduce_add_sync(0xffffffffu, (unsigned)ndone);
     if ((threadIdx.x & 31) == 0 && ndone) atomicAdd(&s.counters[5], ndone);
@@ -570,7 +597,7 @@ __global__ void sca_output_kernel(const ScaParams p, ScaScratch s) {
 
 size_t sca_tiles_bytes(int64_t rows, int64_t cols) {
     const int64_t nodes = ((rows + kT - 1) / kT) * ((cols + kT - 1) / kT) * kScaSlots;
-    return (size_t)nodes * (4 * 4 + 2 * 8 + 2 * 4) + 256;
+    return (size_t)nodes * (3 * 4 + 2 * 8 + 4) + 256;
 }
 
 ScaTiles sca_tiles_layout(void* base, int64_t rows, int64_t cols) {
@@ -588,10 +615,6 @@ ScaTiles sca_tiles_layout(void* base, int64_t rows, int64_t cols) {
     T.yslot = (int32_t*)b;
     b += nodes * 4;
     T.xpar = (int32_t*)b;
-    b += nodes * 4;
-    T.xdeg = (int32_t*)b;
-    b += nodes * 4;
-    T.totb = (uint32_t*)b;
     b += nodes * 4;
     T.tinb = (uint32_t*)b;
     return T;
