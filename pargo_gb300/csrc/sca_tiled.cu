@@ -245,26 +245,32 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                 S.im[i] = (uint8_t)m;
             }
             __syncthreads();
-            // The in-tile forest.
+            // The in-tile forest.  A thread owns column lc = tid % 64 of rows
+            // tid / 64 + 4q; the raster's work region (rows and columns 1 ..
+            // n - 2) in tile-local coordinates bounds every test.
             unsigned long long nvalid = 0, nring = 0;
-            for (int i = tid; i < kCells; i += kThreads) {
-                const int lr = i / kT, lc = i % kT;
-                const int64_t r = r0 + lr, c = c0 + lc;
+            const int wr_lo = (int)max((int64_t)-2, 1 - r0), wr_hi = (int)min((int64_t)kT + 1, p.rows - 2 - r0);
+            const int wc_lo = (int)max((int64_t)-2, 1 - c0), wc_hi = (int)min((int64_t)kT + 1, p.cols - 2 - c0);
+            auto work = [&](int lr, int lc) { return lr >= wr_lo && lr <= wr_hi && lc >= wc_lo && lc <= wc_hi; };
+            const int lc = tid & (kT - 1);
+#pragma unroll 2
+            for (int q = 0; q < kCells / kThreads; q++) {
+                const int lr = (tid >> 6) + q * (kThreads / kT);
+                const int i = lr * kT + lc;
                 const int ca = lr + 2, cb = lc + 2;
                 int16_t lp = -1;
                 int deg = 0;
                 uint8_t f = 0;
-                if (lr < th && lc < tw && in_work(p, r, c) && S.cd[ca * kH + cb] != kNodata) {
+                const int8_t k = S.cd[ca * kH + cb];
+                if (lr < th && lc < tw && work(lr, lc) && k != kNodata) {
                     f = 1;
                     nvalid++;
-                    const int8_t k = S.cd[ca * kH + cb];
                     if (k >= 0) {
                         const int a = k / 3 - 1, b = k % 3 - 1;
+                        const int tr = lr + a, tc = lc + b;
                         const int8_t tk = S.cd[(ca + a) * kH + (cb + b)];
-                        if (in_work(p, r + a, c + b) && tk != kNodata && tk != 8 - k) {
-                            const int tr = lr + a, tc = lc + b;
+                        if (work(tr, tc) && tk != kNodata && tk != 8 - k)
                             lp = (tr >= 0 && tc >= 0 && tr < th && tc < tw) ? (int16_t)(tr * kT + tc) : (int16_t)-2;
-                        }
                     }
                     // children: in-tile ones count towards the walk; an inflow from
                     // the ring is never released; a non-source child that follows
@@ -275,19 +281,19 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                         m &= m - 1;
                         const int kk = bit < 4 ? bit : bit + 1;
                         const int a = kk / 3 - 1, b = kk % 3 - 1;
-                        if (!in_work(p, r + a, c + b)) {
+                        const int qr = lr + a, qc = lc + b;
+                        if (!work(qr, qc)) {
                             nring++;
                             continue;
                         }
-                        const int qr = lr + a, qc = lc + b;
                         if (qr >= 0 && qc >= 0 && qr < th && qc < tw) deg++;
-                        if ((a > 0 || (a == 0 && b > 0)) && S.im[(qr + 1) * kM + qc + 1] != 0) f |= 2;
+                        if (kk > 4 && S.im[(qr + 1) * kM + qc + 1] != 0) f |= 2;  // kk > 4: a later cell in raster order
                     }
                 }
                 S.lpar[i] = lp;
                 reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));  // leaves fixed before any walk
                 S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;  // the in-tile children to come
-                if (lr < th && lc < tw) s.forest[r * p.cols + c] = pack_forest(f, deg, lp);
+                if (lr < th && lc < tw) s.forest[(r0 + lr) * p.cols + (c0 + lc)] = pack_forest(f, deg, lp);
             }
             atomicAdd(&S.cnt[0], nvalid);
             if (nring) atomicAdd(&S.cnt[2], nring);
@@ -392,16 +398,20 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             // a pointer is an ancestor of its cell at every moment, so the
             // rounds need no read/write separation.  The last cell keeps its
             // own -1 or -2.  lpar is rebuilt by the final pass.
+            unsigned active = 0xFFFFu;  // this thread's cells tid + 256 q whose pointer may still move
 #pragma unroll 1
             for (int round = 0; round < 12; round++) {
                 int moved = 0;
-                for (int i = tid; i < kCells; i += kThreads) {
-                    const int q = S.lpar[i];
-                    if (q < 0) continue;
-                    const int q2 = ((volatile int16_t*)S.lpar)[q];
+                for (unsigned m = active; m; m &= m - 1) {
+                    const int q = __ffs(m) - 1;
+                    const int i = tid + q * kThreads;
+                    const int pq = S.lpar[i];
+                    const int q2 = pq >= 0 ? ((volatile int16_t*)S.lpar)[pq] : -1;
                     if (q2 >= 0) {
                         S.lpar[i] = (int16_t)q2;
                         moved = 1;
+                    } else {
+                        active &= ~(1u << q);  // at its path's last cell (or the last cell itself)
                     }
                 }
                 if (!__syncthreads_or(moved)) break;  // every pointer is at its path's last cell
@@ -630,6 +640,14 @@ cudaError_t sca_run_tiled(const ScaParams& p, const ScaScratch& s, const ScaTile
         cudaSuccess)
         return e;
     if ((e = cudaFuncSetAttribute(sca_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem1)) !=
+        cudaSuccess)
+        return e;
+    // all of the SM's unified memory as shared memory: 6 first-pass and 5
+    // final-pass tiles in flight per SM
+    if ((e = cudaFuncSetAttribute(sca_tile_kernel<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100)) !=
+        cudaSuccess)
+        return e;
+    if ((e = cudaFuncSetAttribute(sca_tile_kernel<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100)) !=
         cudaSuccess)
         return e;
     int dev = 0, sms = 0, per0 = 0, per1 = 0;
