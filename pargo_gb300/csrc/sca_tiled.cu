@@ -80,6 +80,9 @@ __device__ __forceinline__ int8_t decode8(const ScaParams& p, int64_t r, int64_t
 __device__ __forceinline__ void load_codes_i8(const ScaParams& p, int64_t r0, int64_t c0, int8_t* cd, int tid) {
     constexpr int kPer = (kH * kH + 255) / 256;  // 19
     constexpr int kHalf = (kPer + 1) / 2;          // two groups of loads in flight
+    // An int8 value equals the nodata value exactly when the nodata value is
+    // that integer: the classification stays on the integer pipes.
+    const int ndv = (p.nodata == floor(p.nodata) && p.nodata >= -128.0 && p.nodata <= 127.0) ? (int)p.nodata : 1000;
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         int v[kHalf];
@@ -87,14 +90,16 @@ __device__ __forceinline__ void load_codes_i8(const ScaParams& p, int64_t r0, in
         for (int q = 0; q < kHalf; q++) {
             const int i = tid + (h * kHalf + q) * 256;
             const int64_t r = r0 + i / kH, c = c0 + i % kH;
-            v[q] = 256;  // outside: not a byte value
+            v[q] = ndv;  // outside the raster: nodata
             if (i < kH * kH && r >= 0 && c >= 0 && r < p.rows && c < p.cols)
                 v[q] = reinterpret_cast<const int8_t*>(p.d8.base + r * p.d8.pitch)[c];
         }
 #pragma unroll
         for (int q = 0; q < kHalf; q++) {
             const int i = tid + (h * kHalf + q) * 256;
-            if (i < kH * kH) cd[i] = v[q] == 256 ? kNodata : classify8(p, (double)v[q]);
+            const int x = v[q];
+            const int8_t k = x == ndv ? kNodata : ((x >= 0 && x <= 8 && x != 4) ? (int8_t)x : kNoFlow);
+            if (i < kH * kH) cd[i] = k;
         }
         asm volatile("" ::: "memory");
     }
@@ -172,6 +177,14 @@ constexpr unsigned long long kXOne = 1ULL << kXCountShift, kXBadOne = 1ULL << kX
 constexpr unsigned long long kXSum = kXBadOne - 1;
 __device__ __forceinline__ unsigned long long xpack(unsigned long long total, unsigned bad) {
     return total | (bad ? kXBadOne : 0ULL);
+}
+
+// The IEEE double of a count below 2^53, built on the integer pipes.
+__device__ __forceinline__ unsigned long long count_bits(unsigned long long x) {
+    if (x == 0) return 0;
+    const int e = 63 - __clzll((long long)x);  // x = 1.m * 2^e
+    const unsigned long long m = (x << (52 - e)) & 0xFFFFFFFFFFFFFULL;
+    return ((unsigned long long)(1023 + e) << 52) | m;
 }
 
 // A cell's in-tile forest as one word: flags (1 valid work cell, 2 "bad"),
@@ -464,7 +477,11 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                     s.conv[g] = tot;
                     s.ship[g] = ok ? (unsigned long long)S.sub_bad(i) : 0ULL;
                 } else {
-                    put_value(p.out, r, c, valid ? (double)tot : p.out.nodata);
+                    if (p.out.dtype == PARGO_F64)  // the count's double from its bits: no FP64 conversion
+                        reinterpret_cast<double*>(p.out.base + r * p.out.pitch)[c] =
+                            valid ? __longlong_as_double((long long)count_bits(tot)) : p.out.nodata;
+                    else
+                        put_value(p.out, r, c, valid ? (double)tot : p.out.nodata);
                     if (r >= lastr - 1 && r <= lastr + 1 && c >= lastc - 1 && c <= lastc + 1) s.conv[g] = tot;
                 }
             }
