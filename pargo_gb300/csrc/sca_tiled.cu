@@ -411,20 +411,16 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             // a pointer is an ancestor of its cell at every moment, so the
             // rounds need no read/write separation.  The last cell keeps its
             // own -1 or -2.  lpar is rebuilt by the final pass.
-            unsigned active = 0xFFFFu;  // this thread's cells tid + 256 q whose pointer may still move
 #pragma unroll 1
             for (int round = 0; round < 12; round++) {
                 int moved = 0;
-                for (unsigned m = active; m; m &= m - 1) {
-                    const int q = __ffs(m) - 1;
-                    const int i = tid + q * kThreads;
-                    const int pq = S.lpar[i];
-                    const int q2 = pq >= 0 ? ((volatile int16_t*)S.lpar)[pq] : -1;
+                for (int i = tid; i < kCells; i += kThreads) {
+                    const int q = S.lpar[i];
+                    if (q < 0) continue;
+                    const int q2 = ((volatile int16_t*)S.lpar)[q];
                     if (q2 >= 0) {
                         S.lpar[i] = (int16_t)q2;
                         moved = 1;
-                    } else {
-                        active &= ~(1u << q);  // at its path's last cell (or the last cell itself)
                     }
                 }
                 if (!__syncthreads_or(moved)) break;  // every pointer is at its path's last cell
