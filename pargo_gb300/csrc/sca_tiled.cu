@@ -14,19 +14,24 @@
 //
 // Phases (one launch each):
 //  1. per 64 x 64 tile (codes with a 2-cell halo in shared memory): the in-tile
-//     forest, its subtree sums by a shared-memory topological walk (in-degree
-//     counters; the last contributor continues), and for every border cell the
-//     exit its in-tile path reaches.  Exits (cells whose parent lies in another
-//     tile) record their in-tile sum and the entry cell they feed.
+//     forest (from byte inflow masks), stored as one word per cell for phase
+//     4; its subtree sums by a shared-memory topological walk (one atomic add
+//     per step on the parent's word of pending children, bad-child count and
+//     sum; the last contributor continues); and for every border cell the
+//     exit its in-tile path reaches, by pointer jumping.  Exits (cells whose
+//     parent lies in another tile) record their in-tile sum and the entry
+//     cell they feed.
 //  2. the exit forest: exit x's parent is the exit reached from the entry x
-//     feeds; its in-degrees.
+//     feeds; its feeding counts, added into the parents' packed words.
 //  3. subtree sums over the exit forest (its leaves marked first, then a
-//     global-memory walk; chains are as long as the tiles a river crosses);
-//     each exit adds its total to the inflow of the entry it feeds.
-//  4. per tile again: the in-tile sums with the entries' inflows added -> the
-//     final counts and flags.
-//  5. output: converged counts, or the shipped sums; the reference's last-cell
-//     quirk (a nodata last work cell accumulates what flows into it).
+//     global-memory walk, again one atomic per step; chains are as long as the
+//     tiles a river crosses); each exit adds its total to the inflow of the
+//     entry it feeds.
+//  4. per tile again, from the stored forest: the in-tile sums with the
+//     entries' inflows added; converged contract: the output itself, then a
+//     one-thread kernel for the reference's last-cell quirk (a nodata last
+//     work cell accumulates what flows into it).
+//  5. shipped contract only: the output pass over the final counts and flags.
 // Cycles (inside a tile or across tiles) and inflows from the raster's ring,
 // which the reference never releases, leave cells or exits uncompleted; the
 // host compares the completion counts.
