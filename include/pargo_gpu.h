@@ -245,7 +245,10 @@ pargo_status pargo_mfd(pargo_ctx* ctx, const pargo_raster* dem, pargo_raster* we
  * that sweep.  Sums are FP64 with the reference's operation order, so the
  * output is bit-identical given the same weights.  weights: 8 rasters (F32 or
  * F64), nodata = |w0 - nodata| < 1e-6; sca: F32 or F64 with weight layer 0's
- * nodata.  PARGO_ERR_CYCLE when the weights hold a cycle. */
+ * nodata.  A cell waits only on the cells before it in raster order, so
+ * weights that form a cycle are evaluated as the sweep evaluates them (a
+ * cycle's cells never pull each other's later inflows) rather than refused;
+ * PARGO_ERR_CYCLE would report a valid cell left unprocessed. */
 pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_raster* sca, const pargo_nbr* nbr,
                            void* stream);
 

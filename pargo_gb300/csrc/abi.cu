@@ -1621,7 +1621,8 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
         if (ht[2] != 0)
             return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: %llu nodata cells carry positive weights", ht[2]);
         if (ht[0] != ht[1])
-            return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: %llu of %llu valid cells processed (cycle)", ht[1], ht[0]);
+            return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: only %llu of %llu valid cells processed",
+                        ht[1], ht[0]);
         return PARGO_OK;
     }
     cudaGetLastError();  // clear the refused launch
@@ -1667,7 +1668,8 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     if (ht[2] != 0)
         return fail(ctx, PARGO_ERR_INVALID_ARG, "sca_mfd: %llu nodata cells carry positive weights", ht[2]);
     if (ht[0] != ht[1])
-        return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: %llu of %llu valid cells processed (cycle)", ht[1], ht[0]);
+        return fail(ctx, PARGO_ERR_CYCLE, "sca_mfd: only %llu of %llu valid cells processed",
+                        ht[1], ht[0]);
     return PARGO_OK;
 }
 

@@ -126,10 +126,9 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdPara
         const int64_t r = i / p.cols, c = i % p.cols;
         const bool work = r >= 1 && c >= 1 && r <= p.rows - 2 && c <= p.cols - 2;
         uint8_t f = 0;
-        int cnt = 0;
         if (work) {
             const bool valid = !w0_nodata(p, r, c);
-            int indeg = 0;
+            int indeg = 0, cnt = 0;
             for (int k = 0; k < 9; k++) {
                 if (k == 4) continue;
                 const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
@@ -148,9 +147,32 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdPara
             }
         }
         p.flags[i] = f;
+    }
+    if (nvalid) atomicAdd(&p.totals[0], nvalid);
+    if (bad) atomicAdd(&p.totals[2], bad);
+}
+
+// What a cell waits for: the sweep pulls an inflow n into c only when n is a
+// source (its sum is 1 from the start) or n precedes c in raster order and
+// is done, so c's sum and flag depend on its inflows at window positions 0-3
+// (NW, N, NE, W) that are valid work cells and not sources, and on nothing
+// that follows it.  cnt = the number of those; cells with none form the first
+// frontier (appended with one atomic per warp).
+__global__ void __launch_bounds__(kThreads) sca_mfd_counts_kernel(const ScaMfdParams p) {
+    const int64_t n = p.rows * p.cols;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / p.cols, c = i % p.cols;
+        const uint8_t f = p.flags[i];
+        int cnt = 0;
+        if (f & kValid) {  // a valid work cell: its 8 neighbours are in the raster
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
+                const uint8_t fq = p.flags[qr * p.cols + qc];  // 0 on the ring
+                if ((fq & kValid) && !(fq & kSource) && positive(p.w[layer_towards_centre(k)], qr, qc)) cnt++;
+            }
+        }
         p.cnt[i] = cnt;
-        // the first frontier: valid cells with no inflow from a valid work cell,
-        // appended with one atomic per warp
         const bool first = (f & kValid) && cnt == 0;
         const unsigned act = __activemask();
         const unsigned m = __ballot_sync(act, first);
@@ -162,8 +184,6 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_init_kernel(const ScaMfdPara
             if (first) p.list_a[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
         }
     }
-    if (nvalid) atomicAdd(&p.totals[0], nvalid);
-    if (bad) atomicAdd(&p.totals[2], bad);
 }
 
 // A weight: whether it is > 0 (positive() above) and its value, from one load.
@@ -211,8 +231,10 @@ __device__ __forceinline__ unsigned sca_mfd_process(const ScaMfdParams& p, int64
         if (!pq[t]) continue;
         const int k = t < 4 ? t : t + 1;
         const int64_t q = i + (int64_t)(k / 3 - 1) * p.cols + (k % 3 - 1);
-        const bool pulled = (fq[t] & kValid) && ((fq[t] & kSource) || (q < i && (fq[t] & kDone)));
-        if (pulled) sum = __dadd_rn(sum, __dmul_rn(sq[t], wq[t]));
+        const bool src = (fq[t] & kSource) != 0;
+        const bool pulled = (fq[t] & kValid) && (src || (q < i && (fq[t] & kDone)));
+        // a source's sum is 1 (it has no inflow), whether or not it has been processed yet
+        if (pulled) sum = __dadd_rn(sum, __dmul_rn(src ? 1.0 : sq[t], wq[t]));
         else done = false;
     }
     p.sca[i] = sum;
@@ -231,7 +253,10 @@ __device__ __forceinline__ unsigned sca_mfd_process(const ScaMfdParams& p, int64
     for (int q = 0; q < 8; q++) {
         const int pos = pos_of_layer(q);
         const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
-        const bool go = po[q] && dr >= 1 && dc >= 1 && dr <= p.rows - 2 && dc <= p.cols - 2 && (fd[q] & kValid);
+        // only receivers that follow this cell in raster order (positions 5-8)
+        // counted it, and only when it is not a source
+        const bool go = !(fi & kSource) && pos > 4 && po[q] && dr >= 1 && dc >= 1 && dr <= p.rows - 2 &&
+                        dc <= p.cols - 2 && (fd[q] & kValid);
         left[q] = go ? atomicSub(&p.cnt[dr * p.cols + dc], 1) : 0;
     }
     unsigned ready = 0;
@@ -396,6 +421,8 @@ cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t
     if (e != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(p.totals, 0, 4 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
     sca_mfd_init_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    sca_mfd_counts_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
