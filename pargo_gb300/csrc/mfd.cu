@@ -15,14 +15,18 @@
 // the reference makes ONE raster-order accumulation sweep, in which a cell
 // adds sca(n) w(n -> cell) for each inflow n whose degree is 0 at that moment
 // -- a source, or an earlier cell that pulled all its own inflows ("done").
-// Here the same sums are evaluated in topological order: a cell is processed
-// once every inflow from a valid work cell is processed (in-degree counters;
-// the thread that releases a cell's last inflow processes it next, see the
-// walk form below); it then adds, in the reference's window order and in
-// FP64 with separately rounded products and sums, the inflows the sweep pulls
-// (source, or earlier in raster order and done), so with the same weights the
-// result equals the reference's bit for bit.  Inflows from cells that are
-// never processed (the ring, nodata) are never pulled.
+// Here the same sums are evaluated in dependency order: the sweep can pull
+// only sources (whose sum is 1 from the start) and earlier cells, so a cell
+// is processed once its inflows that precede it in raster order and are valid
+// work cells other than sources are processed (counters; the thread that
+// releases a cell's last such inflow processes it next, see the walk form
+// below) -- nothing that follows it, so the chains are the flow paths that
+// keep going forward in raster order (2048^2 hydro: 632 levels, against 3264
+// when every inflow was waited on).  It then adds, in the reference's window
+// order and in FP64 with separately rounded products and sums, the inflows
+// the sweep pulls (source, or earlier in raster order and done), so with the
+// same weights the result equals the reference's bit for bit.  Inflows from
+// cells that are never processed (the ring, nodata) are never pulled.
 
 #include "common.cuh"
 #include "kernels.h"
@@ -33,6 +37,9 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr uint8_t kValid = 1, kSource = 2, kNeverDone = 4, kDone = 8;
+// flag bits 4-7: the receivers at positions 5-8 (layers 4-7) that wait on the
+// cell -- valid work cells its positive weights reach, when it is no source
+constexpr int kReleaseShift = 4;
 
 // window position of c seen from its neighbour at position k, and that
 // neighbour's layer for it
@@ -173,6 +180,18 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_counts_kernel(const ScaMfdPa
             }
         }
         p.cnt[i] = cnt;
+        if ((f & kValid) && !(f & kSource)) {
+            unsigned rel = 0;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int pos = pos_of_layer(4 + j);  // 5 .. 8: after the cell in raster order
+                const uint8_t fd = p.flags[i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1)];  // 0 on the ring
+                if ((fd & kValid) && positive(p.w[4 + j], r, c)) rel |= 1u << j;
+            }
+            // only this thread writes this byte; kValid and kSource, which others
+            // read here, keep their values
+            if (rel) p.flags[i] = (uint8_t)(f | (rel << kReleaseShift));
+        }
         const bool first = (f & kValid) && cnt == 0;
         const unsigned act = __activemask();
         const unsigned m = __ballot_sync(act, first);
@@ -184,6 +203,12 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_counts_kernel(const ScaMfdPa
             if (first) p.list_a[base + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
         }
     }
+}
+
+// the cell of layer q's receiver
+__device__ __forceinline__ int64_t receiver(const ScaMfdParams& p, int64_t i, int q) {
+    const int pos = pos_of_layer(q);
+    return i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1);
 }
 
 // A weight: whether it is > 0 (positive() above) and its value, from one load.
@@ -239,36 +264,16 @@ __device__ __forceinline__ unsigned sca_mfd_process(const ScaMfdParams& p, int64
     }
     p.sca[i] = sum;
     p.flags[i] = fi | (done ? kDone : 0);
-    bool po[8];
-    uint8_t fd[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-        (void)weight_at(p.w[q], r, c, po[q]);
-        const int pos = pos_of_layer(q);
-        fd[q] = p.flags[i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1)];
-    }
     __threadfence();  // this cell's sum and flag before the counters that release its receivers
-    int left[8];
+    // the receivers that counted this cell (set up front in its flags)
+    const unsigned rel = fi >> kReleaseShift;
+    int left[4];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int pos = pos_of_layer(q);
-        const int64_t dr = r + pos / 3 - 1, dc = c + pos % 3 - 1;
-        // only receivers that follow this cell in raster order (positions 5-8)
-        // counted it, and only when it is not a source
-        const bool go = !(fi & kSource) && pos > 4 && po[q] && dr >= 1 && dc >= 1 && dr <= p.rows - 2 &&
-                        dc <= p.cols - 2 && (fd[q] & kValid);
-        left[q] = go ? atomicSub(&p.cnt[dr * p.cols + dc], 1) : 0;
-    }
+    for (int j = 0; j < 4; j++) left[j] = (rel >> j) & 1u ? atomicSub(&p.cnt[receiver(p, i, 4 + j)], 1) : 0;
     unsigned ready = 0;
 #pragma unroll
-    for (int q = 0; q < 8; q++) ready |= (left[q] == 1 ? 1u : 0u) << q;
+    for (int j = 0; j < 4; j++) ready |= (left[j] == 1 ? 1u : 0u) << (4 + j);
     return ready;
-}
-
-// the cell of layer q's receiver
-__device__ __forceinline__ int64_t receiver(const ScaMfdParams& p, int64_t i, int q) {
-    const int pos = pos_of_layer(q);
-    return i + (int64_t)(pos / 3 - 1) * p.cols + (pos % 3 - 1);
 }
 
 __device__ __forceinline__ void sca_mfd_cell(const ScaMfdParams& p, int64_t i, int32_t* next, int32_t* next_count) {
@@ -443,7 +448,10 @@ cudaError_t launch_sca_mfd_persistent(const ScaMfdParams& p, int num_sms, cudaSt
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // every block resident: a thread waiting for a queued cell never waits on
     // a block that has not started
-    sca_mfd_walk_kernel<<<(unsigned)(num_sms * per_sm), kThreads, 0, st>>>(p);
+    // one block per SM: more walkers than that only contend for the queue
+    // (8192^2: 64 ms with one block per SM, 77 / 90 / 104 ms with 2 / 3 / 4;
+    // half the SMs, 71 ms)
+    sca_mfd_walk_kernel<<<(unsigned)num_sms, kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
 
