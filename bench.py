@@ -811,8 +811,8 @@ def run_mfd(args, ws, rank, local, side=8192):
         "config": {"workload": "mfd%d: MFD-md weights (exponent 1.1) + MFD SCA on the pit-removed %dx%d hydro "
                                "DEM (seed 1, 30 m cells, float64 levels), 8 float32 layers, float64 SCA"
                                % (side, side, side), "l2": "inputs larger than L2"},
-        "roofline": {"bound": "hbm", "kernel": "sca_mfd_walk_kernel (MFD SCA: threads walk the flow DAG in one "
-                                               "persistent launch)", "achieved": round(achieved, 1),
+        "roofline": {"bound": "hbm", "kernel": "sca_mfd_records_kernel + sca_mfd_band_kernel (MFD SCA: warps walk "
+                                               "32-row bands in step)", "achieved": round(achieved, 1),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 5), "peak_source": kind,
                      "traffic": None, "algorithmic_bytes_per_cell": 40, "sca_ms": round(ms_s, 3),
                      "sca_share_of_step": round(ms_s / ms, 4) if ms > 0 else None,

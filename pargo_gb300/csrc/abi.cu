@@ -68,7 +68,7 @@ enum SlotId {
     kSlotPipeD8, kSlotPipeSca, kSlotPipeCodes, kSlotScaTiles, kSlotMfdLayer0,
     kSlotMfdCnt = kSlotMfdLayer0 + 8, kSlotMfdFlags, kSlotMfdSca, kSlotMfdLists, kSlotStripSlow, kSlotLoadRows,
     kSlotBatchStripMaps, kSlotBatchSegStart, kSlotBatchNstrips, kSlotBatchSlow, kSlotFillMosaic, kSlotFillItems,
-    kSlotBatchSegLoad, kSlotBatchOrder, kSlotScaForest, kSlotCount
+    kSlotBatchSegLoad, kSlotBatchOrder, kSlotScaForest, kSlotMfdRecords, kSlotCount
 };
 static_assert(kSlotCount <= 48, "context slot table");
 
@@ -1606,13 +1606,17 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     p.barrier = (unsigned int*)(lists + 3 * n + 4);
     p.totals = (unsigned long long*)(((uintptr_t)(lists + 3 * n + 8) + 7) & ~(uintptr_t)7);
     p.error_flag = ctx->d_error;
+    bool f32 = true;
+    for (int q = 0; q < 8; q++) f32 = f32 && p.w[q].dtype == PARGO_F32;
+    void* records = slot(ctx, kSlotMfdRecords, sca_mfd_band_bytes(p.rows, p.cols, f32), &e);
+    if (!records) return cuda_fail(ctx, e, "sca_mfd records");
     CU(ctx, launch_sca_mfd_init(p, ctx->num_sms, s));
     int32_t* hc = (int32_t*)pinned(ctx, 128, &e);
     if (!hc) return cuda_fail(ctx, e, "pinned counters");
-    // One persistent launch in which threads walk the flow DAG (a cell is
-    // processed by the thread that released its last inflow); where that
-    // launch cannot run, frontier rounds as CUDA graphs.
-    if (launch_sca_mfd_persistent(p, ctx->num_sms, s) == cudaSuccess) {
+    // Warps walk 32-row bands in step (every dependency of the reference's
+    // sweep points forward in raster order); the band cursor and the bands'
+    // progress words live in the list scratch, which this form does not use.
+    if (launch_sca_mfd_band(p, records, lists, ctx->num_sms, s) == cudaSuccess) {
         CU(ctx, launch_sca_mfd_output(p, ctx->num_sms, s));
         if ((st = unstage_out(ctx, so, s)) != PARGO_OK) return st;
         unsigned long long* ht = (unsigned long long*)(hc + 8);
@@ -1628,6 +1632,7 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     cudaGetLastError();  // clear the refused launch
     // Frontier rounds, 32 per CUDA graph (an even number: list A is current
     // again after each graph), until both lists are empty.
+    CU(ctx, launch_sca_mfd_counts(p, ctx->num_sms, s));
     constexpr int kRounds = 32;
     CU(ctx, cudaEventRecord(ctx->ev_a, s));
     CU(ctx, cudaStreamWaitEvent(ctx->own, ctx->ev_a, 0));

@@ -253,17 +253,20 @@ struct ScaMfdParams {
     int32_t* list_c;               // spare list
     int32_t* counts;               // [0] length of list_a, [1] of list_b, [2] finished blocks / list_b claims, [3] list_a claims
     unsigned long long* totals;    // [0] valid cells, [1] processed cells, [2] nodata cells with weights
-    unsigned int* barrier;         // [0] pending ready cells (walk form)
-    int* error_flag;               // a bounded wait of the walk form gave up
+    unsigned int* barrier;         // unused
+    int* error_flag;               // a bounded wait of the band form gave up
 };
 cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t st);
+// The round form's counters and first frontier (after the init).
+cudaError_t launch_sca_mfd_counts(const ScaMfdParams& p, int num_sms, cudaStream_t st);
 cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms, cudaStream_t st);
 cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st);
-// The walk form: one persistent launch (every block resident) in which a
-// thread goes on with the cell its processing made ready; returns an error
-// (and launches nothing) when the kernel cannot be made resident, so the
-// caller can take the per-round launches instead.
-cudaError_t launch_sca_mfd_persistent(const ScaMfdParams& p, int num_sms, cudaStream_t st);
+// The band form (every dependency of the sweep points forward in raster
+// order): per-cell records, then warps walking 32-row bands in step.
+// `records`: sca_mfd_band_bytes(rows, cols, all weights F32) bytes; `words`:
+// 1 + ceil((rows - 2) / 32) ints.
+size_t sca_mfd_band_bytes(int64_t rows, int64_t cols, bool f32);
+cudaError_t launch_sca_mfd_band(const ScaMfdParams& p, void* records, int* words, int num_sms, cudaStream_t st);
 
 // grad.cu
 struct GradParams {

@@ -17,16 +17,16 @@
 // -- a source, or an earlier cell that pulled all its own inflows ("done").
 // Here the same sums are evaluated in dependency order: the sweep can pull
 // only sources (whose sum is 1 from the start) and earlier cells, so a cell
-// is processed once its inflows that precede it in raster order and are valid
-// work cells other than sources are processed (counters; the thread that
-// releases a cell's last such inflow processes it next, see the walk form
-// below) -- nothing that follows it, so the chains are the flow paths that
-// keep going forward in raster order (2048^2 hydro: 632 levels, against 3264
-// when every inflow was waited on).  It then adds, in the reference's window
-// order and in FP64 with separately rounded products and sums, the inflows
-// the sweep pulls (source, or earlier in raster order and done), so with the
-// same weights the result equals the reference's bit for bit.  Inflows from
-// cells that are never processed (the ring, nodata) are never pulled.
+// needs only its NW, N, NE and W neighbours' sums and done flags -- nothing
+// that follows it.  The band form below walks 32-row bands in step on that
+// structure; the round form (frontier rounds over counters of those earlier
+// inflows, a fallback where the band launch cannot be configured) processes
+// a cell once they are processed.  Either then adds, in the reference's
+// window order and in FP64 with separately rounded products and sums, the
+// inflows the sweep pulls (source, or earlier in raster order and done), so
+// with the same weights the result equals the reference's bit for bit.
+// Inflows from cells that are never processed (the ring, nodata) are never
+// pulled.
 
 #include "common.cuh"
 #include "kernels.h"
@@ -314,89 +314,200 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdPar
     }
 }
 
-constexpr long long kWaitBudget = 4000000000LL;  // ~2 s of SM clocks without a queued cell arriving
+// ---------------------------------------------------------- band form --
+// Every dependency of the sweep points forward in raster order: a cell needs
+// only its NW, N, NE and W neighbours' sums and done flags (the sources
+// anywhere count as 1).  A warp takes a band of 32 rows; lane L walks row
+// R0 + L, two columns behind lane L - 1 (at step s it is at column
+// 1 + s - 2L), so the three upper neighbours of its cell are the results of
+// lane L - 1's last three steps (shuffles) and the left one is its own last
+// result.  Lane 0's upper row is the previous band's last row, read from
+// global memory in chunks of 32 columns once that band has published them
+// (bands are taken in order, so the band waited on is running or done).
+// A cell's static data -- the 8 inflow weights and the valid / source /
+// positive masks of its neighbours -- is gathered first into one record per
+// cell (sca_mfd_records_kernel) and streamed by each lane a few steps ahead
+// with asynchronous copies.
 
-// Walk form, one persistent launch with every block resident.  A thread takes
-// a ready cell (the first frontier, then cells queued by other threads),
-// processes it, and goes on at once with a receiver this made ready -- its
-// last inflow is then final -- queuing any further ready receivers; a
-// thread's walk follows the flow down the DAG, so no round waits on the
-// slowest cell of a level.  Each cell is processed once, after all its
-// inflows (their counters), so the sums are those of the rounds.
-//   counts[0]  cells of the first frontier (list_a), from the init kernel
-//   counts[3]  claimed from list_a
-//   counts[1]  queued in list_b (each cell at most once: room for every cell)
-//   counts[2]  claimed from list_b
-//   barrier[0] pending: ready cells not yet finished, raised before a cell is
-//              queued and lowered when a walk ends -- zero exactly when every
-//              ready cell is done.
-// list_b starts filled with -1; a claimed position is waited on until its
-// cell is written (bounded: the error flag ends the launch).
-__global__ void sca_mfd_walk_setup_kernel(const ScaMfdParams p) {
-    p.barrier[0] = (unsigned int)p.counts[0];
-    p.counts[1] = 0;
-    p.counts[2] = 0;
-    p.counts[3] = 0;
-}
-
-__device__ int64_t walk_claim(const ScaMfdParams& p, int64_t n) {
-    const int32_t a = atomicAdd(&p.counts[3], 1);
-    if (a < *((volatile int32_t*)&p.counts[0])) return p.list_a[a];
-    const int32_t b = atomicAdd(&p.counts[2], 1);
-    const long long t0 = clock64();
-    unsigned ns = 32;
-    for (;;) {
-        if (b < n) {
-            const int32_t v = *((volatile int32_t*)&p.list_b[b]);
-            if (v >= 0) return v;
-        }
-        if (*((volatile unsigned int*)&p.barrier[0]) == 0) return -1;  // every ready cell done
-        if (*((volatile int*)p.error_flag) != 0) return -1;
-        if (clock64() - t0 > kWaitBudget) {
-            atomicExch(p.error_flag, 1);
-            return -1;
-        }
-        __nanosleep(ns);
-        if (ns < 1024) ns *= 2;
-    }
-}
-
-__global__ void __launch_bounds__(kThreads) sca_mfd_walk_kernel(const ScaMfdParams p) {
+// rm bits: 0-3 the cell's own static flags; 8-15 positive inflow weight from
+// neighbour t (window order t = 0..7: positions 0-3, 5-8); 16-23 that
+// neighbour is a valid work cell; 24-31 it is a source.
+template <typename WT>
+__global__ void __launch_bounds__(kThreads) sca_mfd_records_kernel(const ScaMfdParams p, WT* rw, uint32_t* rm) {
     const int64_t n = p.rows * p.cols;
-    unsigned long long done_cells = 0;
-    for (;;) {
-        int64_t cell = walk_claim(p, n);
-        if (cell < 0) break;
-        while (cell >= 0) {
-            __threadfence();  // the released inflows' sums and flags are visible
-            unsigned ready = sca_mfd_process(p, cell);
-            done_cells++;
-            const int nr = __popc(ready);
-            int64_t next = -1;
-            if (nr) {
-                const int q0 = __ffs(ready) - 1;
-                next = receiver(p, cell, q0);
-                ready &= ready - 1;
-                if (nr > 1) {
-                    __threadfence();  // what released these cells is visible to whoever takes them
-                    atomicAdd(&p.barrier[0], (unsigned int)(nr - 1));  // raised before the cells are queued
-                    const int32_t pos = atomicAdd(&p.counts[1], nr - 1);
-                    int k = 0;
-                    while (ready) {
-                        const int q = __ffs(ready) - 1;
-                        ready &= ready - 1;
-                        if (pos + k < n) atomicExch(&p.list_b[pos + k], (int32_t)receiver(p, cell, q));
-                        k++;
-                    }
-                }
-            } else {
-                atomicAdd(&p.barrier[0], 0xFFFFFFFFu);  // this walk ends: one pending cell fewer
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t fi = p.flags[i];
+        uint32_t m = 0;
+        if (fi & kValid) {  // a valid work cell: its 8 neighbours are in the raster
+            const int64_t r = i / p.cols, c = i % p.cols;
+            m = fi & 0x0Fu;
+#pragma unroll
+            for (int t = 0; t < 8; t++) {
+                const int k = t < 4 ? t : t + 1;
+                const int64_t qr = r + k / 3 - 1, qc = c + k % 3 - 1;
+                bool pos;
+                const double w = weight_at(p.w[layer_towards_centre(k)], qr, qc, pos);
+                const uint8_t fq = p.flags[qr * p.cols + qc];
+                rw[i * 8 + t] = pos ? (WT)w : (WT)0;  // exact: WT is the weights' own type
+                m |= (pos ? 1u : 0u) << (8 + t);
+                m |= ((fq & kValid) ? 1u : 0u) << (16 + t);
+                m |= ((fq & kSource) ? 1u : 0u) << (24 + t);
             }
-            cell = next;
         }
+        rm[i] = m;
     }
-    const unsigned dc = __reduce_add_sync(__activemask(), (unsigned)done_cells);
-    if ((threadIdx.x & 31) == __ffs(__activemask()) - 1 && dc) atomicAdd(&p.totals[1], (unsigned long long)dc);
+}
+
+constexpr int kBandRows = 32;
+constexpr int kBandPre = 8;    // record slots a lane has in flight (16 measured no faster)
+constexpr int kBandWarps = 4;  // bands (warps) per block
+constexpr int kBandChunk = 8;  // columns of the previous band's last row published and read at a time
+constexpr long long kBandPatience = 4000000000LL;  // ~2 s of SM clocks without the previous band moving
+
+template <typename WT>
+struct BandSmem {
+    WT w[kBandPre][8][32];              // [slot][t][lane]
+    uint32_t m[kBandPre][32];
+    double up[64];                      // the previous band's last row, a ring of 64 columns
+    uint8_t upd[64];                    // its done flags
+};
+
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+
+// One warp per band; kBandWarps warps per block, each with its own smem.
+template <typename WT>
+__global__ void __launch_bounds__(kBandWarps * 32) sca_mfd_band_kernel(const ScaMfdParams p, const WT* rw, const uint32_t* rm,
+                                                               int* band_next, int* prog, int nbands) {
+    extern __shared__ __align__(16) unsigned char band_smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    BandSmem<WT>& S = reinterpret_cast<BandSmem<WT>*>(band_smem)[wid];
+    const int64_t cols = p.cols, last_col = p.cols - 2;  // work columns 1 .. cols - 2
+    const int64_t nsteps = last_col + 2 * (kBandRows - 1);
+    unsigned long long processed = 0;
+    bool failed = false;
+    for (;;) {
+        int b = 0;
+        if (lane == 0) b = atomicAdd(band_next, 1);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b >= nbands || failed) break;
+        const int64_t R0 = 1 + (int64_t)b * kBandRows, r = R0 + lane;
+        const bool row_ok = r <= p.rows - 2;
+        // the previous band's last row (row R0 - 1), chunk j = columns 8j .. 8j + 7
+        auto load_chunk = [&](int64_t j) -> bool {
+            const int64_t c_hi = min(kBandChunk * j + kBandChunk - 1, last_col);
+            if (b > 0 && c_hi >= 1) {
+                if (lane == 0) {
+                    const long long t0 = clock64();
+                    while (*((volatile int*)&prog[b - 1]) < c_hi) {
+                        if (*((volatile int*)p.error_flag) != 0 || clock64() - t0 > kBandPatience) {
+                            atomicExch(p.error_flag, 1);
+                            failed = true;
+                            break;
+                        }
+                        __nanosleep(20);  // the band above is a few steps ahead: short sleeps
+                    }
+                    __threadfence();
+                }
+                failed = __shfl_sync(0xffffffffu, failed, 0);
+            }
+            const int64_t c = kBandChunk * j + lane;
+            double v = 0.0;
+            uint8_t d = 0;
+            if (lane < kBandChunk && b > 0 && !failed && c >= 1 && c <= last_col) {
+                const int64_t g = (R0 - 1) * cols + c;
+                v = __ldcg(p.sca + g);
+                d = (__ldcg(reinterpret_cast<const unsigned*>(p.flags + (g & ~3LL))) >> (8 * (g & 3))) & kDone;
+            }
+            if (lane < kBandChunk) {
+                S.up[c & 63] = v;
+                S.upd[c & 63] = d;
+            }
+            __syncwarp();
+            return !failed;
+        };
+        // the record of this lane's cell at step s into slot s % kBandPre
+        auto fetch = [&](int64_t s) {
+            const int slot = (int)(s % kBandPre);
+            const int64_t c = 1 + s - 2 * lane;
+            if (row_ok && c >= 1 && c <= last_col) {
+                const int64_t i = r * cols + c;
+#pragma unroll
+                for (int t = 0; t < 8; t++) {
+                    if (sizeof(WT) == 8) cp_async8(&S.w[slot][t][lane], rw + i * 8 + t);
+                    else cp_async4(&S.w[slot][t][lane], rw + i * 8 + t);
+                }
+                cp_async4(&S.m[slot][lane], rm + i);
+            } else {
+                S.m[slot][lane] = 0;  // no cell: nothing to process
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        };
+        if (!load_chunk(0)) break;
+        for (int64_t s = 0; s < kBandPre - 1; s++) fetch(s);
+        double h0 = 0.0, h1 = 0.0, h2 = 0.0;  // this lane's results at steps s-1, s-2, s-3
+        unsigned hd = 0;                        // their done flags: bit 0 = s-1, bit 1 = s-2, bit 2 = s-3
+        for (int64_t s = 0; s < nsteps; s++) {
+            if ((s % kBandChunk) == 0 && !load_chunk(s / kBandChunk + 1)) break;
+            fetch(s + kBandPre - 1);
+            asm volatile("cp.async.wait_group %0;\n" ::"n"(kBandPre - 1) : "memory");
+            // upper neighbours at columns c-1, c, c+1: lane L-1's last three results
+            double u0 = __shfl_up_sync(0xffffffffu, h2, 1), u1 = __shfl_up_sync(0xffffffffu, h1, 1),
+                   u2 = __shfl_up_sync(0xffffffffu, h0, 1);
+            unsigned ud = __shfl_up_sync(0xffffffffu, hd, 1);  // bit 2: c-1, bit 1: c, bit 0: c+1
+            const int64_t c = 1 + s - 2 * lane;
+            if (lane == 0) {  // the previous band's last row, columns s .. s + 2
+                u0 = S.up[s & 63];
+                u1 = S.up[(s + 1) & 63];
+                u2 = S.up[(s + 2) & 63];
+                ud = (S.upd[s & 63] ? 4u : 0u) | (S.upd[(s + 1) & 63] ? 2u : 0u) | (S.upd[(s + 2) & 63] ? 1u : 0u);
+            }
+            const int slot = (int)(s % kBandPre);
+            const uint32_t m = S.m[slot][lane];
+            double sum = 0.0;
+            bool done = false;
+            if (m & kValid) {
+                sum = 1.0;
+                // the inflows the sweep pulls: valid and a source, or one of the
+                // earlier four (NW, N, NE, W) and done
+                const unsigned pos = (m >> 8) & 0xFFu, val = (m >> 16) & 0xFFu, src = (m >> 24) & 0xFFu;
+                const unsigned dn = ((ud >> 2) & 1u) | (((ud >> 1) & 1u) << 1) | ((ud & 1u) << 2) | ((hd & 1u) << 3);
+                unsigned pulled = pos & val & (src | dn);
+                done = !(m & kNeverDone) && pulled == pos;
+                while (pulled) {  // in window order, as the reference sweeps it
+                    const int t = __ffs(pulled) - 1;
+                    pulled &= pulled - 1;
+                    const double x = (src >> t) & 1u ? 1.0 : t == 0 ? u0 : t == 1 ? u1 : t == 2 ? u2 : h0;
+                    sum = __dadd_rn(sum, __dmul_rn(x, (double)S.w[slot][t][lane]));
+                }
+                const int64_t g = r * cols + c;
+                p.sca[g] = sum;
+                p.flags[g] = (uint8_t)((m & 0x0Fu) | (done ? kDone : 0));
+                processed++;
+            }
+            h2 = h1;
+            h1 = h0;
+            h0 = sum;
+            hd = ((hd << 1) | (done ? 1u : 0u)) & 7u;
+            // the last lane publishes its row's progress every kBandChunk columns
+            if (lane == kBandRows - 1 && c >= 1 && c <= last_col &&
+                ((c % kBandChunk) == kBandChunk - 1 || c == last_col)) {
+                __threadfence();
+                atomicExch(&prog[b], (int)c);
+            }
+            __syncwarp();
+        }
+        asm volatile("cp.async.wait_all;\n" ::: "memory");
+        __syncwarp();
+    }
+    const unsigned long long tot = __reduce_add_sync(0xffffffffu, (unsigned)processed);
+    if (lane == 0 && tot) atomicAdd(&p.totals[1], tot);
 }
 
 __global__ void __launch_bounds__(kThreads) sca_mfd_output_kernel(const ScaMfdParams p) {
@@ -426,7 +537,10 @@ cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t
     if (e != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(p.totals, 0, 4 * sizeof(unsigned long long), st)) != cudaSuccess) return e;
     sca_mfd_init_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sca_mfd_counts(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
     sca_mfd_counts_kernel<<<(unsigned)blocks_for(p.rows * p.cols, num_sms), kThreads, 0, st>>>(p);
     return cudaGetLastError();
 }
@@ -437,22 +551,41 @@ cudaError_t launch_sca_mfd_round(const ScaMfdParams& p, int parity, int num_sms,
     return cudaGetLastError();
 }
 
-cudaError_t launch_sca_mfd_persistent(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sca_mfd_walk_kernel, kThreads, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorLaunchOutOfResources;
+
+// The band form: records, then one launch of 32-row bands.  `words` holds the
+// band cursor and one progress word per band.
+size_t sca_mfd_band_bytes(int64_t rows, int64_t cols, bool f32) {
+    return (size_t)(rows * cols) * ((f32 ? 4 : 8) * 8 + 4) + 256;
+}
+
+template <typename WT>
+static cudaError_t launch_band(const ScaMfdParams& p, void* records, int* words, int num_sms, cudaStream_t st) {
     const int64_t n = p.rows * p.cols;
-    if ((e = cudaMemsetAsync(p.list_b, 0xFF, (size_t)n * sizeof(int32_t), st)) != cudaSuccess) return e;
-    sca_mfd_walk_setup_kernel<<<1, 1, 0, st>>>(p);
+    WT* rw = reinterpret_cast<WT*>(((uintptr_t)records + 15) & ~(uintptr_t)15);
+    uint32_t* rm = reinterpret_cast<uint32_t*>(rw + n * 8);
+    const int nbands = (int)((p.rows - 2 + kBandRows - 1) / kBandRows);
+    cudaError_t e = cudaMemsetAsync(words, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(words + 1, 0xFF, (size_t)nbands * sizeof(int), st)) != cudaSuccess) return e;
+    sca_mfd_records_kernel<WT><<<(unsigned)blocks_for(n, num_sms), kThreads, 0, st>>>(p, rw, rm);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    // every block resident: a thread waiting for a queued cell never waits on
-    // a block that has not started
-    // one block per SM: more walkers than that only contend for the queue
-    // (8192^2: 64 ms with one block per SM, 77 / 90 / 104 ms with 2 / 3 / 4;
-    // half the SMs, 71 ms)
-    sca_mfd_walk_kernel<<<(unsigned)num_sms, kThreads, 0, st>>>(p);
+    const int smem = kBandWarps * (int)sizeof(BandSmem<WT>);
+    if ((e = cudaFuncSetAttribute(sca_mfd_band_kernel<WT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)) !=
+        cudaSuccess)
+        return e;
+    // enough warps for every band at once (bands are taken in order, so none
+    // waits on a band no warp has taken)
+    int64_t blocks = (nbands + kBandWarps - 1) / kBandWarps;
+    if (blocks < num_sms) blocks = num_sms;
+    sca_mfd_band_kernel<WT><<<(unsigned)blocks, kBandWarps * 32, smem, st>>>(p, rw, rm, words, words + 1, nbands);
     return cudaGetLastError();
+}
+
+cudaError_t launch_sca_mfd_band(const ScaMfdParams& p, void* records, int* words, int num_sms, cudaStream_t st) {
+    if (p.rows < 3 || p.cols < 3) return cudaSuccess;  // no work cell
+    bool f32 = true;
+    for (int q = 0; q < 8; q++) f32 = f32 && p.w[q].dtype == PARGO_F32;
+    return f32 ? launch_band<float>(p, records, words, num_sms, st) : launch_band<double>(p, records, words, num_sms, st);
 }
 
 cudaError_t launch_sca_mfd_output(const ScaMfdParams& p, int num_sms, cudaStream_t st) {
