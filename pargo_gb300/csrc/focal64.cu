@@ -86,34 +86,44 @@ __device__ __noinline__ CellOut cell_general64(double z0, double z1, double z2, 
 
 constexpr int kNoBinade = -1000000;
 
-// Keys of row `ty` (tile-local) for this lane's columns 2l-1 .. 2l+2, and the
-// row's common binade (kNoBinade when the four differ, when one may be nodata,
-// or when the binade's ulp scale does not fit a normal float).  Within one
-// binade (equal key >> 52: sign and exponent) key differences are the exact
-// value differences in units of the binade's ulp, of either sign.
+// Keys of row `ty` (tile-local) for this lane's columns 2l-1 .. 2l+2, the
+// common binade of each of its two cells' three columns (kNoBinade when they
+// differ, when one may be nodata, or when the binade's ulp scale does not fit
+// a normal float), and which columns hold +inf.  Within one binade (equal
+// key >> 52: sign and exponent) key differences are the exact value
+// differences in units of the binade's ulp, of either sign.
 constexpr long long kInfKey = 0x7FF0000000000000LL;  // key of +inf: the pipeline levels' nodata
 
-__device__ __forceinline__ int load_keys(const double* s, int ty, int lane, long long k[4], const Focal64Params& P,
-                                         int klo, int khi, bool& all_inf) {
+struct RowKeys {
+    int t0, t1;    // the common binade of columns 0-2 (cell 0's window) and 1-3 (cell 1's), else kNoBinade
+    unsigned inf;  // bit a: column a holds +inf (a nodata level of the pipeline)
+};
+__device__ __forceinline__ RowKeys load_keys(const double* s, int ty, int lane, long long k[4], const Focal64Params& P,
+                                             int klo, int khi) {
     const double* row = s + (ty + 1) * kBoxW + 2 * lane + 1;  // column 2l-1 sits at box column 2l+1
     const double2 q = *reinterpret_cast<const double2*>(row + 1);
     k[0] = dkey64(row[0]);
     k[1] = dkey64(q.x);
     k[2] = dkey64(q.y);
     k[3] = dkey64(row[3]);
-    all_inf = k[0] == kInfKey && k[1] == kInfKey && k[2] == kInfKey && k[3] == kInfKey;
-    const int t = (int)(k[0] >> 52);
-    bool ok = (int)(k[1] >> 52) == t && (int)(k[2] >> 52) == t && (int)(k[3] >> 52) == t;
-    const int e = t >= 0 ? t : -1 - t;  // biased exponent
-    ok = ok && e >= 960 && e <= 1190;   // 2^(1075 - e) and 2^(e - 1075) are normal floats; no inf/NaN
-    if (!P.nodata_is_inf) {
+    RowKeys o;
+    int t[4];
+    bool ok[4];
+    o.inf = 0;
 #pragma unroll
-        for (int a = 0; a < 4; a++) {
+    for (int a = 0; a < 4; a++) {
+        t[a] = (int)(k[a] >> 52);
+        const int e = t[a] >= 0 ? t[a] : -1 - t[a];  // biased exponent
+        ok[a] = e >= 960 && e <= 1190;  // 2^(1075 - e) and 2^(e - 1075) are normal floats; no inf/NaN
+        if (!P.nodata_is_inf) {
             const int hi = (int)(k[a] >> 32);
-            ok = ok && !(hi >= klo && hi <= khi);
+            ok[a] = ok[a] && !(hi >= klo && hi <= khi);
         }
+        o.inf |= (k[a] == kInfKey ? 1u : 0u) << a;
     }
-    return ok ? t : kNoBinade;
+    o.t0 = ok[0] && ok[1] && ok[2] && t[1] == t[0] && t[2] == t[0] ? t[0] : kNoBinade;
+    o.t1 = ok[1] && ok[2] && ok[3] && t[2] == t[1] && t[3] == t[1] ? t[1] : kNoBinade;
+    return o;
 }
 
 // An exact int64 difference (|d| < 2^53) as a float without the 64-bit
@@ -180,9 +190,8 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
     const float slope_nd = (float)p.slope.nodata;  // nodata outputs, converted once
     const int d8_nd = (int)p.d8.nodata;
     long long ka[4], kb[4], kc[4];
-    bool ia, ib, ic;  // rows made only of +inf levels (inside a nodata region of the pipeline)
-    int ta = load_keys(s, r0 - 1, lane, ka, P, klo, khi, ia);
-    int tb = load_keys(s, r0, lane, kb, P, klo, khi, ib);
+    RowKeys ra = load_keys(s, r0 - 1, lane, ka, P, klo, khi);
+    RowKeys rb = load_keys(s, r0, lane, kb, P, klo, khi);
     // the previous row's downward drops seen from this row (negated): S, SE (e1), SW (e2) of row a
     float nS[2], e1p[3], e2p[3];
 #pragma unroll
@@ -192,13 +201,11 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
         e1p[a] = i64f(ka[a] - kb[a + 1]) * kinv;
         e2p[a] = i64f(ka[a + 1] - kb[a]) * kinv;
     }
-    unsigned redo = 0;
+    unsigned redo = 0;  // bit 2i + j: cell j of row i goes to the general path
 #pragma unroll 1
     for (int i = 0; i < kRows; i++) {
-        const int tc = load_keys(s, r0 + i + 1, lane, kc, P, klo, khi, ic);
+        const RowKeys rc = load_keys(s, r0 + i + 1, lane, kc, P, klo, khi);
         const int64_t gy = gy0 + i;
-        const bool fast = interior && ta != kNoBinade && ta == tb && tb == tc;
-        const bool all_nodata = P.nodata_is_inf && ia && ib && ic;  // both windows are nodata
         // drops of row b shared by the cells they join
         float h[3], e1[3], e2[3], vS[2];
 #pragma unroll
@@ -209,14 +216,23 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
         }
 #pragma unroll
         for (int j = 0; j < 2; j++) vS[j] = i64f(kb[j + 1] - kc[j + 1]);
+        const unsigned infs = ra.inf | rb.inf | rc.inf;
         float sl[2] = {0.0f, 0.0f};
         int cd[2] = {0, 0};
-        if (fast) {
-            const int e = ta >= 0 ? ta : -1 - ta;
-            const float unit = __int_as_float((127 + e - 1075) << 23);     // the binade's ulp
-            const float inv_unit = __int_as_float((127 + 1075 - e) << 23);
+        bool nodata[2], gen[2];
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
+        for (int j = 0; j < 2; j++) {
+            // a +inf level in the cell's window makes both outputs nodata, as
+            // the general path's nodata bands do; else the integer path when
+            // the window lies in one binade
+            nodata[j] = P.nodata_is_inf && ((infs >> j) & 7u) != 0;
+            const int ta = j ? ra.t1 : ra.t0, tb = j ? rb.t1 : rb.t0, tc = j ? rc.t1 : rc.t0;
+            const bool fast = !nodata[j] && interior && ta != kNoBinade && ta == tb && tb == tc;
+            gen[j] = !nodata[j] && !fast;
+            if (fast) {
+                const int e = ta >= 0 ? ta : -1 - ta;
+                const float unit = __int_as_float((127 + e - 1075) << 23);     // the binade's ulp
+                const float inv_unit = __int_as_float((127 + 1075 - e) << 23);
                 if (p.do_slope) {
                     const long long nx = ((ka[j + 2] - ka[j]) + (kc[j + 2] - kc[j])) + 2 * (kb[j + 2] - kb[j]);
                     const long long ny = ((ka[j] - kc[j]) + (ka[j + 2] - kc[j + 2])) + 2 * (ka[j + 1] - kc[j + 1]);
@@ -227,20 +243,20 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
                     cd[j] = d8_fast_scaled(-e1p[j], -nS[j], -e2p[j + 1], h[j], -h[j + 1], e2[j], vS[j], e1[j + 1],
                                            inv_unit);
                     if (cd[j] != kD8Unsure && p.dir_type != 8 && cd[j] >= 0) cd[j] = d8_bit_code(cd[j]);
+                    gen[j] = cd[j] == kD8Unsure;
                 }
             }
+            redo |= (gen[j] ? 1u : 0u) << (2 * i + j);
         }
-        const bool rb = !all_nodata && (!fast || cd[0] == kD8Unsure || cd[1] == kD8Unsure);
-        redo |= (rb ? 1u : 0u) << i;
         if (gy < p.rows) {
 #pragma unroll
             for (int j = 0; j < 2; j++) {
                 const int64_t gx = gx0 + j;
                 if (gx >= p.cols) break;
-                if (all_nodata) {
+                if (nodata[j]) {
                     if (p.do_slope) put_float(p.slope, gy, gx, slope_nd);
                     if (p.do_d8) put_int(p.d8, gy, gx, d8_nd);
-                } else if (!rb) {
+                } else if (!gen[j]) {
                     if (p.do_slope) put_float(p.slope, gy, gx, sl[j]);
                     if (p.do_d8) put_int(p.d8, gy, gx, cd[j]);
                 }
@@ -267,10 +283,8 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
             e1p[a] = e1[a];
             e2p[a] = e2[a];
         }
-        ta = tb;
-        tb = tc;
-        ia = ib;
-        ib = ic;
+        ra = rb;
+        rb = rc;
     }
     // Rows the integer path did not finish: the general FP64 path on the
     // staged window.  Their cells are first gathered across the warp, so the
@@ -282,14 +296,12 @@ __device__ __forceinline__ void compute_tile64(const double* s, int64_t y0, int6
     int n = 0;
 #pragma unroll 1
     for (int i = 0; i < kRows; i++) {
-        const bool rb = (redo >> i) & 1u;
-        const unsigned b = __ballot_sync(0xFFFFFFFFu, rb);
-        if (rb) {
-            const int pos = n + 2 * __popc(b & lt);
-            items[pos] = (uint16_t)((i << 6) | (2 * lane));
-            items[pos + 1] = (uint16_t)((i << 6) | (2 * lane + 1));
-        }
-        n += 2 * __popc(b);
+        const unsigned rd = (redo >> (2 * i)) & 3u;  // this lane's cells of row i
+        const unsigned b1 = __ballot_sync(0xFFFFFFFFu, rd & 1u), b2 = __ballot_sync(0xFFFFFFFFu, rd & 2u);
+        int pos = n + __popc(b1 & lt) + __popc(b2 & lt);
+        if (rd & 1u) items[pos++] = (uint16_t)((i << 6) | (2 * lane));
+        if (rd & 2u) items[pos] = (uint16_t)((i << 6) | (2 * lane + 1));
+        n += __popc(b1) + __popc(b2);
     }
     __syncwarp();
 #pragma unroll 1
