@@ -156,33 +156,43 @@ __global__ void __launch_bounds__(kThreads) slope_grad_kernel(const GradParams p
 }
 
 // TMA-staged form of the same computation, for 16-byte aligned float32
-// inputs: one thread loads the block's z (and z_ref) with its two-cell halo
-// as a 2-D box (72 x 36 floats from column x0 - 4: the box's x coordinate
-// stays 16-byte aligned), the block turns nodata into NaN in place four
-// values at a time, and the A/B and gather phases run as above on the boxes.
-// The per-element address arithmetic and bounds checks of the staging (a
-// quarter of the kernel's instructions; it is issue bound) go away.  Cells
-// outside the raster load as 0 instead of NaN: only ring cells and cells
-// beyond the raster have them in their windows, and those have no slope.
-constexpr int kTBW = kBW + 8;                 // box columns: x0-4 .. x0+67
-constexpr int kTBH = kZH;                     // box rows: y0-2 .. y0+33
+// inputs, on 32 x 60 blocks: one thread loads the block's z (and z_ref) with
+// its two-cell halo as a 2-D box (68 x 36 floats from column x0 - 4: the
+// box's x coordinate stays 16-byte aligned), the block turns nodata into NaN
+// in place four values at a time, and each phase runs on column strips: a
+// thread owns one column of 9 (A, B) rows or 8 output rows and walks down it
+// with a rolling three-row window in registers, so a cell reads its three new
+// values instead of its whole window and no index is divided.  The arithmetic
+// of each cell is that of the form above, in the same order.  Cells outside
+// the raster load as 0 instead of NaN: only ring cells and cells beyond the
+// raster have them in their windows, and those have no slope.
+constexpr int kGH = 32, kGW = 60;             // dL/dz block (60: x0 stays a multiple of 4)
+constexpr int kGAH = kGH + 2, kGAW = kGW + 2;  // A, B with a one-cell halo: 34 x 62
+constexpr int kTBW = kGW + 8;                 // box columns: x0-4 .. x0+63
+constexpr int kTBH = kGH + 4;                 // box rows: y0-2 .. y0+33
 constexpr int kBoxFloats = kTBW * kTBH;
-constexpr int kBoxBytes = kBoxFloats * 4;     // 10368: a multiple of 128
+constexpr int kBoxBytes = kBoxFloats * 4;     // 9792
+// a TMA destination starts on a 128-byte boundary: z_ref's box follows z's
+// at the next one
+constexpr int kBoxStride = (kBoxBytes + 127) / 128 * 128;  // 9856
+static_assert(kBoxStride % 128 == 0 && kBoxStride >= kBoxBytes, "box alignment");
+constexpr int kSegA = 9, kSegO = 8;           // rows per thread: A/B (4 strips of 34), output (4 of 32)
 constexpr long long kWaitBudget = 4000000000LL;
+static_assert(kGAW * 4 <= kThreads && kGW * 4 <= kThreads, "one thread per column strip");
 
 __global__ void __launch_bounds__(kThreads) slope_grad_tma_kernel(const __grid_constant__ CUtensorMap mz,
                                                                   const __grid_constant__ CUtensorMap mr,
                                                                   const GradParams p, int mode, int64_t nbx) {
     extern __shared__ __align__(1024) unsigned char grad_smem[];
     float* bz = reinterpret_cast<float*>(grad_smem);
-    float* br = bz + kBoxFloats;
-    __shared__ float sa[kAH][kAW + 1];
-    __shared__ float sb[kAH][kAW + 1];
+    float* br = reinterpret_cast<float*>(grad_smem + kBoxStride);
+    __shared__ float sa[kGAH][kGAW + 1];
+    __shared__ float sb[kGAH][kGAW + 1];
     __shared__ double red[kThreads / 32];
     __shared__ __align__(8) uint64_t bar;
     const int tid = threadIdx.x;
     const int64_t by = blockIdx.x / nbx, bx = blockIdx.x % nbx;
-    const int64_t y0 = by * kBH, x0 = bx * kBW;
+    const int64_t y0 = by * kGH, x0 = bx * kGW;
     const float kNaN = __int_as_float(0x7FC00000);
     if (tid == 0) {
         tma_prefetch_desc(&mz);
@@ -200,10 +210,9 @@ __global__ void __launch_bounds__(kThreads) slope_grad_tma_kernel(const __grid_c
         return;
     }
     // nodata (Eps 1e-7) as NaN, four values at a time
-    {
-        float4* z4 = reinterpret_cast<float4*>(bz);
-        const int n4 = (mode == 0 ? 2 : 1) * kBoxFloats / 4;  // br follows bz
-        for (int i = tid; i < n4; i += kThreads) {
+    for (int box = 0; box < (mode == 0 ? 2 : 1); box++) {
+        float4* z4 = reinterpret_cast<float4*>(box ? br : bz);
+        for (int i = tid; i < kBoxFloats / 4; i += kThreads) {
             float4 v = z4[i];
             v.x = p.nd7f.has(v.x) ? kNaN : v.x;
             v.y = p.nd7f.has(v.y) ? kNaN : v.y;
@@ -213,54 +222,85 @@ __global__ void __launch_bounds__(kThreads) slope_grad_tma_kernel(const __grid_c
         }
     }
     __syncthreads();
+    // A and B on the 34 x 62 cells around the block: cell (a, b) is raster
+    // (y0 - 1 + a, x0 - 1 + b), its window the box's rows a .. a+2, columns
+    // b+2 .. b+4.  Thread: column b = tid % 62, rows 9k .. 9k + 8.
     float lsum = 0.0f;
-    for (int i = tid; i < kAH * kAW; i += kThreads) {
-        const int a = i / kAW, b = i % kAW;  // cell (y0 - 1 + a, x0 - 1 + b); its window starts at box (a, b + 2)
-        const int64_t r = y0 - 1 + a, c = x0 - 1 + b;
-        float A = 0.0f, B = 0.0f;
-        const bool inner = r >= 1 && c >= 1 && r <= p.rows - 2 && c <= p.cols - 2;
-        const float* wz = bz + a * kTBW + b + 2;
-        float nx, ny;
-        numerators(wz, kTBW, nx, ny);
-        const float q = __fmaf_rn(nx, nx, __fmul_rn(ny, ny));
-        if (inner && wz[kTBW + 1] == wz[kTBW + 1] && q == q) {  // centre and neighbours valid
-            const float s = horn_slope(nx, ny, p.k_fd);
-            float g = 0.0f;
-            bool have = true;
-            if (mode == 0) {
-                const float* wr = br + a * kTBW + b + 2;
-                float mx, my;
-                numerators(wr, kTBW, mx, my);
-                const float sref = horn_slope(mx, my, p.k_fd);
-                have = wr[kTBW + 1] == wr[kTBW + 1] && sref == sref;
-                if (have) {
-                    const float d = s - sref;
-                    g = 2.0f * d;
-                    if (a >= 1 && b >= 1 && a <= kBH && b <= kBW) lsum += d * d;
-                }
-            } else {
-                g = load_f32(p.gslope, r, c);
-            }
-            if (have && q > 0.0f) {  // subgradient 0 at zero slope
-                const float f = g * p.k_fd * rsqrtf(q);
-                A = f * nx;
-                B = f * ny;
-            }
+    if (tid < kGAW * 4) {
+        const int b = tid % kGAW, a0 = (tid / kGAW) * kSegA, a1 = min(a0 + kSegA, kGAH);
+        const int64_t c = x0 - 1 + b;
+        const bool col_in = c >= 1 && c <= p.cols - 2;
+        const float* wz = bz + a0 * kTBW + b + 2;
+        const float* wr = br + a0 * kTBW + b + 2;
+        float z0 = wz[0], z1 = wz[1], z2 = wz[2], z3 = wz[kTBW], z4 = wz[kTBW + 1], z5 = wz[kTBW + 2];
+        float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, r3 = 0.0f, r4 = 0.0f, r5 = 0.0f;
+        if (mode == 0) {
+            r0 = wr[0], r1 = wr[1], r2 = wr[2], r3 = wr[kTBW], r4 = wr[kTBW + 1], r5 = wr[kTBW + 2];
         }
-        sa[a][b] = A;
-        sb[a][b] = B;
+        for (int a = a0; a < a1; a++) {
+            const float* nz = bz + (a + 2) * kTBW + b + 2;  // the window's third row
+            const float z6 = nz[0], z7 = nz[1], z8 = nz[2];
+            const int64_t r = y0 - 1 + a;
+            float A = 0.0f, B = 0.0f;
+            const bool inner = col_in && r >= 1 && r <= p.rows - 2;
+            const float nx = __fmaf_rn(2.0f, __fsub_rn(z5, z3), __fadd_rn(__fsub_rn(z2, z0), __fsub_rn(z8, z6)));
+            const float ny = __fmaf_rn(2.0f, __fsub_rn(z1, z7), __fadd_rn(__fsub_rn(z0, z6), __fsub_rn(z2, z8)));
+            const float q = __fmaf_rn(nx, nx, __fmul_rn(ny, ny));
+            float r6 = 0.0f, r7 = 0.0f, r8 = 0.0f;
+            if (mode == 0) {
+                const float* nr = br + (a + 2) * kTBW + b + 2;
+                r6 = nr[0], r7 = nr[1], r8 = nr[2];
+            }
+            if (inner && z4 == z4 && q == q) {  // centre and neighbours valid
+                const float s = horn_slope(nx, ny, p.k_fd);
+                float g = 0.0f;
+                bool have = true;
+                if (mode == 0) {
+                    const float mx = __fmaf_rn(2.0f, __fsub_rn(r5, r3), __fadd_rn(__fsub_rn(r2, r0), __fsub_rn(r8, r6)));
+                    const float my = __fmaf_rn(2.0f, __fsub_rn(r1, r7), __fadd_rn(__fsub_rn(r0, r6), __fsub_rn(r2, r8)));
+                    const float sref = horn_slope(mx, my, p.k_fd);
+                    have = r4 == r4 && sref == sref;
+                    if (have) {
+                        const float d = s - sref;
+                        g = 2.0f * d;
+                        if (a >= 1 && b >= 1 && a <= kGH && b <= kGW) lsum += d * d;
+                    }
+                } else {
+                    g = load_f32(p.gslope, r, c);
+                }
+                if (have && q > 0.0f) {  // subgradient 0 at zero slope
+                    const float f = g * p.k_fd * rsqrtf(q);
+                    A = f * nx;
+                    B = f * ny;
+                }
+            }
+            sa[a][b] = A;
+            sb[a][b] = B;
+            z0 = z3, z1 = z4, z2 = z5, z3 = z6, z4 = z7, z5 = z8;
+            r0 = r3, r1 = r4, r2 = r5, r3 = r6, r4 = r7, r5 = r8;
+        }
     }
     __syncthreads();
-    for (int i = tid; i < kBH * kBW; i += kThreads) {
-        const int a = i / kBW, b = i % kBW;
-        const int64_t r = y0 + a, c = x0 + b;
-        if (r >= p.rows || c >= p.cols) continue;
-        const float* A0 = &sa[a][b];
-        const float* B0 = &sb[a][b];
-        constexpr int L = kAW + 1;
-        const float ga = (-A0[2 * L + 2] + A0[2 * L]) + 2.0f * (-A0[L + 2] + A0[L]) + (-A0[2] + A0[0]);
-        const float gb = (B0[2 * L + 2] + 2.0f * B0[2 * L + 1] + B0[2 * L]) - (B0[2] + 2.0f * B0[1] + B0[0]);
-        reinterpret_cast<float*>(reinterpret_cast<char*>(p.gz) + r * p.gz_pitch)[c] = ga + gb;
+    // dL/dz of the 32 x 60 block: thread column b = tid % 60, rows 8k .. 8k + 7
+    if (tid < kGW * 4) {
+        const int b = tid % kGW, a0 = (tid / kGW) * kSegO;
+        const int64_t c = x0 + b;
+        // A's middle column has no weight in d nx / d z
+        float A0 = sa[a0][b], A2 = sa[a0][b + 2], A3 = sa[a0 + 1][b], A5 = sa[a0 + 1][b + 2];
+        float B0 = sb[a0][b], B1 = sb[a0][b + 1], B2 = sb[a0][b + 2];
+        float B3 = sb[a0 + 1][b], B4 = sb[a0 + 1][b + 1], B5 = sb[a0 + 1][b + 2];
+        for (int a = a0; a < a0 + kSegO; a++) {
+            const float A6 = sa[a + 2][b], A8 = sa[a + 2][b + 2];
+            const float B6 = sb[a + 2][b], B7 = sb[a + 2][b + 1], B8 = sb[a + 2][b + 2];
+            const int64_t r = y0 + a;
+            // the form above's sums, in its order
+            const float ga = (-A8 + A6) + 2.0f * (-A5 + A3) + (-A2 + A0);
+            const float gb = (B8 + 2.0f * B7 + B6) - (B2 + 2.0f * B1 + B0);
+            if (r < p.rows && c < p.cols)
+                reinterpret_cast<float*>(reinterpret_cast<char*>(p.gz) + r * p.gz_pitch)[c] = ga + gb;
+            A0 = A3, A2 = A5, A3 = A6, A5 = A8;
+            B0 = B3, B1 = B4, B2 = B5, B3 = B6, B4 = B7, B5 = B8;
+        }
     }
     if (mode == 0 && p.loss) {
         float v = lsum;
@@ -294,9 +334,9 @@ int grad_box_cols() { return kTBW; }
 
 cudaError_t launch_slope_loss_grad_tma(const CUtensorMap* mz, const CUtensorMap* mr, const GradParams& p, int mode,
                                        cudaStream_t st) {
-    const int64_t nby = (p.rows + kBH - 1) / kBH, nbx = (p.cols + kBW - 1) / kBW;
+    const int64_t nby = (p.rows + kGH - 1) / kGH, nbx = (p.cols + kGW - 1) / kGW;
     if (nby * nbx == 0) return cudaSuccess;
-    const size_t smem = 2 * (size_t)kBoxBytes;
+    const size_t smem = (size_t)kBoxStride + kBoxBytes;
     cudaError_t e = cudaFuncSetAttribute(slope_grad_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     slope_grad_tma_kernel<<<(unsigned)(nby * nbx), kThreads, smem, st>>>(*mz, mode == 0 ? *mr : *mz, p, mode, nbx);
