@@ -70,6 +70,21 @@ def test_sca_bit_exact_given_oracle_weights(ctx, oracle_lib):
         assert np.array_equal(g.view(np.int64), ref.view(np.int64)), (shape, np.abs(g - ref).max())
 
 
+@pytest.mark.parametrize("shape", [(1100, 70), (45, 1500), (33, 34), (34, 33)])
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_sca_bands_tall_wide_and_edge_sizes(shape, dt, ctx, oracle_lib):
+    """Many 32-row bands over short rows, one band over long rows, and sizes
+    around one band (33 and 34 rows: a second band of one work row or none),
+    with float32 and float64 weights: bit for bit against the oracle."""
+    dem = _dem(oracle_lib, shape, 77 + shape[0] % 13)
+    w = oracle_lib.mfd(dem, ND, 30.0, 1.1).astype(dt)
+    ref = oracle_lib.sca_mfd(w.astype(np.float64), ND)
+    out = empty_dev(shape, np.float64)
+    ctx.sca_mfd([abi.raster(dev(np.ascontiguousarray(w[q])), ND) for q in range(8)], abi.raster(out, ND))
+    g = host(out)
+    assert np.array_equal(g.view(np.int64), ref.view(np.int64)), (shape, np.abs(g - ref).max())
+
+
 def test_sca_host_buffers_float32_weights(ctx, oracle_lib):
     dem = _dem(oracle_lib, (140, 170), 76)
     w = oracle_lib.mfd(dem, ND, 30.0, 1.1).astype(np.float32)
