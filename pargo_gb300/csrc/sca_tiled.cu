@@ -15,12 +15,11 @@
 // Phases (one launch each):
 //  1. per 64 x 64 tile (codes with a 2-cell halo in shared memory): the in-tile
 //     forest (from byte inflow masks), stored as one word per cell for phase
-//     4; its subtree sums by a shared-memory topological walk (one atomic add
-//     per step on the parent's word of pending children, bad-child count and
-//     sum; the last contributor continues); and for every border cell the
-//     exit its in-tile path reaches, by pointer jumping.  Exits (cells whose
-//     parent lies in another tile) record their in-tile sum and the entry
-//     cell they feed.
+//     4; every cell's path end by pointer jumping; the in-tile subtree of an
+//     exit (a cell whose parent lies in another tile) is the set of cells
+//     whose path ends at it, so its sum and bad flag are counts and ORs over
+//     them, with no walk.  Exits record their in-tile sum and the entry cell
+//     they feed; every border cell records the exit its path reaches.
 //  2. the exit forest: exit x's parent is the exit reached from the entry x
 //     feeds; its feeding counts, added into the parents' packed words.
 //  3. subtree sums over the exit forest (its leaves marked first, then a
@@ -28,9 +27,11 @@
 //     tiles a river crosses); each exit adds its total to the inflow of the
 //     entry it feeds.
 //  4. per tile again, from the stored forest: the in-tile sums with the
-//     entries' inflows added; converged contract: the output itself, then a
-//     one-thread kernel for the reference's last-cell quirk (a nodata last
-//     work cell accumulates what flows into it).
+//     entries' inflows added, by a shared-memory topological walk (one atomic
+//     add per step on the parent's word of pending children, bad-child count
+//     and sum; the last contributor continues); converged contract: the
+//     output itself, then a one-thread kernel for the reference's last-cell
+//     quirk (a nodata last work cell accumulates what flows into it).
 //  5. shipped contract only: the output pass over the final counts and flags.
 // Cycles (inside a tile or across tiles) and inflows from the raster's ring,
 // which the reference never releases, leave cells or exits uncompleted; the
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                 }
                 S.lpar[i] = lp;
                 reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));  // leaves fixed before any walk
-                S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;  // the in-tile children to come
+                S.acc[i] = 0;  // counted below, once the paths' last cells are known
                 if (lr < th && lc < tw) s.forest[(r0 + lr) * p.cols + (c0 + lc)] = pack_forest(f, deg, lp);
             }
             atomicAdd(&S.cnt[0], nvalid);
@@ -356,52 +357,55 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             }
             __syncthreads();
         }
-        // Topological walk from the in-tile leaves: a walker holds the value
-        // of its cell's word once every child has folded in (a leaf's word is
-        // final from the start; anything else's is the last child's return
-        // value plus its own add), so a step is one atomic on the parent.
-        // Walkers take leaves from one shared cursor (a warp's lanes that
-        // need one take consecutive cells with a single atomic), so a lane
-        // that ends a chain starts the next leaf while long chains go on.
+        // Final pass: the topological walk from the in-tile leaves.
         using Acc = typename Smem::Acc;
         unsigned long long ndone = 0;
-        {
-            const int lane = tid & 31;
-            int cur = -1;
-            Acc v = 0;
-            for (;;) {
-                const unsigned need = __ballot_sync(0xffffffffu, cur == -1);
-                if (need) {
-                    int base = 0;
-                    if (lane == __ffs(need) - 1) base = atomicAdd(&S.next, __popc(need));
-                    base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
-                    if (cur == -1) {
-                        const int i = base + __popc(need & ((1u << lane) - 1));
-                        if (i < kCells && (S.flag(i) & 8)) {
-                            cur = i;
-                            v = S.acc[i];
-                        } else if (i >= kCells) {
-                            cur = -2;  // no leaves left for this lane
+        if constexpr (FINAL) {
+            // Topological walk from the in-tile leaves: a walker holds the value
+            // of its cell's word once every child has folded in (a leaf's word is
+            // final from the start; anything else's is the last child's return
+            // value plus its own add), so a step is one atomic on the parent.
+            // Walkers take leaves from one shared cursor (a warp's lanes that
+            // need one take consecutive cells with a single atomic), so a lane
+            // that ends a chain starts the next leaf while long chains go on.
+            {
+                const int lane = tid & 31;
+                int cur = -1;
+                Acc v = 0;
+                for (;;) {
+                    const unsigned need = __ballot_sync(0xffffffffu, cur == -1);
+                    if (need) {
+                        int base = 0;
+                        if (lane == __ffs(need) - 1) base = atomicAdd(&S.next, __popc(need));
+                        base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
+                        if (cur == -1) {
+                            const int i = base + __popc(need & ((1u << lane) - 1));
+                            if (i < kCells && (S.flag(i) & 8)) {
+                                cur = i;
+                                v = S.acc[i];
+                            } else if (i >= kCells) {
+                                cur = -2;  // no leaves left for this lane
+                            }
                         }
                     }
-                }
-                if (!__any_sync(0xffffffffu, cur >= 0) && !__any_sync(0xffffffffu, cur == -1)) break;
-                if (cur >= 0) {
-                    const Acc tot = 1 + (v & Smem::kSum);
-                    const bool bad = (S.flag(cur) & 18u) != 0 || ((v >> Smem::kBadShift) & 0xFu) != 0;
-                    S.acc[cur] = Smem::kDone | (bad ? Smem::kBadOne : (Acc)0) | tot;  // nothing else writes it now
-                    ndone++;
-                    const int par = S.lpar[cur];
-                    if (par < 0) {
-                        cur = -1;
-                    } else {
-                        const Acc delta = tot + (bad ? Smem::kBadOne : (Acc)0) - Smem::kOne;  // the count field is >= 1
-                        const Acc old = atomicAdd(&S.acc[par], delta);
-                        if (((old >> Smem::kDegShift) & 0xFu) != 1u) {
-                            cur = -1;  // another child is still to come
+                    if (!__any_sync(0xffffffffu, cur >= 0) && !__any_sync(0xffffffffu, cur == -1)) break;
+                    if (cur >= 0) {
+                        const Acc tot = 1 + (v & Smem::kSum);
+                        const bool bad = (S.flag(cur) & 18u) != 0 || ((v >> Smem::kBadShift) & 0xFu) != 0;
+                        S.acc[cur] = Smem::kDone | (bad ? Smem::kBadOne : (Acc)0) | tot;  // nothing else writes it now
+                        ndone++;
+                        const int par = S.lpar[cur];
+                        if (par < 0) {
+                            cur = -1;
                         } else {
-                            v = old + delta;
-                            cur = par;
+                            const Acc delta = tot + (bad ? Smem::kBadOne : (Acc)0) - Smem::kOne;  // the count field is >= 1
+                            const Acc old = atomicAdd(&S.acc[par], delta);
+                            if (((old >> Smem::kDegShift) & 0xFu) != 1u) {
+                                cur = -1;  // another child is still to come
+                            } else {
+                                v = old + delta;
+                                cur = par;
+                            }
                         }
                     }
                 }
@@ -430,6 +434,29 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                 }
                 if (!__syncthreads_or(moved)) break;  // every pointer is at its path's last cell
             }
+            // The in-tile subtree of an exit is the set of cells whose path
+            // ends at it: its size is their count and its bad flag the OR of
+            // their own, taken with one atomic per group of a warp's lanes
+            // that share the exit.  A cell whose path ends (its last cell has
+            // no parent here) is done; a path still inside the tile after the
+            // jumps runs into a cycle.
+            for (int i = tid; i < kCells; i += kThreads) {
+                const int q = S.lpar[i];
+                const int last = q >= 0 ? q : i;
+                const int lp = S.lpar[last];
+                const unsigned f = S.flag(i);
+                const bool valid = (f & 1u) != 0, ends = valid && lp < 0;
+                if (ends) atomicOr(&S.acc[i], Smem::kDone);
+                const bool to_exit = ends && lp == -2;
+                const unsigned grp = __match_any_sync(0xffffffffu, to_exit ? last : -1);
+                const unsigned lead = __ffs(grp) - 1;
+                const bool bad_any = (__ballot_sync(0xffffffffu, to_exit && (f & 2u)) & grp) != 0;
+                if (to_exit && (tid & 31) == (int)lead) {
+                    atomicAdd(&S.acc[last], (Acc)__popc(grp));
+                    if (bad_any) atomicOr(&S.acc[last], Smem::kBadOne);
+                }
+            }
+            __syncthreads();
             // Border cells: the exit each in-tile path reaches; exits record
             // their in-tile totals and the entry they feed.
             for (int i = tid; i < kCells; i += kThreads) {
