@@ -150,15 +150,24 @@ struct TileSmem {
     static constexpr Acc kDone = (Acc)0xF << kDegShift;
     // first pass only: the codes, (a, b) = (r - r0 + 2, c - c0 + 2), and the
     // inflow masks of the tile and a 1-cell ring, (a, b) = (r - r0 + 1, c - c0 + 1)
+    // in-tile parent, -1 none, -2 outside the tile; in the final pass packed
+    // with the flags the walk reads: parent + 2 (bits 0-12), valid (13), bad
+    // or fed by a not-pulled inflow (14), in-tile leaf (15)
+    alignas(16) int16_t lpar[kCells];
+    Acc acc[kCells];
+    uint32_t flagw[FINAL ? 1 : kCells / 4];  // first pass: a byte of static flags per cell
     int8_t cd[FINAL ? 1 : kH * kH];
     uint8_t im[FINAL ? 1 : kM * kM];
-    int16_t lpar[kCells];        // in-tile parent, -1 none, -2 outside the tile
-    Acc acc[kCells];
-    uint32_t flagw[kCells / 4];  // a byte of static flags per cell
     unsigned long long cnt[3];   // valid, completed, ring inflows
     int next;                    // the walk's next cell to look at for a leaf
     int16_t slotcell[FINAL ? kScaSlots : 1];  // final pass: the valid cell at each border slot, -1 none
     __device__ __forceinline__ unsigned flag(int i) const { return (flagw[i >> 2] >> (8 * (i & 3))) & 0xFFu; }
+    // the final pass's packed parent and flags
+    __device__ __forceinline__ unsigned packed(int i) const { return (unsigned)(uint16_t)lpar[i]; }
+    __device__ __forceinline__ int parent(int i) const { return (int)(packed(i) & 0x1FFFu) - 2; }
+    __device__ __forceinline__ bool p_valid(int i) const { return (packed(i) >> 13) & 1u; }
+    __device__ __forceinline__ bool p_bad(int i) const { return (packed(i) >> 14) & 1u; }
+    __device__ __forceinline__ bool p_leaf(int i) const { return (packed(i) >> 15) & 1u; }
     __device__ __forceinline__ bool done(int i) const { return (acc[i] & kDone) == kDone; }
     __device__ __forceinline__ Acc total(int i) const { return acc[i] & kSum; }
     __device__ __forceinline__ unsigned sub_bad(int i) const { return (unsigned)((acc[i] >> kBadShift) & 1u); }
@@ -335,8 +344,9 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             for (int q = 0; q < kPer; q++) {
                 const int i = tid + q * kThreads;
                 const unsigned f = fw[q] & 3u, deg = (fw[q] >> 4) & 0xFu;
-                S.lpar[i] = (int16_t)((int)(fw[q] >> 8) - 2);
-                reinterpret_cast<uint8_t*>(S.flagw)[i] = (uint8_t)(f | (f && deg == 0 ? 8 : 0));
+                // parent + 2 straight from the word (bits 8-20), then valid, bad and leaf
+                S.lpar[i] = (int16_t)(uint16_t)(((fw[q] >> 8) & 0x1FFFu) | ((f & 1u) << 13) | (((f >> 1) & 1u) << 14) |
+                                                ((f && deg == 0 ? 1u : 0u) << 15));
                 S.acc[i] = (typename Smem::Acc)deg * Smem::kOne;
                 if (f & 1u) {
                     nvalid++;
@@ -353,7 +363,8 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
             const int i = tid < kScaSlots ? S.slotcell[tid] : -1;
             if (i >= 0) {
                 S.acc[i] += (typename Smem::Acc)xin;
-                if (xinb & 1u) atomicOr(&S.flagw[i >> 2], 16u << (8 * (i & 3)));
+                if (xinb & 1u)  // the bad bit of its packed parent word (lpar is 4-byte aligned)
+                    atomicOr(reinterpret_cast<unsigned*>(S.lpar) + (i >> 1), (1u << 14) << (16 * (i & 1)));
             }
             __syncthreads();
         }
@@ -380,7 +391,7 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                         base = __shfl_sync(0xffffffffu, base, __ffs(need) - 1);
                         if (cur == -1) {
                             const int i = base + __popc(need & ((1u << lane) - 1));
-                            if (i < kCells && (S.flag(i) & 8)) {
+                            if (i < kCells && S.p_leaf(i)) {
                                 cur = i;
                                 v = S.acc[i];
                             } else if (i >= kCells) {
@@ -391,10 +402,10 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                     if (!__any_sync(0xffffffffu, cur >= 0) && !__any_sync(0xffffffffu, cur == -1)) break;
                     if (cur >= 0) {
                         const Acc tot = 1 + (v & Smem::kSum);
-                        const bool bad = (S.flag(cur) & 18u) != 0 || ((v >> Smem::kBadShift) & 0xFu) != 0;
+                        const bool bad = S.p_bad(cur) || ((v >> Smem::kBadShift) & 0xFu) != 0;
                         S.acc[cur] = Smem::kDone | (bad ? Smem::kBadOne : (Acc)0) | tot;  // nothing else writes it now
                         ndone++;
-                        const int par = S.lpar[cur];
+                        const int par = S.parent(cur);
                         if (par < 0) {
                             cur = -1;
                         } else {
@@ -498,7 +509,7 @@ __global__ void __launch_bounds__(kThreads, FINAL ? 5 : 6) sca_tile_kernel(const
                 if (lr >= th || lc >= tw) continue;
                 const int64_t r = r0 + lr, c = c0 + lc;
                 const int64_t g = r * p.cols + c;
-                const bool valid = (S.flag(i) & 1u) != 0;
+                const bool valid = S.p_valid(i);
                 const bool ok = valid && S.done(i);
                 const unsigned long long tot = ok ? (unsigned long long)S.total(i) : 0ULL;
                 if (p.shipped) {
