@@ -1601,9 +1601,7 @@ pargo_status pargo_sca_mfd(pargo_ctx* ctx, const pargo_raster* weights, pargo_ra
     if (!p.cnt || !p.flags || !p.sca || !lists) return cuda_fail(ctx, e, "sca_mfd scratch");
     p.list_a = lists;
     p.list_b = lists + n;
-    p.list_c = lists + 2 * n;
     p.counts = lists + 3 * n;
-    p.barrier = (unsigned int*)(lists + 3 * n + 4);
     p.totals = (unsigned long long*)(((uintptr_t)(lists + 3 * n + 8) + 7) & ~(uintptr_t)7);
     p.error_flag = ctx->d_error;
     bool f32 = true;

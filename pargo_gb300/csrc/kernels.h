@@ -245,15 +245,13 @@ struct ScaMfdParams {
     long long nd_lo, nd_hi;        // weight layer 0 nodata band (|w - nd| < 1e-6) as keys
     double nodata;                 // written on nodata cells and the ring
     OutView out;
-    int32_t* cnt;                  // inflows from valid work cells not yet processed
-    uint8_t* flags;                // valid, source, never done, done
+    int32_t* cnt;                  // round form: earlier non-source inflows not yet processed
+    uint8_t* flags;                // valid, source, never done, done; bits 4-7 the round form's release mask
     double* sca;
     int32_t* list_a;
     int32_t* list_b;
-    int32_t* list_c;               // spare list
-    int32_t* counts;               // [0] length of list_a, [1] of list_b, [2] finished blocks / list_b claims, [3] list_a claims
+    int32_t* counts;               // round form: [0] length of list_a, [1] of list_b, [2] finished blocks
     unsigned long long* totals;    // [0] valid cells, [1] processed cells, [2] nodata cells with weights
-    unsigned int* barrier;         // unused
     int* error_flag;               // a bounded wait of the band form gave up
 };
 cudaError_t launch_sca_mfd_init(const ScaMfdParams& p, int num_sms, cudaStream_t st);
