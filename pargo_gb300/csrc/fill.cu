@@ -144,14 +144,38 @@ __global__ void __launch_bounds__(256) fill_init_tile_kernel(const FillParams p,
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t y0 = (t / p.tiles_x) * kT - 1, x0 = (t % p.tiles_x) * kT - 1;  // window origin
         if (tid == 0) any_outlet = 0;
-        for (int i = tid; i < kH * kH; i += 256) {
+        // the window's DEM values, every load of a thread issued before the
+        // first is converted (one memory round trip per tile)
+        constexpr int kPer = (kH * kH + 255) / 256;  // 5
+        int64_t raw[kPer];
+        bool in[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int i = tid + q * 256;
             const int64_t r = y0 + i / kH, c = x0 + i % kH;
-            const bool inner = r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
+            in[q] = i < kH * kH && r > 0 && c > 0 && r < p.rows - 1 && c < p.cols - 1;
+            raw[q] = 0;
+            if (in[q]) {
+                const char* row = reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch;
+                raw[q] = p.dem_f64 ? reinterpret_cast<const long long*>(row)[c]
+                                   : (long long)reinterpret_cast<const unsigned*>(row)[c];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+            const int i = tid + q * 256;
+            if (i >= kH * kH) continue;
             bool nd = true;
             int64_t k = kKeyInf;
-            if (inner) {
-                nd = dem_is_nodata(p, r, c);
-                k = dem_key(p, r, c);
+            if (in[q]) {
+                if (p.dem_f64) {
+                    k = dkey(__longlong_as_double(raw[q]));
+                    nd = k >= dkey(p.nd6d.lo) && k <= dkey(p.nd6d.hi);  // an empty band has lo > hi: its keys too
+                } else {
+                    const float f = __uint_as_float((unsigned)raw[q]);
+                    k = fkey64(f);
+                    nd = p.nd6f.has(f);
+                }
             }
             zk[i] = k;
             ndf[i] = nd ? 1 : 0;
