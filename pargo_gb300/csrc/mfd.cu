@@ -322,8 +322,10 @@ __global__ void __launch_bounds__(kThreads) sca_mfd_round_kernel(const ScaMfdPar
 // 1 + s - 2L), so the three upper neighbours of its cell are the results of
 // lane L - 1's last three steps (shuffles) and the left one is its own last
 // result.  Lane 0's upper row is the previous band's last row, read from
-// global memory in chunks of 32 columns once that band has published them
-// (bands are taken in order, so the band waited on is running or done).
+// global memory in chunks of 8 columns once that band has published them
+// (bands are taken in order, so the band waited on is running or done; the
+// wait sleeps 20 ns at a time, gives up after kBandPatience cycles without
+// progress and sets the error flag).
 // A cell's static data -- the 8 inflow weights and the valid / source /
 // positive masks of its neighbours -- is gathered first into one record per
 // cell (sca_mfd_records_kernel) and streamed by each lane a few steps ahead
