@@ -418,6 +418,7 @@ __global__ void __launch_bounds__(kBandWarps * 32) sca_mfd_band_kernel(const Sca
                     __threadfence();
                 }
                 failed = __shfl_sync(0xffffffffu, failed, 0);
+                __syncwarp();  // orders lane 0's observation before the other lanes' loads
             }
             const int64_t c = kBandChunk * j + lane;
             double v = 0.0;
