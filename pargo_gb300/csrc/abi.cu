@@ -517,7 +517,8 @@ struct JsonReader {
             do {
                 if (!str(nullptr) || !eat(':') || !skip()) return ok = false;
             } while (eat(','));
-            return eat('}') || (ok = false);
+            if (eat('}')) return true;
+            return ok = false;
         }
         if (c == '[') {
             i++;
@@ -525,7 +526,8 @@ struct JsonReader {
             do {
                 if (!skip()) return ok = false;
             } while (eat(','));
-            return eat(']') || (ok = false);
+            if (eat(']')) return true;
+            return ok = false;
         }
         if (t.compare(i, 4, "true") == 0 || t.compare(i, 4, "null") == 0) {
             i += 4;
@@ -554,7 +556,8 @@ struct JsonReader {
             else ok = skip();
             if (!ok) return false;
         } while (eat(','));
-        return eat('}') || (ok = false);
+        if (eat('}')) return true;
+        return ok = false;
     }
 };
 

@@ -86,18 +86,12 @@ __device__ __forceinline__ int64_t add_gap(int64_t k, double gap) {
 }
 
 // The DEM value at (r, c) as an order-preserving key of its double value,
-// and its nodata test (Eps 1e-6) -- both from the bits: a float DEM widened
-// to double and compared in double would cost conversions and compares on
-// the FP64 pipe (a narrow pipe on this part) for every cell a visit loads.
+// from the bits: a float DEM widened to double and compared in double would
+// cost conversions and compares on the FP64 pipe (a narrow pipe on this part)
+// for every cell a visit loads.
 __device__ __forceinline__ int64_t dem_key(const FillParams& p, int64_t r, int64_t c) {
     const char* row = reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch;
     return p.dem_f64 ? dkey(reinterpret_cast<const double*>(row)[c]) : fkey64(reinterpret_cast<const float*>(row)[c]);
-}
-__device__ __forceinline__ bool dem_is_nodata(const FillParams& p, int64_t r, int64_t c) {
-    const char* row = reinterpret_cast<const char*>(p.dem) + r * p.dem_pitch;
-    if (!p.dem_f64) return p.nd6f.has(reinterpret_cast<const float*>(row)[c]);
-    const int64_t k = dkey(reinterpret_cast<const double*>(row)[c]);
-    return k >= dkey(p.nd6d.lo) && k <= dkey(p.nd6d.hi);  // an empty band has lo > hi: its keys too
 }
 
 // A level into a filled-DEM output, nodata levels (+inf) as the output's
@@ -137,13 +131,11 @@ __global__ void fill_init_tiles_kernel(const FillParams p, FillScratch s) {
 __global__ void __launch_bounds__(256) fill_init_tile_kernel(const FillParams p, FillScratch s) {
     __shared__ int64_t zk[kH * kH];
     __shared__ uint8_t ndf[kH * kH];  // 1: a nodata level (nodata DEM value, the ring, beyond the raster)
-    __shared__ int any_outlet;
     const int tid = threadIdx.x;
     const int64_t ntiles = p.tiles_y * p.tiles_x;
     const int64_t kinit = dkey(p.init_level);
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int64_t y0 = (t / p.tiles_x) * kT - 1, x0 = (t % p.tiles_x) * kT - 1;  // window origin
-        if (tid == 0) any_outlet = 0;
         // the window's DEM values, every load of a thread issued before the
         // first is converted (one memory round trip per tile)
         constexpr int kPer = (kH * kH + 255) / 256;  // 5
