@@ -896,7 +896,7 @@ def run_load(args, ws, rank, local, side=32768, grain=16):
         "config": {"workload": "load%d: intensity compute layer (grain %d) of the %dx%d float32 hydro DEM (seed 1), "
                                "%d-part row decomposition" % (side, grain, side, side, nparts),
                    "l2": "inputs larger than L2"},
-        "roofline": {"bound": "hbm", "kernel": "compute_load_kernel", "achieved": round(achieved, 1), "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "compute_load_count_kernel<16> (integer loads: a warp counts 32 data columns of a compute row)", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": kind, "traffic": None,
                      "algorithmic_bytes_per_cell": 4, "kernel_ms": round(ms_k, 3)},
         "cpu_baseline": cpu,

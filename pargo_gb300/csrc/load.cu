@@ -62,6 +62,68 @@ __global__ void __launch_bounds__(256) compute_load_kernel(const LoadParams p) {
     }
 }
 
+// Nodata count of data column c over rows r0 .. r0 + nrows - 1 of layer l:
+// every row's load issued before the first test.
+template <int G>
+__device__ __forceinline__ int column_nodata(const LoadParams& p, int l, int64_t r0, int nrows, int64_t c) {
+    const InView& v = p.data[l];
+    const char* base = v.base + r0 * v.pitch;
+    int nd = 0;
+    if (v.dtype == PARGO_F64) {
+        double x[G];
+#pragma unroll
+        for (int q = 0; q < G; q++) x[q] = q < nrows ? reinterpret_cast<const double*>(base + q * v.pitch)[c] : 0.0;
+#pragma unroll
+        for (int q = 0; q < G; q++) {
+            const long long k = dkey64(x[q]);
+            nd += (q < nrows && k >= p.nd_lo[l] && k <= p.nd_hi[l]) ? 1 : 0;
+        }
+    } else {
+        float x[G];
+#pragma unroll
+        for (int q = 0; q < G; q++) x[q] = q < nrows ? reinterpret_cast<const float*>(base + q * v.pitch)[c] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < G; q++) nd += (q < nrows && p.ndf[l].has(x[q])) ? 1 : 0;
+    }
+    return nd;
+}
+
+// Integer loads with a grain G that divides 32: the counts do not depend on
+// the order of the cells, so a warp reads 32 consecutive data columns of one
+// compute row (one column per lane, G rows, coalesced) and adds each compute
+// cell's counts over its G lanes.  The 32-column chunks start at data column
+// 1 + 32 j, a compute cell's first column, so no cell straddles two chunks.
+template <int G>
+__global__ void __launch_bounds__(256) compute_load_count_kernel(const LoadParams p) {
+    const int lane = threadIdx.x & 31;
+    const int64_t chunks = (p.ccols * G + 31) / 32;  // per compute row
+    const int64_t tasks = p.crows * chunks;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < tasks; w += nwarps) {
+        const int64_t cr = w / chunks, j = w % chunks;
+        const int64_t cc = (32 * j + lane) / G;  // this lane's compute column
+        const int64_t c = 1 + 32 * j + lane;     // and data column
+        const bool work = cc < p.ccols &&
+                          (!p.compute_ring || (cr >= 1 && cc >= 1 && cr <= p.crows - 2 && cc <= p.ccols - 2));
+        const int64_t r0 = cr * G + 1;
+        const int nrows = (int)(min(r0 + G, p.rows) - r0);
+        int nd = 0;
+        if (work && c < p.cols)
+            for (int l = 0; l < p.count; l++) nd += column_nodata<G>(p, l, r0, nrows, c);
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+        if (lane % G == 0 && cc < p.ccols) {
+            double acc = 0.0;
+            if (work) {
+                const int64_t c_end = min((cc + 1) * G + 1, p.cols);
+                const long long total = (long long)p.count * nrows * (c_end - (cc * G + 1));
+                acc = __dadd_rn(__dmul_rn((double)(total - nd), p.valid_load), __dmul_rn((double)nd, p.nodata_load));
+            }
+            put_value(p.load, cr, cc, acc);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(128) row_load_kernel(const InView load, int64_t crows, int64_t ccols, double nodata,
                                                        double* row_load) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < crows; r += (int64_t)gridDim.x * blockDim.x) {
@@ -78,9 +140,29 @@ __global__ void __launch_bounds__(128) row_load_kernel(const InView load, int64_
 
 }  // namespace
 
+template <int G>
+static cudaError_t launch_count(const LoadParams& p, int num_sms, cudaStream_t s) {
+    const int64_t tasks = p.crows * ((p.ccols * G + 31) / 32);  // one warp each
+    int64_t blocks = (tasks + 7) / 8;
+    if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
+    compute_load_count_kernel<G><<<(unsigned)blocks, 256, 0, s>>>(p);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_compute_load(const LoadParams& p, int num_sms, cudaStream_t s) {
     const int64_t n = p.crows * p.ccols;
     if (n == 0) return cudaSuccess;
+    if (p.integral) {
+        switch (p.grain) {
+            case 1: return launch_count<1>(p, num_sms, s);
+            case 2: return launch_count<2>(p, num_sms, s);
+            case 4: return launch_count<4>(p, num_sms, s);
+            case 8: return launch_count<8>(p, num_sms, s);
+            case 16: return launch_count<16>(p, num_sms, s);
+            case 32: return launch_count<32>(p, num_sms, s);
+            default: break;  // other grains: one thread per compute cell
+        }
+    }
     int64_t blocks = (n + 255) / 256;
     if (blocks > (int64_t)num_sms * 16) blocks = (int64_t)num_sms * 16;
     compute_load_kernel<<<(unsigned)blocks, 256, 0, s>>>(p);

@@ -36,6 +36,23 @@ def test_compute_layer_bit_exact(shape, grain, ring, loads, ctx, oracle_lib):
     assert bits_equal(host(out), ref)
 
 
+@pytest.mark.parametrize("shape,grain,ring,loads,nl,dt", [((1030, 1234), 16, False, (0.0, 1.0), 1, np.float32),
+                                                          ((517, 700), 8, True, (2.0, 5.0), 2, np.float32),
+                                                          ((300, 333), 32, True, (1.0, 4.0), 1, np.float32),
+                                                          ((203, 157), 2, True, (0.0, 1.0), 1, np.float64),
+                                                          ((35, 35), 32, False, (0.0, 1.0), 1, np.float32),
+                                                          ((150, 190), 16, False, (3.0, 0.0), 2, np.float64)])
+def test_integer_loads_counted_by_columns(shape, grain, ring, loads, nl, dt, ctx, oracle_lib):
+    """Integer loads with a grain dividing 32 take the column-counting kernel
+    (warps over 32 consecutive data columns): ragged last compute rows and
+    columns, the compute ring, several layers, float32 and float64 data."""
+    layers = [_dem(shape, 11 * k + grain).astype(dt) for k in range(nl)]
+    ref = oracle_lib.compute_load(np.stack(layers) if nl > 1 else layers[0], ND, grain, loads[0], loads[1], ring)
+    out = empty_dev(ref.shape, np.float64)
+    ctx.compute_load([abi.raster(dev(x), ND) for x in layers], abi.raster(out, ND), grain, loads[0], loads[1], ring)
+    assert bits_equal(host(out), ref)
+
+
 def test_float64_data_several_layers_host_buffers(ctx, oracle_lib):
     a = _dem((150, 190), 5).astype(np.float64)
     b = _dem((150, 190), 6).astype(np.float64)
