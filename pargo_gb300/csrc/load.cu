@@ -9,8 +9,13 @@
 // nodata_load for the others,
 // skipping data cells past the raster's last row or column.  The sums are
 // sequential FP64 additions in that order, so the layer equals the
-// reference's bit for bit.  One thread per compute cell: a warp's 32 threads
-// read 32 adjacent blocks, i.e. 32 * grain consecutive values of a data row.
+// reference's bit for bit.  Two kernels:
+//  * integer loads whose sums stay below 2^53 and a grain dividing 32
+//    (compute_load_count_kernel): every partial sum is exact, so the cells
+//    are counted in any order -- a warp reads 32 consecutive data columns of
+//    one compute row, coalesced, and the counts are scaled by the loads;
+//  * any other case (compute_load_kernel): one thread per compute cell
+//    adding the loads in the reference's order.
 //
 // Row loads (DeComposition::valRowDcmp, gpro/deComposition.h:320-335): per
 // compute row, the left-to-right FP64 sum of the cells that are above -9999
