@@ -14,8 +14,9 @@
 //    (compute_load_count_kernel): every partial sum is exact, so the cells
 //    are counted in any order -- a warp reads 32 consecutive data columns of
 //    one compute row, coalesced, and the counts are scaled by the loads;
-//  * any other case (compute_load_kernel): one thread per compute cell
-//    adding the loads in the reference's order.
+//  * any other grain or load (compute_load_kernel): one thread per compute
+//    cell, counting (integer loads) or adding the loads in the reference's
+//    order.
 //
 // Row loads (DeComposition::valRowDcmp, gpro/deComposition.h:320-335): per
 // compute row, the left-to-right FP64 sum of the cells that are above -9999
