@@ -18,6 +18,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -200,8 +201,11 @@ inline void make_parent_dirs(const std::string& path) {
 inline bool write_tune_cache(const std::string& path, const std::vector<TuneEntry>& v) {
     if (path.empty()) return false;
     make_parent_dirs(path);
+    // a temporary name of this process and call: writers in other threads
+    // or processes never share one (the last rename wins)
+    static std::atomic<unsigned> seq{0};
     char suffix[64];
-    snprintf(suffix, sizeof(suffix), ".tmp%ld", (long)getpid());
+    snprintf(suffix, sizeof(suffix), ".tmp%ld.%u", (long)getpid(), seq.fetch_add(1));
     const std::string tmp = path + suffix;
     FILE* f = fopen(tmp.c_str(), "wb");
     if (!f) return false;

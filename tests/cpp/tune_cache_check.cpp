@@ -1,6 +1,7 @@
 // Host-only checks of the autotuner's cache file (pargo_gb300/csrc/tune_cache.h):
 // write/read round trips, malformed and foreign content, the path rules and
-// the write through a temporary file.  Usage: tune_cache_check <scratch dir>.
+// the write through a temporary file, also from two threads at once.
+// Usage: tune_cache_check <scratch dir>.
 // Prints one line per failed check and exits non-zero if any failed.
 #include "tune_cache.h"
 
@@ -9,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 using pargo::TuneEntry;
@@ -121,6 +123,27 @@ int main(int argc, char** argv) {
     put(p2, "{\"pad\": " + std::string(40, '[') + std::string(40, ']') +
                 ", \"entries\": [{\"op\": \"a\", \"size_class\": 1, \"variant\": \"v\"}]}");
     CHECK(pargo::read_tune_cache(p2).size() == 1);
+
+    // writers in two threads: every read sees one writer's whole file, and no
+    // temporary file is left behind
+    {
+        const std::string p3 = dir + "/c/tune.json";
+        const std::vector<TuneEntry> va(3, entry("a", "d", 1, "v", 1.0)), vb(5, entry("b", "d", 2, "w", 2.0));
+        bool ok_a = true, ok_b = true;
+        std::thread ta([&] { for (int k = 0; k < 200; k++) ok_a = pargo::write_tune_cache(p3, va) && ok_a; });
+        std::thread tb([&] { for (int k = 0; k < 200; k++) ok_b = pargo::write_tune_cache(p3, vb) && ok_b; });
+        int seen_bad = 0;
+        for (int k = 0; k < 200; k++) {
+            const std::vector<TuneEntry> got = pargo::read_tune_cache(p3);
+            const bool whole = got.empty() || (got.size() == 3 && got[0].op == "a") || (got.size() == 5 && got[0].op == "b");
+            seen_bad += whole ? 0 : 1;
+        }
+        ta.join();
+        tb.join();
+        CHECK(ok_a && ok_b);
+        CHECK(seen_bad == 0);
+        CHECK(files_in(dir + "/c") == 1);
+    }
 
     // the cache path: PARGO_TUNE_CACHE (empty: no cache), else XDG_CACHE_HOME, else HOME
     setenv("PARGO_TUNE_CACHE", "/x/y.json", 1);
