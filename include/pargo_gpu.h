@@ -352,12 +352,12 @@ pargo_status pargo_slope_loss_grad(pargo_ctx* ctx, const pargo_raster* z, const 
  * the array (21 bytes per cell, ~22 MB) stays allocated on every GPU that loads
  * the library until the process exits.  All calls share that array: calls that
  * overlap on the GPU race, so serialise them.  The first call on a device looks
- * up the array's address (once per device); make it before any stream capture.
- * The address is kept until the process exits, so calls after cudaDeviceReset
- * are not supported.  Layout rules as elsewhere (pitch a whole number of
- * elements covering a row, data aligned to its element size; otherwise
- * PARGO_ERR_INVALID_ARG).  Synchronous: returns after the result and the
- * completion count are known. */
+ * up the array's address (once per device) and keeps it until the process
+ * exits, so calls after cudaDeviceReset are not supported.  Layout rules as
+ * elsewhere (pitch a whole number of elements covering a row, data aligned to
+ * its element size; otherwise PARGO_ERR_INVALID_ARG).  Synchronous: returns
+ * after the result and the completion count are known, so it must not be
+ * called on a stream that is being captured. */
 #define PARGO_SCA_NOALLOC_MAX_CELLS (1LL << 20)
 pargo_status pargo_sca_noalloc(const pargo_raster* d8, pargo_raster* sca, const pargo_nbr* nbr, int contract,
                                void* stream);

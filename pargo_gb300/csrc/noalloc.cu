@@ -19,14 +19,13 @@
 //    rewritten by that call before it is read (the in-degree pass rewrites all
 //    per-cell scratch, the counters are cleared with a memset).
 // The first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (once per device, with that device current); make that
-// first call before any stream capture begins.  The address is kept for the
-// life of the process: after cudaDeviceReset (which unloads the library's
-// device image) the cached address is stale, so calls after a reset are not
-// supported.
+// cudaGetSymbolAddress (once per device, with that device current).  The
+// address is kept for the life of the process: after cudaDeviceReset (which
+// unloads the library's device image) the cached address is stale, so calls
+// after a reset are not supported.
 //
 // Every call is synchronous: it waits on `stream` for the completion count
-// before it returns.
+// before it returns, so it cannot be called on a stream being captured.
 
 #include <math.h>
 
