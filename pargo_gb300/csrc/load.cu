@@ -20,7 +20,7 @@
 //
 // Row loads (DeComposition::valRowDcmp, gpro/deComposition.h:320-335): per
 // compute row, the left-to-right FP64 sum of the cells that are above -9999
-// and above nodata by more than 1e-7; one thread per row.
+// and above nodata by more than 1e-7; one warp per row.
 
 #include "common.cuh"
 #include "kernels.h"
@@ -130,17 +130,47 @@ __global__ void __launch_bounds__(256) compute_load_count_kernel(const LoadParam
     }
 }
 
-__global__ void __launch_bounds__(128) row_load_kernel(const InView load, int64_t crows, int64_t ccols, double nodata,
-                                                       double* row_load) {
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < crows; r += (int64_t)gridDim.x * blockDim.x) {
+__device__ __forceinline__ double load_at(const InView& load, const char* row, int64_t c) {
+    return load.dtype == PARGO_F64 ? reinterpret_cast<const double*>(row)[c]
+                                   : (double)reinterpret_cast<const float*>(row)[c];
+}
+__device__ __forceinline__ bool row_counts(double v, double nodata) {
+    return __dadd_rn(v, 9999.0) > 0.0000001 && __dsub_rn(v, nodata) > 0.0000001;
+}
+
+// One warp per compute row, lanes over its columns (coalesced).  When every
+// value the row counts is an integer of magnitude below int_bound (2^53 over
+// the row's length), every partial sum of the reference's left-to-right FP64
+// sum is an integer below 2^53, exact, so that sum equals the integer sum
+// the lanes form in any order; otherwise lane 0 adds the row in order.
+__global__ void __launch_bounds__(256) row_load_kernel(const InView load, int64_t crows, int64_t ccols, double nodata,
+                                                       double int_bound, double* row_load) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < crows; r += nwarps) {
         const char* row = load.base + r * load.pitch;
-        double acc = 0.0;
-        for (int64_t c = 0; c < ccols; c++) {
-            const double v = load.dtype == PARGO_F64 ? reinterpret_cast<const double*>(row)[c]
-                                                     : (double)reinterpret_cast<const float*>(row)[c];
-            if (__dadd_rn(v, 9999.0) > 0.0000001 && __dsub_rn(v, nodata) > 0.0000001) acc = __dadd_rn(acc, v);
+        long long isum = 0;
+        bool exact = true;
+        for (int64_t c = lane; c < ccols; c += 32) {
+            const double v = load_at(load, row, c);
+            if (!row_counts(v, nodata)) continue;
+            if (v == floor(v) && fabs(v) < int_bound) isum += (long long)v;
+            else exact = false;
         }
-        row_load[r] = acc;
+        exact = __all_sync(0xffffffffu, exact);
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) isum += __shfl_xor_sync(0xffffffffu, isum, o);
+        if (lane == 0) {
+            double acc = (double)isum;
+            if (!exact) {
+                acc = 0.0;
+                for (int64_t c = 0; c < ccols; c++) {
+                    const double v = load_at(load, row, c);
+                    if (row_counts(v, nodata)) acc = __dadd_rn(acc, v);
+                }
+            }
+            row_load[r] = acc;
+        }
     }
 }
 
@@ -178,9 +208,10 @@ cudaError_t launch_compute_load(const LoadParams& p, int num_sms, cudaStream_t s
 cudaError_t launch_row_load(const InView& load, int64_t crows, int64_t ccols, double nodata, double* row_load,
                             int num_sms, cudaStream_t s) {
     if (crows == 0) return cudaSuccess;
-    int64_t blocks = (crows + 127) / 128;
+    int64_t blocks = (crows + 7) / 8;  // a warp per compute row
     if (blocks > (int64_t)num_sms * 8) blocks = (int64_t)num_sms * 8;
-    row_load_kernel<<<(unsigned)blocks, 128, 0, s>>>(load, crows, ccols, nodata, row_load);
+    const double int_bound = 9007199254740992.0 / (double)(ccols > 0 ? ccols : 1);
+    row_load_kernel<<<(unsigned)blocks, 256, 0, s>>>(load, crows, ccols, nodata, int_bound, row_load);
     return cudaGetLastError();
 }
 

@@ -76,6 +76,19 @@ def test_decomposition_matches_oracle(shape, grain, ring, nparts, ctx, oracle_li
     assert np.array_equal(comp2, oc) and np.array_equal(bounds2, ob)
 
 
+@pytest.mark.parametrize("loads,dt", [((0.3, 1.7), np.float64), ((0.0, 1.0), np.float32), ((0.25, 3.0), np.float32)])
+def test_decomposition_of_fractional_and_float32_layers(loads, dt, ctx, oracle_lib):
+    """Row loads summed in the reference's order where they are fractional
+    (the warp's integer sum applies only to integer-valued rows), and from a
+    float32 compute layer."""
+    shape, grain, ring, nparts = (1200, 1333), 10, True, 8
+    dem = _dem(shape, 31)
+    load = oracle_lib.compute_load(dem, ND, grain, loads[0], loads[1], ring).astype(dt)
+    oc, ob = oracle_lib.load_decompose(load.astype(np.float64), ND, shape, nparts, ring)
+    comp, bounds = ctx.load_decompose(abi.raster(dev(load), ND), shape, nparts, ring)
+    assert np.array_equal(comp, oc) and np.array_equal(bounds, ob)
+
+
 def test_rejects_bad_arguments(ctx):
     dem = dev(_dem((50, 60), 1))
     cr, cc = abi.compute_load_dims(50, 60, 4)
