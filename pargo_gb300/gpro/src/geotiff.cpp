@@ -7,6 +7,9 @@
 // (42113); the GeoKey tags (34735-34737) are carried through untouched.
 // Writes little-endian uncompressed float32 or float64 strips with the same
 // tags, as the reference's GTiff output (gpro/rasterLayer.h:957-995) carries them.
+// The file is read in one call and decoded a strip or tile row at a time (rows
+// of a little-endian file as plain copies on a little-endian host); the writer
+// streams its samples through a fixed buffer after the header.
 #include <cstdio>
 
 #include "gpro/gpro.h"
@@ -71,15 +74,66 @@ double sample(const Reader& r, size_t o, int bits, int fmt) {
     }
 }
 
+// Little-endian host: samples of a little-endian file are copied as they lie.
+bool host_little_endian() {
+    const uint16_t one = 1;
+    unsigned char c;
+    memcpy(&c, &one, 1);
+    return c == 1;
+}
+
+// n consecutive samples starting at byte o into dst; the same values as
+// sample() one by one, with the common little-endian cases as plain copies.
+void samples(const Reader& r, size_t o, size_t n, int bits, int fmt, double* dst) {
+    const unsigned char* p = r.b.data() + o;
+    if (!r.big && host_little_endian()) {
+        if (bits == 32 && fmt == 3) {
+            for (size_t k = 0; k < n; k++) {
+                float v;
+                memcpy(&v, p + 4 * k, 4);
+                dst[k] = v;
+            }
+            return;
+        }
+        if (bits == 64 && fmt == 3) {
+            memcpy(dst, p, 8 * n);
+            return;
+        }
+        if (bits == 16 && fmt == 2) {
+            for (size_t k = 0; k < n; k++) {
+                int16_t v;
+                memcpy(&v, p + 2 * k, 2);
+                dst[k] = v;
+            }
+            return;
+        }
+        if (bits == 32 && fmt == 2) {
+            for (size_t k = 0; k < n; k++) {
+                int32_t v;
+                memcpy(&v, p + 4 * k, 4);
+                dst[k] = v;
+            }
+            return;
+        }
+    }
+    for (size_t k = 0; k < n; k++) dst[k] = sample(r, o + k * ((size_t)bits / 8), bits, fmt);
+}
+
 }  // namespace
 
 bool read_geotiff(const char* path, GeoRaster* out, std::string* err) {
-    std::ifstream f(path, std::ios::binary);
+    std::ifstream f(path, std::ios::binary | std::ios::ate);
     if (!f) {
         *err = std::string("cannot open ") + path;
         return false;
     }
-    std::vector<unsigned char> b((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    const std::streamoff fsize = f.tellg();
+    std::vector<unsigned char> b(fsize > 0 ? (size_t)fsize : 0);
+    f.seekg(0);
+    if (!b.empty() && !f.read(reinterpret_cast<char*>(b.data()), (std::streamsize)b.size())) {
+        *err = std::string(path) + ": read failed";
+        return false;
+    }
     if (b.size() < 8 || !((b[0] == 'I' && b[1] == 'I') || (b[0] == 'M' && b[1] == 'M'))) {
         *err = std::string(path) + ": not a TIFF file";
         return false;
@@ -160,6 +214,7 @@ bool read_geotiff(const char* path, GeoRaster* out, std::string* err) {
             const size_t base = (size_t)num(so, s);
             const int r0 = (int)s * per;
             const int nr = std::min(per, g.rows - r0);
+            if (nr <= 0) break;  // strips past the last row carry nothing
             const size_t need = (size_t)nr * g.cols * bpp;
             if (sbc && (size_t)num(sbc, s) < need) {
                 *err = std::string(path) + ": short strip";
@@ -169,9 +224,7 @@ bool read_geotiff(const char* path, GeoRaster* out, std::string* err) {
                 *err = std::string(path) + ": truncated strip";
                 return false;
             }
-            for (int i = 0; i < nr; i++)
-                for (int j = 0; j < g.cols; j++)
-                    g.values[(size_t)(r0 + i) * g.cols + j] = sample(r, base + ((size_t)i * g.cols + j) * bpp, bits, fmt);
+            samples(r, base, (size_t)nr * g.cols, bits, fmt, g.values.data() + (size_t)r0 * g.cols);
         }
     } else if (to) {
         const Entry* tw = find(322);
@@ -189,12 +242,10 @@ bool read_geotiff(const char* path, GeoRaster* out, std::string* err) {
                 *err = std::string(path) + ": truncated tile";
                 return false;
             }
-            for (int i = 0; i < TL; i++)
-                for (int j = 0; j < TW; j++) {
-                    const int rr = ty * TL + i, cc = tx * TW + j;
-                    if (rr < g.rows && cc < g.cols)
-                        g.values[(size_t)rr * g.cols + cc] = sample(r, base + ((size_t)i * TW + j) * bpp, bits, fmt);
-                }
+            const int nc = std::min(TW, g.cols - tx * TW);
+            for (int i = 0; i < TL && ty * TL + i < g.rows; i++)
+                samples(r, base + (size_t)i * TW * bpp, (size_t)nc, bits, fmt,
+                        g.values.data() + (size_t)(ty * TL + i) * g.cols + (size_t)tx * TW);
         }
     } else {
         *err = std::string(path) + ": no strips or tiles";
@@ -303,8 +354,8 @@ bool write_geotiff(const char* path, const GeoRaster& m, const double* values, i
     const size_t data_off = (cursor + 15) & ~(size_t)15;
     for (uint32_t s = 0; s < nstrips; s++) offs[s] = (uint32_t)(data_off + (size_t)s * per * rowbytes);
     memcpy(w.entries[5].data.data(), offs.data(), 4 * (size_t)nstrips);  // tag 273
-    std::vector<unsigned char> out;
-    out.reserve(data_off + total);
+    std::vector<unsigned char> out;  // header, IFD and tag values; the samples are streamed after them
+    out.reserve(data_off);
     out.push_back('I');
     out.push_back('I');
     put16(out, 42);
@@ -332,24 +383,27 @@ bool write_geotiff(const char* path, const GeoRaster& m, const double* values, i
         }
     }
     out.resize(data_off, 0);
-    for (size_t i = 0; i < (size_t)m.rows * m.cols; i++) {
-        if (bpp == 4) {
-            const float v = (float)values[i];
-            unsigned char c[4];
-            memcpy(c, &v, 4);
-            out.insert(out.end(), c, c + 4);
-        } else {
-            unsigned char c[8];
-            memcpy(c, &values[i], 8);
-            out.insert(out.end(), c, c + 8);
-        }
-    }
     std::ofstream f(path, std::ios::binary);
     if (!f) {
         *err = std::string("cannot create ") + path;
         return false;
     }
     f.write((const char*)out.data(), (std::streamsize)out.size());
+    // the samples, little-endian, through a buffer of about 4 MB
+    const size_t n_all = (size_t)m.rows * m.cols, chunk = (size_t)1 << 19;
+    std::vector<unsigned char> buf(chunk * bpp);
+    for (size_t i0 = 0; i0 < n_all && f; i0 += chunk) {
+        const size_t n = std::min(chunk, n_all - i0);
+        if (bpp == 4) {
+            for (size_t k = 0; k < n; k++) {
+                const float v = (float)values[i0 + k];
+                memcpy(buf.data() + 4 * k, &v, 4);
+            }
+        } else {
+            memcpy(buf.data(), values + i0, 8 * n);
+        }
+        f.write((const char*)buf.data(), (std::streamsize)(n * bpp));
+    }
     return (bool)f;
 }
 
