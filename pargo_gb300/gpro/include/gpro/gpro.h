@@ -8,8 +8,9 @@
 // runs unchanged, on one GPU, in one process, without MPI or GDAL:
 //   - Application::START(any ProgramType) opens the GPU context (device from
 //     the PARGO_DEVICE environment variable, default 0);
-//   - RasterLayer reads and writes GeoTIFF itself (uncompressed strips or
-//     tiles; float/int samples), keeping the georeferencing tags;
+//   - RasterLayer reads and writes GeoTIFF itself (classic or BigTIFF,
+//     uncompressed strips or tiles; float/int samples), keeping the
+//     georeferencing tags;
 //   - a single process owns the whole raster, so every decomposition type
 //     reads the full raster and writeFile writes it (the reference's writeFile
 //     returns false for NON_DCMP, gpro/rasterLayer.h:1011-1013, which is why its
@@ -117,8 +118,11 @@ struct GeoRaster {
     std::vector<double> values;              // row-major, converted to double
 };
 bool read_geotiff(const char* path, GeoRaster* out, std::string* err);
-// Writes `values` (rows x cols doubles) as samples of `dtype` (F32 or F64).
-bool write_geotiff(const char* path, const GeoRaster& meta, const double* values, int dtype, std::string* err);
+// Writes `values` (rows x cols doubles) as samples of `dtype` (F32 or F64):
+// classic TIFF while the samples fit in it (below 4 GB), else BigTIFF, or
+// BigTIFF always when `force_bigtiff`.
+bool write_geotiff(const char* path, const GeoRaster& meta, const double* values, int dtype, std::string* err,
+                   bool force_bigtiff = false);
 
 class MetaData {
 public:
